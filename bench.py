@@ -1,0 +1,304 @@
+"""Benchmark: ms/tick of a 1M-node 3D force layout (link + many-body + centre) on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--nodes N]
+
+Workload (the metric's headline configuration): 3D, 1,000,000 nodes at the reference's
+phyllotaxis start, 1,499,999 links (random tree + 500,000 distinct random pairs, the reference
+benchmark's generator, LCG seed 42), forceLink(distance 30, strength 1/min(degree)) +
+forceManyBody(-30, theta 0.9) + forceCenter(), alpha 1, alphaDecay 1 - 0.001^(1/300),
+velocityDecay 0.4. A step is one tick. Synthetic, seeded data (no dataset is involved).
+
+  value     ms per tick, device-timed with CUDA events on the engine's stream, state resident
+  e2e       ms per tick through the C ABI with host buffers: each step uploads every position
+            from pinned host memory (fl_update_positions), queues the tick (fl_enqueue) and reads
+            positions and velocities back into pinned host memory (fl_sync)
+  roofline  the dominant kernel (the tree walk) against measured HBM bandwidth, and its FP32
+            pipe view from interaction counts
+  cpu_baseline  the oracle (FP64 C restatement of the reference's CPU simulation, one core) on
+            a bounded sample: ticks of the same 1M-node layout
+
+With --impl reference, the same workload runs on the CPU implementation (the oracle; the
+reference's own CPU code is JavaScript, and there is no Node.js on this machine).
+Multi-GPU: the single simulation does not shard; N ranks run N independent replicas.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "d3-force-3d-webgpu_gb300"))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "ms/tick at 1M nodes (3D link+charge+center)"
+UNIT = "ms/tick"
+
+# algorithmic bytes per node of one tick (link + charge + center, 1.5 links per node): state
+# read + write 64, pins 4, charge 140, link 4 + 32 per link (48 at 1.5 links/node), centre 4
+BYTES_PER_NODE_TICK = 64 + 4 + 140 + 4 + 48
+# the walk's compulsory traffic per point: its sorted point (16) and permutation entry (4),
+# the child slots of the tree read once (24 B x ~2 per point), the velocity read + write (32)
+WALK_BYTES_PER_NODE = 16 + 4 + 48 + 32
+FLOPS_PER_INTERACTION = 20  # FP32 ops per accepted cell or point interaction
+FLOPS_PER_OPEN = 8          # per opened-cell test
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--nodes", type=int, default=1_000_000)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def workload(n):
+    from forcegpu.graphs import benchmark_links, link_defaults, phyllotaxis
+    src, dst = benchmark_links(n, n // 2, seed=42)
+    bias, strength = link_defaults(n, src, dst)
+    xyz = phyllotaxis(n, 3)
+    return xyz, src, dst, bias, strength
+
+
+def alphas(k, start=1.0):
+    decay = 1 - 0.001 ** (1 / 300)
+    out, a = [], start
+    for _ in range(k):
+        a += (0 - a) * decay
+        out.append(a)
+    return np.array(out), a
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region (SM clock, max clock, throttle reasons)."""
+
+    def __init__(self):
+        self.rows, self.proc = [], None
+
+    def start(self):
+        cmd = ["nvidia-smi", "--query-gpu=clocks.sm,clocks.max.sm,power.draw,"
+               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+               "--format=csv,noheader,nounits", "-i", os.environ.get("LOCAL_RANK", "0"), "-lms", "100"]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm = [float(r[0]) for r in self.rows if len(r) >= 7 and r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if len(r) >= 7 and r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows if len(r) >= 7 for i in range(4)
+                          if r[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def cpu_baseline(xyz, src, dst, n, ticks=2):
+    """The oracle (one core) on a bounded sample: 1 warm + `ticks` timed ticks at full size."""
+    import oracle
+    o = oracle.OracleSim(n, 3, xyz=xyz)
+    o.link(src, dst, distance=30.0)
+    o.manybody(theta=0.9)
+    o.center()
+    o.tick(1)
+    t0 = time.perf_counter()
+    o.tick(ticks)
+    dt = time.perf_counter() - t0
+    return dt / ticks * 1e3, ticks
+
+
+def run_reference(args):
+    """--impl reference: the CPU implementation of the path (the oracle port), rank 0 only."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    n = args.nodes
+    xyz, src, dst, _, _ = workload(n)
+    import oracle
+    o = oracle.OracleSim(n, 3, xyz=xyz)
+    o.link(src, dst, distance=30.0)
+    o.manybody(theta=0.9)
+    o.center()
+    warm = max(1, min(args.warmup, 1))
+    steps = max(1, min(args.steps, 5))
+    o.tick(warm)
+    t0 = time.perf_counter()
+    o.tick(steps)
+    ms = (time.perf_counter() - t0) / steps * 1e3
+    line = {"metric": METRIC, "value": ms, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": steps, "warmup": warm, "ms_per_step": ms, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "3D layout, %d nodes, %d links, link+charge(theta 0.9)+center"
+                                   % (n, len(src)), "nodes": n, "links": int(len(src))},
+            "cpu_baseline": {"value": ms, "unit": UNIT, "cores": 1, "kind": "port",
+                             "sample": "ticks %d-%d of the layout, full size" % (warm + 1, warm + steps)},
+            "e2e": {"value": ms, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    import forcegpu
+    from forcegpu import Engine
+    from forcegpu._lib import Q_DEVICE_BYTES, Q_LAUNCHES, desc_from_gpu
+
+    n = args.nodes
+    xyz, src, dst, bias, strength = workload(n)
+    pos4 = np.zeros((n, 4), np.float32)
+    pos4[:, :3] = xyz
+    eng = Engine(local)
+    eng.set_nodes(pos4, 3)
+    links = {"type": "link", "version": 1, "source": src, "target": dst, "iterations": 1,
+             "strengths": strength, "distances": np.full(len(src), 30.0), "bias": bias}
+    d_link, keep_l = desc_from_gpu(links, 1, n)
+    charge = {"type": "manyBody", "version": 1, "strengths": np.full(n, -30.0), "distanceMin2": 1.0,
+              "distanceMax2": math.inf, "theta2": 0.81}
+    d_charge, keep_c = desc_from_gpu(charge, 2, n)
+    d_center, keep_x = desc_from_gpu({"type": "center", "x": 0, "y": 0, "z": 0, "strength": 1.0}, 3, n)
+    descs = [(d_link, keep_l), (d_charge, keep_c), (d_center, keep_x)]
+    eng.set_forces(descs)
+    eng.set_seed(12345)
+    decay = 0.6
+    total = args.warmup + args.steps
+    al, _ = alphas(total + 2 * args.steps + 8)
+
+    stream = torch.cuda.ExternalStream(eng.stream(), device=local)
+    # warm-up
+    eng.enqueue(al[:args.warmup], decay)
+    eng.idle()
+
+    # timed region: K ticks, state resident, CUDA events on the engine's stream
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    eng.profile(True)
+    launches0 = eng.query(Q_LAUNCHES)
+    clocks = Clocks()
+    clocks.start()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    eng.enqueue(al[args.warmup:total], decay)
+    e1.record(stream)
+    eng.idle()
+    barrier()
+    clk = clocks.stop()
+    ms_total = e0.elapsed_time(e1)
+    launches = eng.query(Q_LAUNCHES) - launches0
+    prof = eng.profile_read()
+    eng.profile(False)
+    if world > 1:
+        t = torch.tensor([ms_total], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_tick = ms_total / args.steps
+    value = ms_total / (args.steps * world)
+
+    # e2e through the C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        hp = torch.empty((n, 4), dtype=torch.float32, pin_memory=True)
+        hv = torch.empty((n, 4), dtype=torch.float32, pin_memory=True)
+        eng.sync_into(hp.data_ptr(), hv.data_ptr())
+        hpn = hp.numpy()
+        k = args.steps
+        a2 = al[total:total + k]
+        barrier()
+        t0 = time.perf_counter()
+        for i in range(k):
+            eng.update_positions(0, hpn)
+            eng.enqueue(a2[i:i + 1], decay)
+            eng.sync_into(hp.data_ptr(), hv.data_ptr())
+        barrier()
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / k
+        if world > 1:
+            t = torch.tensor([e2e_ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            e2e_ms = float(t.item())
+        e2e = {"value": e2e_ms / world, "unit": UNIT, "h2d_bytes_per_step": 16 * n + 8,
+               "d2h_bytes_per_step": 32 * n}
+
+    dev_bytes = eng.query(Q_DEVICE_BYTES)
+    peaks, peak_kind = measured_peaks()
+    walk_ms, walk_n = prof.get("walk", (0.0, 0))
+    walk_avg = walk_ms / max(1, walk_n)
+    walk_bytes = WALK_BYTES_PER_NODE * n
+    achieved = walk_bytes / (walk_avg * 1e-3) / 1e9 if walk_avg else None
+    roof = {"bound": "hbm", "kernel": "k_walk", "achieved": achieved, "peak": peaks["hbm_gbs"],
+            "unit": "GB/s", "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
+            "traffic": None, "peak_kind": peak_kind,
+            "algorithmic_bytes_per_launch": walk_bytes, "avg_launch_ms": walk_avg,
+            "tick_bytes": BYTES_PER_NODE_TICK * n,
+            "tick_hbm_frac": BYTES_PER_NODE_TICK * n / (ms_tick * 1e-3) / 1e9 / peaks["hbm_gbs"]}
+    kernels = {k: {"ms_per_tick": v[0] / args.steps, "launches": v[1]} for k, v in prof.items()}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_tick, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "3D layout, %d nodes, %d links, link+charge(theta 0.9)+center, "
+                                   "ticks %d-%d from the phyllotaxis start" % (n, len(src), args.warmup + 1, total),
+                       "nodes": n, "links": int(len(src)), "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "working set %.0f MB > 126 MB L2 (no flush)" % (dev_bytes / 1e6)},
+            "gpu_launches": int(launches), "clocks": clk, "roofline": roof, "kernels": kernels}
+    if e2e:
+        line["e2e"] = e2e
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        ms_cpu, t = cpu_baseline(xyz, src, dst, n)
+        line["cpu_baseline"] = {"value": ms_cpu, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": "ticks 2-%d of the same 1M-node layout (oracle, FP64, one core)" % (1 + t),
+                                "host_cores": os.cpu_count()}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

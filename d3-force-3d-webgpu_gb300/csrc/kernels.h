@@ -1,0 +1,125 @@
+// Host-side launchers of the engine's kernels (one translation unit each group).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+// ---------------------------------------------------------------- radix sort (sort.cu)
+// Stable LSD sort of (uint64 key, uint32 value) pairs on the key bits [lo_bit, 64), 8 bits per
+// pass: one histogram pass fused into the key producer (or run on its own), then one onesweep
+// pass per digit (warp match ranking, decoupled look-back over tiles, staged coalesced scatter).
+struct FlSortBufs {
+  uint64_t* keys[2];
+  uint32_t* vals[2];
+  uint32_t* hist;      // [8][256] digit counts per pass
+  uint32_t* status;    // [8][tiles][256] look-back words
+  uint32_t* counters;  // [8] tile tickets
+  int64_t cap;         // pairs the buffers hold
+  int64_t tiles_cap;
+};
+int fl_sort_tile();  // pairs per onesweep tile
+size_t fl_sort_bytes(int64_t n);
+// Carve the buffers out of one allocation of fl_sort_bytes(n) bytes.
+void fl_sort_carve(FlSortBufs* b, void* base, int64_t n);
+// Zero the histogram, the tickets and the look-back words for `passes` passes.
+void fl_sort_reset(const FlSortBufs* b, int64_t n, int passes, cudaStream_t st);
+// Histogram of the keys in keys[0] (when the producer did not fuse it).
+void fl_sort_histogram(const FlSortBufs* b, int64_t n, int lo_bit, cudaStream_t st, int64_t* launches);
+// Run the passes from keys[0]/vals[0]; returns which buffer (0/1) holds the result.
+int fl_sort_passes(const FlSortBufs* b, int64_t n, int lo_bit, uint32_t* err, cudaStream_t st,
+                   int64_t* launches);
+
+// Single-pass exclusive scan of n uint32 values (decoupled look-back); out[i] = base + sum(in[<i]).
+size_t fl_scan_bytes(int64_t n);
+void fl_scan_exclusive(const uint32_t* in, uint32_t* out, int64_t n, uint32_t base, void* scratch,
+                       uint32_t* err, cudaStream_t st, int64_t* launches);
+
+// ---------------------------------------------------------------- state kernels (state.cu)
+void fl_launch_reduce(const float4* pos, int n, int ndim, int want_box, int want_sum,
+                      FlReduce* red, cudaStream_t st);
+void fl_launch_center_apply(float4* pos, int n, int ndim, const FlReduce* red, double cx,
+                            double cy, double cz, double strength, cudaStream_t st);
+// v *= decay; p += v; pinned axes: p = fix, v = 0. When red != NULL, first shifts p by the
+// centre force of (cx, cy, cz, strength) computed from red->sum (the centre force fused).
+void fl_launch_integrate(float4* pos, float4* vel, const float4* fix, const uint32_t* mask, int n,
+                         int ndim, float decay, const FlReduce* red, double cx, double cy,
+                         double cz, double strength, cudaStream_t st);
+void fl_launch_radial(const float4* pos, float4* vel, const float* radius, const float* strength,
+                      int n, int ndim, float cx, float cy, float cz, float alpha, cudaStream_t st);
+void fl_launch_position(const float4* pos, float4* vel, const float* target, const float* strength,
+                        int n, int axis, float alpha, cudaStream_t st);
+
+// ---------------------------------------------------------------- link (link.cu)
+struct FlLinkCsr {
+  const int32_t* row;      // [n + 1]
+  const float4* entry;     // [2m] (other node as int bits, distance, strength, bias share)
+  const uint32_t* code;    // [2m] link * 2 + (this node is the target)
+};
+void fl_launch_link(const float4* pos, const float4* vel_in, float4* vel_out, FlLinkCsr csr, int n,
+                    int ndim, float alpha, uint32_t step, uint32_t seed, cudaStream_t st);
+
+// ---------------------------------------------------------------- many-body (tree.cu)
+struct FlTreeBufs {
+  int n, ndim, levels, bits;
+  uint32_t* left;        // [n-1] child: internal index, or 0x80000000 | sorted leaf
+  uint32_t* right;       // [n-1]
+  uint32_t* parent;      // [n-1] parent of internal nodes; [0] unused
+  uint32_t* leaf_parent; // [n]
+  uint32_t* range;       // [2(n-1)] first, last sorted leaf of each internal node
+  uint8_t* depth;        // [n-1] d3 depth of each internal node's cell
+  uint32_t* count;       // [n-1] children of a head (0 for other nodes)
+  uint32_t* first;       // [n-1] first child slot of a head
+  uint32_t* flag;        // [n-1] bottom-up arrival counters
+  float4* cell;          // [n-1] head: centroid, value at its own depth
+  float4* leaf;          // [n] sorted points: position, strength
+  float4* child_data;    // [2n] slot: centroid or position, value at own depth / strength
+  uint2* child_meta;     // [2n] slot: (first child slot, count | depth << 26) or (sorted index, ~0)
+  void* scan_scratch;
+};
+struct FlWalkParams {
+  float thresh[32];   // (cube size / 2^k)^2 / theta^2
+  float damp[32];     // sqrt(4 / 2^dims)^j
+  float dmin2, dmax2;
+  int ndim;
+  uint32_t step, seed;
+};
+size_t fl_tree_bytes(int64_t n);
+void fl_tree_carve(FlTreeBufs* t, void* base, int64_t n, int ndim);
+// Bounding box -> d3 cube -> Morton keys (left-aligned) + values = node index, fused with the
+// sort's digit histogram. Also sets the walk's per-depth thresholds on the device.
+void fl_launch_morton(const float4* pos, int n, int ndim, const FlReduce* red, uint64_t* keys,
+                      uint32_t* vals, uint32_t* hist, int lo_bit, float* cube_out,
+                      cudaStream_t st);
+// Karras build + sorted leaves (position, strength) gather.
+void fl_launch_build(const FlTreeBufs* t, const uint64_t* skeys, const uint32_t* perm,
+                     const float4* pos, const float* strength, cudaStream_t st, int64_t* launches);
+// Heads, child counts, child slots, bottom-up d3 aggregation.
+void fl_launch_aggregate(const FlTreeBufs* t, uint32_t* err, cudaStream_t st, int64_t* launches);
+void fl_launch_walk(const FlTreeBufs* t, const uint32_t* perm, const float* cube, float4* vel,
+                    float alpha, double theta2, double dmin2, double dmax2, uint32_t step,
+                    uint32_t seed, uint32_t* err, cudaStream_t st);
+// Exact all-pairs sum (theta ~ 0): O(n^2), tiled through shared memory.
+void fl_launch_allpairs(const float4* pos, const float* strength, float4* vel, int n, int ndim,
+                        float alpha, float dmin2, float dmax2, uint32_t step, uint32_t seed,
+                        cudaStream_t st);
+
+// ---------------------------------------------------------------- collide (collide.cu)
+void fl_launch_collide_allpairs(const float4* pos, const float4* vel_in, float4* vel_out,
+                                const float* radius, int n, int ndim, float strength,
+                                uint32_t step, uint32_t seed, cudaStream_t st);
+struct FlGridBufs {
+  int n, bits;
+  uint32_t* starts;   // [2^bits] run start per slot (validated against the sorted keys)
+  float4* sorted;     // [n] sorted snapshot position, radius
+};
+size_t fl_grid_bytes(int64_t n);
+void fl_grid_carve(FlGridBufs* g, void* base, int64_t n);
+void fl_launch_grid_keys(const float4* pos, const float4* vel, int n, int ndim, float inv_cell,
+                         int bits, uint64_t* keys, uint32_t* vals, uint32_t* hist, int lo_bit,
+                         cudaStream_t st);
+void fl_launch_grid_query(const FlGridBufs* g, const uint64_t* skeys, const uint32_t* perm,
+                          const float4* pos, const float4* vel_in, float4* vel_out,
+                          const float* radius, int ndim, float inv_cell, float strength,
+                          uint32_t step, uint32_t seed, cudaStream_t st, int64_t* launches);

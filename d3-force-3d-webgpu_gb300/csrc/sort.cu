@@ -1,0 +1,326 @@
+// Onesweep LSD radix sort of (uint64 key, uint32 value) pairs, and a single-pass exclusive scan.
+//
+// Replaces the reference's three-dispatch-per-digit sort (src/gpu/sort.js:4-20, 139-190) with
+// the GB300 form of Adinets & Merrill's "Onesweep" (2022): the digit histograms of every pass
+// come from one read of the keys (fused into the key producer where possible); each pass is one
+// kernel that ranks a tile of 4096 keys by digit with warp match (__match_any_sync), publishes
+// the tile's digit counts, and takes its global offsets from a decoupled look-back over the
+// preceding tiles (bounded: a wait gives up after FL_SPIN_LIMIT polls and raises an error bit
+// instead of hanging); keys are then staged in shared memory in digit order and written out in
+// coalesced runs. Stable: keys of equal digit keep their input order.
+#include "kernels.h"
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kItems = 16;
+constexpr int kTile = kThreads * kItems;
+constexpr uint32_t kValMask = (1u << 30) - 1;
+constexpr uint32_t kFlagAgg = 1u << 30;
+constexpr uint32_t kFlagPre = 2u << 30;
+
+// Block-wide exclusive scan of one value per thread (256 threads); returns the exclusive prefix,
+// and the block total in *total.
+__device__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_warp, uint32_t* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(FL_FULL, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < kWarps ? s_warp[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(FL_FULL, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < kWarps) s_warp[lane] = w;  // inclusive totals of warps
+  }
+  __syncthreads();
+  uint32_t before = (warp ? s_warp[warp - 1] : 0) + x - v;
+  *total = s_warp[kWarps - 1];
+  __syncthreads();
+  return before;
+}
+
+__global__ void __launch_bounds__(256) k_hist(const uint64_t* __restrict__ keys, int64_t n,
+                                              int lo_bit, int passes, uint32_t* hist) {
+  __shared__ uint32_t sh[8 * 256];
+  for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) sh[i] = 0;
+  __syncthreads();
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+    int64_t i = base + threadIdx.x;
+    bool ok = i < n;
+    uint64_t k = ok ? keys[i] : 0;
+    for (int p = 0; p < passes; ++p) {
+      uint32_t d = ok ? (uint32_t)(k >> (lo_bit + 8 * p)) & 255u : 256u + (threadIdx.x & 31);
+      uint32_t peers = __match_any_sync(FL_FULL, d);
+      if (ok && (int)(threadIdx.x & 31) == 31 - __clz(peers)) atomicAdd(&sh[p * 256 + d], __popc(peers));
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < passes * 256; i += blockDim.x)
+    if (sh[i]) atomicAdd(&hist[i], sh[i]);
+}
+
+__global__ void __launch_bounds__(kThreads) k_onesweep(
+    const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
+    uint32_t* __restrict__ vout, int64_t n, int shift, const uint32_t* __restrict__ ghist,
+    uint32_t* status, uint32_t* ticket, uint32_t* err) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint64_t* sk = reinterpret_cast<uint64_t*>(smem);
+  uint32_t* sv = reinterpret_cast<uint32_t*>(sk + kTile);
+  __shared__ uint32_t s_whist[kWarps][256];
+  __shared__ uint32_t s_gexcl[256];
+  __shared__ uint32_t s_texcl[256];
+  __shared__ uint32_t s_base[256];
+  __shared__ uint32_t s_warp[kWarps];
+  __shared__ uint32_t s_tile;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) s_tile = atomicAdd(ticket, 1u);
+  for (int i = tid; i < kWarps * 256; i += kThreads) (&s_whist[0][0])[i] = 0;
+  uint32_t total;
+  s_gexcl[tid] = block_excl_scan(ghist[tid], s_warp, &total);  // syncs inside
+  const uint32_t tile = s_tile;
+  const int64_t tbase = (int64_t)tile * kTile;
+
+  uint64_t key[kItems];
+  uint32_t val[kItems], dig[kItems], rank[kItems];
+  const int64_t wbase = tbase + (int64_t)warp * (32 * kItems);
+#pragma unroll
+  for (int j = 0; j < kItems; ++j) {
+    int64_t idx = wbase + j * 32 + lane;
+    if (idx < n) {
+      key[j] = kin[idx];
+      val[j] = vin[idx];
+      dig[j] = (uint32_t)(key[j] >> shift) & 255u;
+    } else {
+      key[j] = 0;
+      val[j] = 0;
+      dig[j] = 256u + lane;  // unique: ranked alone, never stored
+    }
+  }
+  const uint32_t lt = fl::lanemask_lt();
+#pragma unroll
+  for (int j = 0; j < kItems; ++j) {
+    uint32_t peers = __match_any_sync(FL_FULL, dig[j]);
+    int leader = 31 - __clz(peers);
+    uint32_t before = 0;
+    if (lane == leader && dig[j] < 256u) {
+      before = s_whist[warp][dig[j]];
+      s_whist[warp][dig[j]] = before + __popc(peers);
+    }
+    before = __shfl_sync(FL_FULL, before, leader);
+    rank[j] = before + __popc(peers & lt);
+    __syncwarp();
+  }
+  __syncthreads();
+
+  // per digit (one thread each): exclusive prefix over warps, the tile's count
+  const uint32_t d = tid;
+  uint32_t run = 0;
+#pragma unroll
+  for (int w = 0; w < kWarps; ++w) {
+    uint32_t t = s_whist[w][d];
+    s_whist[w][d] = run;
+    run += t;
+  }
+  uint32_t* mine = status + (size_t)tile * 256 + d;
+  fl::st_relaxed(mine, (tile == 0 ? kFlagPre : kFlagAgg) | run);
+  s_texcl[d] = block_excl_scan(run, s_warp, &total);
+
+  uint32_t prefix = 0;
+  if (tile > 0) {
+    int64_t p = (int64_t)tile - 1;
+    uint32_t spins = 0;
+    for (;;) {
+      uint32_t w = fl::ld_relaxed(status + (size_t)p * 256 + d);
+      uint32_t f = w & ~kValMask;
+      if (f == 0) {
+        if (++spins > FL_SPIN_LIMIT) {
+          atomicOr(err, FL_ERR_LOOKBACK);
+          break;
+        }
+        if (spins > 64) __nanosleep(100);
+        continue;
+      }
+      prefix += w & kValMask;
+      if (f == kFlagPre || p == 0) break;
+      --p;
+    }
+    fl::st_relaxed(mine, kFlagPre | (prefix + run));
+  }
+  s_base[d] = s_gexcl[d] + prefix - s_texcl[d];
+  __syncthreads();
+
+#pragma unroll
+  for (int j = 0; j < kItems; ++j) {
+    if (dig[j] < 256u) {
+      uint32_t pos = s_texcl[dig[j]] + s_whist[warp][dig[j]] + rank[j];
+      sk[pos] = key[j];
+      sv[pos] = val[j];
+    }
+  }
+  __syncthreads();
+  const int valid = (int)((n - tbase) < kTile ? (n - tbase) : kTile);
+  for (int i = tid; i < valid; i += kThreads) {
+    uint64_t k = sk[i];
+    uint32_t g = s_base[(uint32_t)(k >> shift) & 255u] + (uint32_t)i;
+    if (g < (uint64_t)n) {  // always true unless a look-back gave up (reported in err)
+      kout[g] = k;
+      vout[g] = sv[i];
+    }
+  }
+}
+
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kThreads * kScanItems;
+
+__global__ void __launch_bounds__(kThreads) k_scan(const uint32_t* __restrict__ in,
+                                                   uint32_t* __restrict__ out, int64_t n,
+                                                   uint32_t base, uint32_t* status,
+                                                   uint32_t* ticket, uint32_t* err) {
+  __shared__ uint32_t s_warp[kWarps];
+  __shared__ uint32_t s_tile, s_prefix;
+  const int tid = threadIdx.x;
+  if (tid == 0) s_tile = atomicAdd(ticket, 1u);
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  const int64_t first = (int64_t)tile * kScanTile + (int64_t)tid * kScanItems;
+  uint32_t v[kScanItems], sum = 0;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    v[j] = first + j < n ? in[first + j] : 0;
+    sum += v[j];
+  }
+  uint32_t total;
+  uint32_t before = block_excl_scan(sum, s_warp, &total);
+  if (tid == 0) {
+    uint32_t* mine = status + tile;
+    fl::st_relaxed(mine, (tile == 0 ? kFlagPre : kFlagAgg) | total);
+    uint32_t prefix = 0;
+    if (tile > 0) {
+      int64_t p = (int64_t)tile - 1;
+      uint32_t spins = 0;
+      for (;;) {
+        uint32_t w = fl::ld_relaxed(status + p);
+        uint32_t f = w & ~kValMask;
+        if (f == 0) {
+          if (++spins > FL_SPIN_LIMIT) {
+            atomicOr(err, FL_ERR_LOOKBACK);
+            break;
+          }
+          if (spins > 64) __nanosleep(100);
+          continue;
+        }
+        prefix += w & kValMask;
+        if (f == kFlagPre || p == 0) break;
+        --p;
+      }
+      fl::st_relaxed(mine, kFlagPre | (prefix + total));
+    }
+    s_prefix = prefix;
+  }
+  __syncthreads();
+  uint32_t acc = base + s_prefix + before;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    if (first + j < n) out[first + j] = acc;
+    acc += v[j];
+  }
+}
+
+inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+int64_t tiles_for(int64_t n) { return (n + kTile - 1) / kTile; }
+
+}  // namespace
+
+int fl_sort_tile() { return kTile; }
+
+size_t fl_sort_bytes(int64_t n) {
+  int64_t cap = n > 0 ? n : 1, tiles = tiles_for(cap);
+  return 2 * align256(8 * (size_t)cap) + 2 * align256(4 * (size_t)cap) + align256(8 * 256 * 4) +
+         align256(8 * (size_t)tiles * 256 * 4) + align256(8 * 4);
+}
+
+void fl_sort_carve(FlSortBufs* b, void* base, int64_t n) {
+  int64_t cap = n > 0 ? n : 1, tiles = tiles_for(cap);
+  char* p = static_cast<char*>(base);
+  for (int i = 0; i < 2; ++i) b->keys[i] = reinterpret_cast<uint64_t*>(p), p += align256(8 * (size_t)cap);
+  for (int i = 0; i < 2; ++i) b->vals[i] = reinterpret_cast<uint32_t*>(p), p += align256(4 * (size_t)cap);
+  b->hist = reinterpret_cast<uint32_t*>(p), p += align256(8 * 256 * 4);
+  b->status = reinterpret_cast<uint32_t*>(p), p += align256(8 * (size_t)tiles * 256 * 4);
+  b->counters = reinterpret_cast<uint32_t*>(p);
+  b->cap = cap;
+  b->tiles_cap = tiles;
+}
+
+void fl_sort_reset(const FlSortBufs* b, int64_t n, int passes, cudaStream_t st) {
+  int64_t tiles = tiles_for(n > 0 ? n : 1);
+  if (tiles == b->tiles_cap) {  // histogram, look-back words and tickets are contiguous
+    const char* a = reinterpret_cast<const char*>(b->hist);
+    const char* e = reinterpret_cast<const char*>(b->counters) + 8 * 4;
+    cudaMemsetAsync(b->hist, 0, (size_t)(e - a), st);
+    return;
+  }
+  cudaMemsetAsync(b->hist, 0, 8 * 256 * 4, st);
+  cudaMemsetAsync(b->counters, 0, 8 * 4, st);
+  for (int p = 0; p < passes; ++p)
+    cudaMemsetAsync(b->status + (size_t)p * b->tiles_cap * 256, 0, (size_t)tiles * 256 * 4, st);
+}
+
+void fl_sort_histogram(const FlSortBufs* b, int64_t n, int lo_bit, cudaStream_t st,
+                       int64_t* launches) {
+  int passes = (64 - lo_bit + 7) / 8;
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 4 * 152) blocks = 4 * 152;
+  if (blocks < 1) blocks = 1;
+  k_hist<<<(int)blocks, 256, 0, st>>>(b->keys[0], n, lo_bit, passes, b->hist);
+  ++*launches;
+}
+
+int fl_sort_passes(const FlSortBufs* b, int64_t n, int lo_bit, uint32_t* err, cudaStream_t st,
+                   int64_t* launches) {
+  static bool configured = false;
+  const size_t dyn = (size_t)kTile * 12;
+  if (!configured) {
+    cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    configured = true;
+  }
+  int passes = (64 - lo_bit + 7) / 8;
+  int cur = 0;
+  int64_t tiles = tiles_for(n);
+  if (n <= 0) return 0;
+  for (int p = 0; p < passes; ++p) {
+    k_onesweep<<<(int)tiles, kThreads, dyn, st>>>(
+        b->keys[cur], b->vals[cur], b->keys[1 - cur], b->vals[1 - cur], n, lo_bit + 8 * p,
+        b->hist + p * 256, b->status + (size_t)p * b->tiles_cap * 256, b->counters + p, err);
+    ++*launches;
+    cur = 1 - cur;
+  }
+  return cur;
+}
+
+size_t fl_scan_bytes(int64_t n) {
+  int64_t tiles = (n + kScanTile - 1) / kScanTile + 1;
+  return align256(4 * (size_t)tiles) + 256;
+}
+
+void fl_scan_exclusive(const uint32_t* in, uint32_t* out, int64_t n, uint32_t base, void* scratch,
+                       uint32_t* err, cudaStream_t st, int64_t* launches) {
+  if (n <= 0) return;
+  int64_t tiles = (n + kScanTile - 1) / kScanTile;
+  uint32_t* status = static_cast<uint32_t*>(scratch);
+  uint32_t* ticket = status + align256(4 * (size_t)(tiles + 1)) / 4;
+  cudaMemsetAsync(scratch, 0, align256(4 * (size_t)(tiles + 1)) + 4, st);
+  k_scan<<<(int)tiles, kThreads, 0, st>>>(in, out, n, base, status, ticket, err);
+  ++*launches;
+}

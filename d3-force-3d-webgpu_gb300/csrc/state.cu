@@ -1,0 +1,192 @@
+// Per-node streaming kernels: the bounding-box / centre reduction, the centre shift, the fused
+// integrate, and the per-node forces (radial, x/y/z). All HBM-bound; one float4 per node.
+#include "kernels.h"
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline int grid_for(int n, int per_block) {
+  int g = (n + per_block - 1) / per_block;
+  if (g < 1) g = 1;
+  return g;
+}
+
+// Bounding box (ordered-uint atomics) and FP64 sum of the positions, one pass.
+// d3 computes the cube from the extent of the points (d3-octree cover) and the centre force
+// sums positions in FP64 (src/center.js:8-26); both come from this one read.
+__global__ void __launch_bounds__(kThreads) k_reduce(const float4* __restrict__ pos, int n,
+                                                     int ndim, int want_box, int want_sum,
+                                                     FlReduce* red) {
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  double sum[3] = {0, 0, 0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float4 p = pos[i];
+    float c[3] = {p.x, p.y, p.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      lo[k] = fminf(lo[k], c[k]);
+      hi[k] = fmaxf(hi[k], c[k]);
+      sum[k] += (double)c[k];
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[k] = fminf(lo[k], __shfl_xor_sync(FL_FULL, lo[k], o));
+      hi[k] = fmaxf(hi[k], __shfl_xor_sync(FL_FULL, hi[k], o));
+      sum[k] += __shfl_xor_sync(FL_FULL, sum[k], o);
+    }
+  }
+  __shared__ float s_lo[3][kThreads / 32], s_hi[3][kThreads / 32];
+  __shared__ double s_sum[3][kThreads / 32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0)
+    for (int k = 0; k < 3; ++k) s_lo[k][warp] = lo[k], s_hi[k][warp] = hi[k], s_sum[k][warp] = sum[k];
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    int k = threadIdx.x;
+    float a = INFINITY, b = -INFINITY;
+    double s = 0;
+    for (int w = 0; w < kThreads / 32; ++w) a = fminf(a, s_lo[k][w]), b = fmaxf(b, s_hi[k][w]), s += s_sum[k][w];
+    if (k < ndim) {
+      if (want_box) {  // lo holds ~ordered(min), so a zeroed record is an empty box
+        atomicMax(&red->lo[k], ~fl::ordered(a));
+        atomicMax(&red->hi[k], fl::ordered(b));
+      }
+      if (want_sum) atomicAdd(&red->sum[k], s);
+    }
+  }
+}
+
+__device__ __forceinline__ void center_shift(const FlReduce* red, int n, int ndim, double cx,
+                                             double cy, double cz, double strength, double* sh) {
+  double c[3] = {cx, cy, cz};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) sh[k] = k < ndim ? (red->sum[k] / n - c[k]) * strength : 0.0;
+}
+
+__global__ void k_center_apply(float4* __restrict__ pos, int n, int ndim, const FlReduce* red,
+                               double cx, double cy, double cz, double strength) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double sh[3];
+  center_shift(red, n, ndim, cx, cy, cz, strength, sh);
+  float4 p = pos[i];
+  p.x = (float)((double)p.x - sh[0]);
+  p.y = (float)((double)p.y - sh[1]);
+  p.z = (float)((double)p.z - sh[2]);
+  pos[i] = p;
+}
+
+// src/simulation.js:61-73 (and src/gpu/wgsl.js INTEGRATE): v *= decay; p += v; a pinned axis
+// takes p = fixed, v = 0. With the centre force fused (it was the last force), positions are
+// first shifted by it, as the reference applies it before integrating.
+__global__ void __launch_bounds__(kThreads) k_integrate(float4* __restrict__ pos,
+                                                        float4* __restrict__ vel,
+                                                        const float4* __restrict__ fix,
+                                                        const uint32_t* __restrict__ mask, int n,
+                                                        int ndim, float decay, const FlReduce* red,
+                                                        double cx, double cy, double cz,
+                                                        double strength) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 p = pos[i], v = vel[i];
+  if (red) {
+    double sh[3];
+    center_shift(red, n, ndim, cx, cy, cz, strength, sh);
+    p.x = (float)((double)p.x - sh[0]);
+    p.y = (float)((double)p.y - sh[1]);
+    p.z = (float)((double)p.z - sh[2]);
+  }
+  uint32_t m = mask[i];
+  v.x *= decay, v.y *= decay, v.z *= decay;
+  p.x += v.x, p.y += v.y, p.z += v.z;
+  if (m) {
+    float4 f = fix[i];
+    if (m & 1u) p.x = f.x, v.x = 0.f;
+    if (m & 2u) p.y = f.y, v.y = 0.f;
+    if (m & 4u) p.z = f.z, v.z = 0.f;
+  }
+  if (ndim < 3) p.z = 0.f, v.z = 0.f;
+  if (ndim < 2) p.y = 0.f, v.y = 0.f;
+  p.w = 0.f, v.w = 0.f;
+  pos[i] = p;
+  vel[i] = v;
+}
+
+__device__ __forceinline__ float or1e6(float v) { return v != 0.f ? v : 1e-6f; }
+
+// forceRadial (src/radial.js:16-28): d = p - c with exact-zero components replaced by 1e-6;
+// v += d * (r_i - |d|) * s_i * alpha / |d|. Axes beyond numDimensions still enter |d| as
+// (0 - c)||1e-6, as in the reference's CPU force (they are never moved).
+__global__ void __launch_bounds__(kThreads) k_radial(const float4* __restrict__ pos,
+                                                     float4* __restrict__ vel,
+                                                     const float* __restrict__ radius,
+                                                     const float* __restrict__ strength, int n,
+                                                     int ndim, float cx, float cy, float cz,
+                                                     float alpha) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 p = pos[i];
+  float dx = or1e6(p.x - cx);
+  float dy = or1e6((ndim > 1 ? p.y : 0.f) - cy);
+  float dz = or1e6((ndim > 2 ? p.z : 0.f) - cz);
+  float r = sqrtf(dx * dx + dy * dy + dz * dz);
+  float k = (radius[i] - r) * strength[i] * alpha / r;
+  float4 v = vel[i];
+  v.x += dx * k;
+  if (ndim > 1) v.y += dy * k;
+  if (ndim > 2) v.z += dz * k;
+  vel[i] = v;
+}
+
+// forceX / forceY / forceZ (src/x.js:12-16): v[axis] += (target_i - p[axis]) * s_i * alpha.
+__global__ void __launch_bounds__(kThreads) k_position(const float4* __restrict__ pos,
+                                                       float4* __restrict__ vel,
+                                                       const float* __restrict__ target,
+                                                       const float* __restrict__ strength, int n,
+                                                       int axis, float alpha) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float p = axis == 0 ? pos[i].x : axis == 1 ? pos[i].y : pos[i].z;
+  float dv = (target[i] - p) * strength[i] * alpha;
+  float4 v = vel[i];
+  if (axis == 0) v.x += dv;
+  else if (axis == 1) v.y += dv;
+  else v.z += dv;
+  vel[i] = v;
+}
+
+}  // namespace
+
+void fl_launch_reduce(const float4* pos, int n, int ndim, int want_box, int want_sum,
+                      FlReduce* red, cudaStream_t st) {
+  int g = grid_for(n, kThreads * 8);
+  if (g > 4 * 152) g = 4 * 152;
+  k_reduce<<<g, kThreads, 0, st>>>(pos, n, ndim, want_box, want_sum, red);
+}
+
+void fl_launch_center_apply(float4* pos, int n, int ndim, const FlReduce* red, double cx,
+                            double cy, double cz, double strength, cudaStream_t st) {
+  k_center_apply<<<grid_for(n, kThreads), kThreads, 0, st>>>(pos, n, ndim, red, cx, cy, cz, strength);
+}
+
+void fl_launch_integrate(float4* pos, float4* vel, const float4* fix, const uint32_t* mask, int n,
+                         int ndim, float decay, const FlReduce* red, double cx, double cy,
+                         double cz, double strength, cudaStream_t st) {
+  k_integrate<<<grid_for(n, kThreads), kThreads, 0, st>>>(pos, vel, fix, mask, n, ndim, decay, red,
+                                                          cx, cy, cz, strength);
+}
+
+void fl_launch_radial(const float4* pos, float4* vel, const float* radius, const float* strength,
+                      int n, int ndim, float cx, float cy, float cz, float alpha, cudaStream_t st) {
+  k_radial<<<grid_for(n, kThreads), kThreads, 0, st>>>(pos, vel, radius, strength, n, ndim, cx, cy,
+                                                       cz, alpha);
+}
+
+void fl_launch_position(const float4* pos, float4* vel, const float* target, const float* strength,
+                        int n, int axis, float alpha, cudaStream_t st) {
+  k_position<<<grid_for(n, kThreads), kThreads, 0, st>>>(pos, vel, target, strength, n, axis, alpha);
+}

@@ -1,0 +1,173 @@
+/*
+ * forcegpu.h -- C ABI of the GB300 force-layout engine (libforcegpu.so).
+ *
+ * The drop-in boundary for the per-tick hot path of forceSimulationGPU: every entry point here
+ * replaces one call of the reference's WebGPU engine (paths within erw-1/d3-force-3d-webgpu),
+ * which the JavaScript facade (src/gpu/simulation.js) drives. Plain C types only: the caller
+ * owns host arrays, which are copied during the call; no pointer is kept after a call returns.
+ * Every function returns an FL_* status; fl_last_error() gives the message of the last failure.
+ * A simulation is single-caller; separate simulations may be used from separate threads.
+ *
+ * Node state layout (as the reference's GPU buffers, src/gpu/wgsl.js:1-10): positions and
+ * velocities are float4 per node (x, y, z, unused w), so arrays are 4*n floats. Axes beyond
+ * numDimensions stay 0. Pins: fix is float4 per node (fx, fy, fz, -), mask bit 1/2/4 = axis
+ * x/y/z pinned (src/gpu/engine.js:131-134).
+ */
+#ifndef FORCEGPU_H
+#define FORCEGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FL_ABI_VERSION 1
+
+/* Status codes. The reference reports failures by rejecting a Promise or falling back to the
+ * CPU (src/gpu/engine.js:50-59, src/gpu/simulation.js:112-116); this engine has no CPU path. */
+enum {
+  FL_OK = 0,
+  FL_E_ARG = 1,         /* invalid argument: sizes, a link endpoint out of range, bad type */
+  FL_E_OOM = 2,         /* a device allocation failed */
+  FL_E_DEVICE = 3,      /* a CUDA call failed (no device, launch error, ...) */
+  FL_E_TIMEOUT = 4,     /* a bounded device-side wait (scan look-back) gave up */
+  FL_E_OVERFLOW = 5,    /* a device-side capacity was exceeded (tree walk stack) */
+  FL_E_STATE = 6,       /* not valid in this state (no nodes, destroyed) */
+  FL_E_UNSUPPORTED = 7  /* a force type with no GPU pass: the reference hands such a
+                           simulation to the CPU (src/gpu/engine.js:41-48); here it is an error */
+};
+
+/* Force types: the `type` of force.gpu() (src/gpu/passes/index.js:8-16). */
+enum {
+  FL_FORCE_MANYBODY = 1, /* src/manyBody.js:142-144   {strengths, distanceMin2, distanceMax2, theta2} */
+  FL_FORCE_LINK = 2,     /* src/link.js:127-129       {links, iterations, strengths, distances, bias} */
+  FL_FORCE_COLLIDE = 3,  /* src/collide.js:134-136    {radii, strength, iterations} */
+  FL_FORCE_CENTER = 4,   /* src/center.js:49-51       {x, y, z, strength} */
+  FL_FORCE_RADIAL = 5,   /* src/radial.js:69-71       {radiuses, strengths, x, y, z} */
+  FL_FORCE_POSITION = 6  /* src/x.js:43-45 (y.js, z.js) {axis, targets, strengths} */
+};
+
+/* One force's descriptor, the C form of force.gpu(). Arrays are read only when `version`
+ * differs from the version the engine last saw for the same `key` (the reference re-uploads on
+ * a version change, e.g. src/gpu/passes/manyBody.js:98-106); scalars are read on every call. */
+typedef struct fl_force_desc {
+  int32_t type;           /* FL_FORCE_* */
+  uint32_t version;       /* bumped by the force whenever its per-node / per-link values change */
+  uint64_t key;           /* identity of the force object: its pass (and uploads) persist while
+                             a force with this key and type stays in the list (engine.js:320-328) */
+  const float* node_a;    /* [n] manyBody strengths | collide radii | radial radiuses |
+                                 position targets */
+  const float* node_b;    /* [n] radial strengths | position strengths */
+  int32_t m;              /* link: number of links */
+  const int32_t* source;  /* link: [m] source node index */
+  const int32_t* target;  /* link: [m] target node index */
+  const float* link_distance; /* link: [m] */
+  const float* link_strength; /* link: [m] */
+  const float* link_bias;     /* link: [m] bias of the target end (src/link.js:73-75) */
+  int32_t iterations;     /* link, collide */
+  int32_t axis;           /* position: 0 = x, 1 = y, 2 = z */
+  double distance_min2;   /* manyBody */
+  double distance_max2;   /* manyBody (may be +inf) */
+  double theta2;          /* manyBody; <= 1e-6 selects the exact all-pairs sum */
+  double strength;        /* collide, center */
+  double x, y, z;         /* center, radial */
+} fl_force_desc;
+
+typedef struct fl_sim fl_sim;
+
+/* Device-resident state, for a renderer that draws without a readback: the reference's
+ * gpuBuffers() (src/gpu/engine.js:416-420), with CUDA device pointers in place of GPUBuffers. */
+typedef struct fl_buffer_info {
+  void* positions;  /* float4 per node, device memory */
+  void* velocities; /* float4 per node, device memory */
+  int32_t count;
+  int32_t stride;   /* 16 */
+} fl_buffer_info;
+
+/* Create an engine on a CUDA device (replaces requestDevice + createEngine,
+ * src/gpu/device.js:19-39, src/gpu/engine.js:73). */
+int32_t fl_create(int32_t device, fl_sim** out);
+/* Release every device buffer (engine.destroy, src/gpu/engine.js:422-427). NULL is allowed. */
+int32_t fl_destroy(fl_sim* sim);
+/* Message of the last failed call on this simulation (or of the last fl_create failure when
+ * sim is NULL). The string lives until the next call on the same simulation. */
+const char* fl_last_error(const fl_sim* sim);
+
+/* Whether `count` nodes fit this device (engine.fits, src/gpu/engine.js:332-338). */
+int32_t fl_fits(fl_sim* sim, int64_t count, int32_t* fits);
+
+/* Replace the node set and upload it (engine.setNodes + uploadAll, src/gpu/engine.js:115-145,
+ * :267-310). pos4/vel4/fix4 are 4*n floats; vel4, fix4 and mask may be NULL (zeros). The
+ * forces must be set again afterwards, as in the reference. n may be 0. */
+int32_t fl_set_nodes(fl_sim* sim, int32_t n, int32_t ndim, const float* pos4, const float* vel4,
+                     const float* fix4, const uint32_t* mask);
+/* Upload nodes [first, first + count) that the caller moved (uploadPositions,
+ * src/gpu/engine.js:147-156): 4*count floats. */
+int32_t fl_update_positions(fl_sim* sim, int32_t first, int32_t count, const float* pos4);
+/* Upload changed pins of nodes [first, first + count) (uploadPinned, src/gpu/engine.js:158-169). */
+int32_t fl_update_pins(fl_sim* sim, int32_t first, int32_t count, const float* fix4,
+                       const uint32_t* mask);
+/* Overwrite velocities of nodes [first, first + count). No counterpart in the reference, whose
+ * GPU owns velocities (docs/differences.md:18); used to start a run from a captured state. */
+int32_t fl_update_velocities(fl_sim* sim, int32_t first, int32_t count, const float* vel4);
+
+/* The forces, in application order (engine.setForces, src/gpu/engine.js:312-330). */
+int32_t fl_set_forces(fl_sim* sim, int32_t count, const fl_force_desc* descs);
+
+/* Seed of the coincident-node jiggle (engine.setSeed, src/gpu/engine.js:340-343). */
+int32_t fl_set_seed(fl_sim* sim, uint32_t seed);
+
+/* Queue `count` ticks without waiting (engine.enqueue, src/gpu/engine.js:351-391). alphas are the
+ * host-computed alpha of each tick (src/gpu/simulation.js:141-151); decay is the velocity
+ * multiplier, 1 - velocityDecay. */
+int32_t fl_enqueue(fl_sim* sim, const double* alphas, int32_t count, double decay);
+/* Wait for every queued tick, then copy positions and velocities (4*n floats each; either may
+ * be NULL) into the caller's arrays (engine.sync + readback, src/gpu/engine.js:218-239,
+ * :406-414). Reports a device-side error raised by any tick since the previous sync. */
+int32_t fl_sync(fl_sim* sim, float* pos4_out, float* vel4_out);
+/* Wait for every queued tick, no readback (engine.idle, src/gpu/engine.js:401-404). */
+int32_t fl_idle(fl_sim* sim);
+/* Whether queued work is still running (engine.busy, src/gpu/engine.js:393-396). */
+int32_t fl_busy(fl_sim* sim, int32_t* busy);
+/* Device pointers of the state (engine.buffers). */
+int32_t fl_buffers(fl_sim* sim, fl_buffer_info* out);
+
+/* ---- measurement (no reference counterpart: the reference times only with performance.now()
+ *      around tickAsync, examples/benchmark.html:105-132) ---- */
+
+/* The cudaStream_t every kernel of this simulation runs on. */
+int32_t fl_stream(fl_sim* sim, void** stream);
+/* Queries: FL_Q_LAUNCHES kernels launched so far, FL_Q_TICKS ticks queued so far, FL_Q_NODES,
+ * FL_Q_ERRWORD the raw device error word, FL_Q_DEVICE_BYTES device memory held. */
+enum { FL_Q_LAUNCHES = 1, FL_Q_TICKS = 2, FL_Q_NODES = 3, FL_Q_ERRWORD = 4, FL_Q_DEVICE_BYTES = 5 };
+int32_t fl_query(fl_sim* sim, int32_t what, int64_t* out);
+/* Per-kernel timing with CUDA events on the simulation's stream: enable, then read the summed
+ * milliseconds and launch count of each kernel group since it was enabled. */
+int32_t fl_profile(fl_sim* sim, int32_t enable);
+/* Fills up to `cap` entries; returns the number of groups in *count. Names live as long as sim. */
+int32_t fl_profile_read(fl_sim* sim, int32_t cap, const char** names, double* ms,
+                        int64_t* launches, int32_t* count);
+
+/* ---- integer stages, exposed for bit-exact checks against a CPU rebuild ---- */
+
+/* Stable LSD radix sort of n (key, value) pairs on key bits [lo_bit, 64), the engine's sort on
+ * its own (the reference's createSort, src/gpu/sort.js:139-190, tested alone by
+ * test/gpu-sort-test.js). Host arrays in and out; device memory is allocated for the call.
+ * Runs on the calling thread's current CUDA device. */
+int32_t fl_radix_sort(const uint64_t* keys, const uint32_t* vals, int64_t n, int32_t lo_bit,
+                      uint64_t* keys_out, uint32_t* vals_out);
+
+/* The many-body tree the last tick built for force `index` of the list (a Barnes-Hut pass,
+ * src/gpu/passes/barnesHut.js:934-1126): sorted left-aligned Morton keys [n], the sort
+ * permutation [n] (node index per sorted position), and per internal node [n-1] its children
+ * (0x80000000 | sorted index for a point) and d3 depth; cube = {origin x, y, z, size, log2 size}.
+ * Any output may be NULL. */
+int32_t fl_debug_tree(fl_sim* sim, int32_t index, uint64_t* keys, uint32_t* perm, uint32_t* left,
+                      uint32_t* right, uint8_t* depth, float* cube5);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
