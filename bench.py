@@ -55,7 +55,7 @@ FLOPS_PER_OPEN = 8          # per opened-cell test
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--steps", type=int, default=300)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--nodes", type=int, default=1_000_000)
@@ -84,31 +84,34 @@ def alphas(k, start=1.0):
 class Clocks:
     """nvidia-smi samples during the timed region (SM clock, max clock, throttle reasons)."""
 
+    CMD = ["nvidia-smi", "--query-gpu=clocks.sm,clocks.max.sm,power.draw,"
+           "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+           "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+           "--format=csv,noheader,nounits"]
+
     def __init__(self):
-        self.rows, self.proc = [], None
+        self.rows, self.thread, self.done = [], None, threading.Event()
 
     def start(self):
-        cmd = ["nvidia-smi", "--query-gpu=clocks.sm,clocks.max.sm,power.draw,"
-               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
-               "--format=csv,noheader,nounits", "-i", os.environ.get("LOCAL_RANK", "0"), "-lms", "100"]
-        try:
-            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            threading.Thread(target=self._read, daemon=True).start()
-        except OSError:
-            self.proc = None
+        cmd = self.CMD + ["-i", os.environ.get("LOCAL_RANK", "0")]
 
-    def _read(self):
-        for line in self.proc.stdout:
-            self.rows.append([c.strip() for c in line.split(",")])
+        def poll():
+            while not self.done.is_set():
+                try:
+                    out = subprocess.run(cmd, capture_output=True, text=True, timeout=5).stdout
+                except (OSError, subprocess.TimeoutExpired):
+                    return
+                for line in out.splitlines():
+                    self.rows.append([c.strip() for c in line.split(",")])
+                self.done.wait(0.05)
+
+        self.thread = threading.Thread(target=poll, daemon=True)
+        self.thread.start()
 
     def stop(self):
-        if self.proc:
-            self.proc.terminate()
-            try:
-                self.proc.wait(timeout=2)
-            except subprocess.TimeoutExpired:
-                self.proc.kill()
+        self.done.set()
+        if self.thread:
+            self.thread.join(timeout=6)
         sm = [float(r[0]) for r in self.rows if len(r) >= 7 and r[0].replace(".", "").isdigit()]
         mx = [float(r[1]) for r in self.rows if len(r) >= 7 and r[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]

@@ -258,6 +258,8 @@ int32_t update_pass(fl_sim* s, Pass* p, const fl_force_desc* d) {
   p->d.source = p->d.target = nullptr;
   p->d.link_distance = p->d.link_strength = p->d.link_bias = nullptr;
   if (d->iterations < 0) return fail(s, FL_E_ARG, "iterations must be >= 0");
+  if (!p->red.p) FL_CK(s, p->red.alloc(sizeof(FlReduce)));  // every pass may reduce
+  if (!p->cube.p) FL_CK(s, p->cube.alloc(64));
   if (!changed) return FL_OK;
   int32_t rc = FL_OK;
   switch (d->type) {
