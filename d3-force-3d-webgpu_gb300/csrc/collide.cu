@@ -137,11 +137,8 @@ __global__ void __launch_bounds__(kThreads) k_grid_keys(const float4* __restrict
       keys[i] = key;
       vals[i] = (uint32_t)i;
     }
-    for (int p = 0; p < passes; ++p) {
-      uint32_t d = ok ? (uint32_t)(key >> (lo_bit + 8 * p)) & 255u : 256u + (threadIdx.x & 31);
-      uint32_t peers = __match_any_sync(FL_FULL, d);
-      if (ok && (int)(threadIdx.x & 31) == 31 - __clz(peers)) atomicAdd(&sh[p * 256 + d], __popc(peers));
-    }
+    for (int p = 0; p < passes; ++p)
+      fl::hist_add(sh + p * 256, (uint32_t)(key >> (lo_bit + 8 * p)) & 255u, ok);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < passes * 256; i += blockDim.x)
@@ -237,7 +234,7 @@ void fl_launch_grid_keys(const float4* pos, const float4* vel, int n, int ndim, 
                          int bits, uint64_t* keys, uint32_t* vals, uint32_t* hist, int lo_bit,
                          cudaStream_t st) {
   int g = (n + kThreads - 1) / kThreads;
-  if (g > 8 * 152) g = 8 * 152;
+  if (g > 2 * 152) g = 2 * 152;  // few blocks: each flushes its histograms with global atomics
   if (g < 1) g = 1;
   k_grid_keys<<<g, kThreads, 0, st>>>(pos, vel, n, ndim, inv_cell, bits, keys, vals, hist, lo_bit);
 }

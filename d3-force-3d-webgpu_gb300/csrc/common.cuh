@@ -62,6 +62,20 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
+// Add one key's digit to a shared histogram, from a whole warp (all lanes call it; `ok` marks
+// the lanes with a key). When every key of the warp has the same digit (typical of the high
+// digits of spatially ordered keys) one atomic adds them all; otherwise each lane adds its own.
+__device__ __forceinline__ void hist_add(uint32_t* sh, uint32_t d, bool ok) {
+  const uint32_t lo = __reduce_min_sync(FL_FULL, ok ? d : 0xffffffffu);
+  const uint32_t hi = __reduce_max_sync(FL_FULL, ok ? d : 0u);
+  if (lo == hi) {
+    const uint32_t cnt = __popc(__ballot_sync(FL_FULL, ok));
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(&sh[lo], cnt);
+  } else if (ok) {
+    atomicAdd(&sh[d], 1u);
+  }
+}
+
 // Relaxed 32-bit load that bypasses L1 (for flags written by other SMs).
 __device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
   uint32_t v;

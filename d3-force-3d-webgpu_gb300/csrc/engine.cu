@@ -73,6 +73,9 @@ struct Pass {
   DevMem cube;
   int alloc_n = -1;
   int sorted_in = -1;  // sort buffer holding the last tick's sorted pairs (-1: no tree yet)
+  bool mixed = false;  // many-body strengths of both signs (cells need the full recursion)
+  float sign = -1.f;   // the one sign of the strengths otherwise
+  int fx_exp = 32;     // scale exponent of the fixed-point cell sums
 };
 
 struct ProfRec {
@@ -101,6 +104,8 @@ struct fl_sim {
   uint32_t seed = 0, step = 0;
   int64_t ticks = 0, launches = 0;
   bool profiling = false;
+  int prof_level = 0;
+  DevMem wstats;  // walk counters (profiling level 2)
   std::vector<ProfRec> prof_pending;
   std::vector<cudaEvent_t> ev_pool;
   double prof_ms[G_COUNT] = {};
@@ -263,9 +268,23 @@ int32_t update_pass(fl_sim* s, Pass* p, const fl_force_desc* d) {
   if (!changed) return FL_OK;
   int32_t rc = FL_OK;
   switch (d->type) {
-    case FL_FORCE_MANYBODY:
+    case FL_FORCE_MANYBODY: {
       rc = upload_nodes(s, p->a, d->node_a, -30.f, true);
+      bool neg = !d->node_a, pos = false;
+      double smax = d->node_a ? 0.0 : 30.0;
+      if (d->node_a)
+        for (int32_t i = 0; i < s->n; ++i) {
+          const float v = d->node_a[i];
+          if (!std::isfinite(v)) continue;
+          neg = neg || v < 0.f, pos = pos || v > 0.f;
+          smax = std::max(smax, (double)std::fabs(v));
+        }
+      p->mixed = neg && pos;
+      p->sign = neg ? -1.f : 1.f;
+      // the largest point weight |s| c^leafDepth: c < 1 in 3D, 1 in 2D, sqrt(2) in 1D
+      p->fx_exp = fl_fixed_exponent(s->n, smax * (s->ndim == 1 ? 8192.0 : 1.0));
       break;
+    }
     case FL_FORCE_LINK:
       rc = upload_links(s, p, d);
       break;
@@ -340,18 +359,20 @@ void encode_manybody(fl_sim* s, Pass* p, float alpha, const FlReduce* box) {
   }
   {
     Scope sc(s, G_BUILD);
-    fl_launch_build(t, p->sb.keys[r], p->sb.vals[r], s->pos.as<float4>(), strength, s->st,
-                    &s->launches);
+    fl_launch_build(t, p->sb.keys[r], p->sb.vals[r], s->pos.as<float4>(), strength, !p->mixed,
+                    p->cube.as<float>(), p->fx_exp, s->st, &s->launches);
   }
   {
     Scope sc(s, G_AGGREGATE);
-    fl_launch_aggregate(t, s->errw.as<uint32_t>(), s->st, &s->launches);
+    fl_launch_aggregate(t, !p->mixed, p->sign, p->cube.as<float>(), p->fx_exp,
+                        s->errw.as<uint32_t>(), s->st, &s->launches);
   }
   {
     Scope sc(s, G_WALK);
     fl_launch_walk(t, p->sb.vals[r], p->cube.as<float>(), vel_cur(s), alpha, p->d.theta2,
                    p->d.distance_min2, p->d.distance_max2, s->step, s->seed,
-                   s->errw.as<uint32_t>(), s->st);
+                   s->errw.as<uint32_t>(),
+                   s->prof_level >= 2 ? s->wstats.as<unsigned long long>() : nullptr, s->st);
     ++s->launches;
   }
 }
@@ -743,6 +764,17 @@ int32_t fl_query(fl_sim* s, int32_t what, int64_t* out) {
       *out = (int64_t)b;
       break;
     }
+    case FL_Q_WALK_TESTS:
+    case FL_Q_WALK_USEFUL:
+    case FL_Q_WALK_MAX_STACK: {
+      unsigned long long w[3] = {0, 0, 0};
+      if (s->wstats.p) {
+        FL_CK(s, cudaStreamSynchronize(s->st));
+        FL_CK(s, cudaMemcpy(w, s->wstats.p, 24, cudaMemcpyDeviceToHost));
+      }
+      *out = (int64_t)w[what - FL_Q_WALK_TESTS];
+      break;
+    }
     default: return fail(s, FL_E_ARG, "unknown query");
   }
   return FL_OK;
@@ -754,7 +786,12 @@ int32_t fl_profile(fl_sim* s, int32_t enable) {
   FL_CK(s, cudaStreamSynchronize(s->st));
   drain_profile(s);
   s->profiling = enable != 0;
+  s->prof_level = enable;
   for (int g = 0; g < G_COUNT; ++g) s->prof_ms[g] = 0, s->prof_count[g] = 0;
+  if (enable >= 2) {
+    if (!s->wstats.p) FL_CK(s, s->wstats.alloc(256));
+    FL_CK(s, cudaMemset(s->wstats.p, 0, 24));
+  }
   return FL_OK;
 }
 

@@ -77,6 +77,8 @@ struct FlTreeBufs {
   float4* child_data;    // [2n] slot: centroid or position, value at own depth / strength
   uint2* child_meta;     // [2n] slot: (first child slot, count | depth << 26) or (sorted index, ~0)
   void* scan_scratch;
+  double* wsum;          // [5n] per sorted point |a|, |a| x, |a| y, |a| z, a; then their prefix sums
+  double* wtiles;        // [5 tiles] partial sums of the prefix scan
 };
 struct FlWalkParams {
   float thresh[32];   // (cube size / 2^k)^2 / theta^2
@@ -92,14 +94,22 @@ void fl_tree_carve(FlTreeBufs* t, void* base, int64_t n, int ndim);
 void fl_launch_morton(const float4* pos, int n, int ndim, const FlReduce* red, uint64_t* keys,
                       uint32_t* vals, uint32_t* hist, int lo_bit, float* cube_out,
                       cudaStream_t st);
-// Karras build + sorted leaves (position, strength) gather.
+// Karras build + sorted leaves (position, strength) gather; with `closed`, the FP64 point
+// records of the closed-form cell sums.
 void fl_launch_build(const FlTreeBufs* t, const uint64_t* skeys, const uint32_t* perm,
-                     const float4* pos, const float* strength, cudaStream_t st, int64_t* launches);
-// Heads, child counts, child slots, bottom-up d3 aggregation.
-void fl_launch_aggregate(const FlTreeBufs* t, uint32_t* err, cudaStream_t st, int64_t* launches);
+                     const float4* pos, const float* strength, bool closed, const float* cube,
+                     int fx_exp, cudaStream_t st, int64_t* launches);
+// Heads, child counts and slots; cell values and centroids in closed form (strengths of one
+// sign, fixed-point sums at scale 2^fx_exp) or by the bottom-up recursion (both signs).
+void fl_launch_aggregate(const FlTreeBufs* t, bool closed, float sign, const float* cube,
+                         int fx_exp, uint32_t* err, cudaStream_t st, int64_t* launches);
+// Scale exponent of the fixed-point cell sums: no sum over n points of weight <= wmax overflows.
+int fl_fixed_exponent(int64_t n, double wmax);
+// stats (optional): [0] child tests made by the warps (32 per child), [1] of those, tests by a
+// lane whose point needed them (the d3 traversal's own work)
 void fl_launch_walk(const FlTreeBufs* t, const uint32_t* perm, const float* cube, float4* vel,
                     float alpha, double theta2, double dmin2, double dmax2, uint32_t step,
-                    uint32_t seed, uint32_t* err, cudaStream_t st);
+                    uint32_t seed, uint32_t* err, unsigned long long* stats, cudaStream_t st);
 // Exact all-pairs sum (theta ~ 0): O(n^2), tiled through shared memory.
 void fl_launch_allpairs(const float4* pos, const float* strength, float4* vel, int n, int ndim,
                         float alpha, float dmin2, float dmax2, uint32_t step, uint32_t seed,

@@ -58,11 +58,8 @@ __global__ void __launch_bounds__(256) k_hist(const uint64_t* __restrict__ keys,
     int64_t i = base + threadIdx.x;
     bool ok = i < n;
     uint64_t k = ok ? keys[i] : 0;
-    for (int p = 0; p < passes; ++p) {
-      uint32_t d = ok ? (uint32_t)(k >> (lo_bit + 8 * p)) & 255u : 256u + (threadIdx.x & 31);
-      uint32_t peers = __match_any_sync(FL_FULL, d);
-      if (ok && (int)(threadIdx.x & 31) == 31 - __clz(peers)) atomicAdd(&sh[p * 256 + d], __popc(peers));
-    }
+    for (int p = 0; p < passes; ++p)
+      fl::hist_add(sh + p * 256, (uint32_t)(k >> (lo_bit + 8 * p)) & 255u, ok);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < passes * 256; i += blockDim.x)
@@ -138,12 +135,27 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(
 
   uint32_t prefix = 0;
   if (tile > 0) {
+    // look back four tiles per round (independent loads), up to the nearest inclusive prefix
     int64_t p = (int64_t)tile - 1;
     uint32_t spins = 0;
     for (;;) {
-      uint32_t w = fl::ld_relaxed(status + (size_t)p * 256 + d);
-      uint32_t f = w & ~kValMask;
-      if (f == 0) {
+      uint32_t w[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        w[k] = p - k >= 0 ? fl::ld_relaxed(status + (size_t)(p - k) * 256 + d) : kFlagPre;
+      int used = 0;
+      bool done = false;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (done || used < k) break;
+        const uint32_t f = w[k] & ~kValMask;
+        if (f == 0) break;  // not published yet: wait for it
+        prefix += w[k] & kValMask;
+        used = k + 1;
+        done = f == kFlagPre;
+      }
+      if (done) break;
+      if (used == 0) {
         if (++spins > FL_SPIN_LIMIT) {
           atomicOr(err, FL_ERR_LOOKBACK);
           break;
@@ -151,9 +163,7 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(
         if (spins > 64) __nanosleep(100);
         continue;
       }
-      prefix += w & kValMask;
-      if (f == kFlagPre || p == 0) break;
-      --p;
+      p -= used;
     }
     fl::st_relaxed(mine, kFlagPre | (prefix + run));
   }

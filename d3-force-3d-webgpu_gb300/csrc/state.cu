@@ -20,6 +20,8 @@ __global__ void __launch_bounds__(kThreads) k_reduce(const float4* __restrict__ 
                                                      FlReduce* red) {
   float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
   double sum[3] = {0, 0, 0};
+  // a few blocks, many positions per thread: the warp shuffles and atomics of the reduction
+  // are paid once per warp, not per handful of positions
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     float4 p = pos[i];
     float c[3] = {p.x, p.y, p.z};
@@ -27,8 +29,8 @@ __global__ void __launch_bounds__(kThreads) k_reduce(const float4* __restrict__ 
     for (int k = 0; k < 3; ++k) {
       lo[k] = fminf(lo[k], c[k]);
       hi[k] = fmaxf(hi[k], c[k]);
-      sum[k] += (double)c[k];
     }
+    if (want_sum) sum[0] += (double)c[0], sum[1] += (double)c[1], sum[2] += (double)c[2];
   }
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -36,7 +38,7 @@ __global__ void __launch_bounds__(kThreads) k_reduce(const float4* __restrict__ 
     for (int o = 16; o > 0; o >>= 1) {
       lo[k] = fminf(lo[k], __shfl_xor_sync(FL_FULL, lo[k], o));
       hi[k] = fmaxf(hi[k], __shfl_xor_sync(FL_FULL, hi[k], o));
-      sum[k] += __shfl_xor_sync(FL_FULL, sum[k], o);
+      if (want_sum) sum[k] += __shfl_xor_sync(FL_FULL, sum[k], o);
     }
   }
   __shared__ float s_lo[3][kThreads / 32], s_hi[3][kThreads / 32];
@@ -60,19 +62,26 @@ __global__ void __launch_bounds__(kThreads) k_reduce(const float4* __restrict__ 
   }
 }
 
+// The centre force's shift, (mean - c) * strength per active axis, computed once per block
+// (FP64 divisions are slow on this part) and shared.
 __device__ __forceinline__ void center_shift(const FlReduce* red, int n, int ndim, double cx,
                                              double cy, double cz, double strength, double* sh) {
-  double c[3] = {cx, cy, cz};
-#pragma unroll
-  for (int k = 0; k < 3; ++k) sh[k] = k < ndim ? (red->sum[k] / n - c[k]) * strength : 0.0;
+  __shared__ double s_shift[3];
+  if (threadIdx.x < 3) {
+    const int k = threadIdx.x;
+    const double c = k == 0 ? cx : k == 1 ? cy : cz;
+    s_shift[k] = k < ndim ? (red->sum[k] / n - c) * strength : 0.0;
+  }
+  __syncthreads();
+  sh[0] = s_shift[0], sh[1] = s_shift[1], sh[2] = s_shift[2];
 }
 
 __global__ void k_center_apply(float4* __restrict__ pos, int n, int ndim, const FlReduce* red,
                                double cx, double cy, double cz, double strength) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
   double sh[3];
   center_shift(red, n, ndim, cx, cy, cz, strength, sh);
+  if (i >= n) return;
   float4 p = pos[i];
   p.x = (float)((double)p.x - sh[0]);
   p.y = (float)((double)p.y - sh[1]);
@@ -91,11 +100,11 @@ __global__ void __launch_bounds__(kThreads) k_integrate(float4* __restrict__ pos
                                                         double cx, double cy, double cz,
                                                         double strength) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double sh[3] = {0, 0, 0};
+  if (red) center_shift(red, n, ndim, cx, cy, cz, strength, sh);  // block-uniform branch
   if (i >= n) return;
   float4 p = pos[i], v = vel[i];
   if (red) {
-    double sh[3];
-    center_shift(red, n, ndim, cx, cy, cz, strength, sh);
     p.x = (float)((double)p.x - sh[0]);
     p.y = (float)((double)p.y - sh[1]);
     p.z = (float)((double)p.z - sh[2]);
@@ -163,8 +172,8 @@ __global__ void __launch_bounds__(kThreads) k_position(const float4* __restrict_
 
 void fl_launch_reduce(const float4* pos, int n, int ndim, int want_box, int want_sum,
                       FlReduce* red, cudaStream_t st) {
-  int g = grid_for(n, kThreads * 8);
-  if (g > 4 * 152) g = 4 * 152;
+  int g = grid_for(n, kThreads * 4);
+  if (g > 2 * 152) g = 2 * 152;
   k_reduce<<<g, kThreads, 0, st>>>(pos, n, ndim, want_box, want_sum, red);
 }
 

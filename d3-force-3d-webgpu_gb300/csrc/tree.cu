@@ -9,22 +9,32 @@
 //              histograms are counted in the same pass
 //   sort       onesweep radix sort of (key, node) (sort.cu)
 //   build      Karras (2012) binary radix tree over the sorted keys; each internal node's d3
-//              depth = common prefix bits / DIMS; the sorted (position, strength) of the points
+//              depth = common prefix bits / DIMS; the sorted (position, strength) of the points,
+//              and each point's d3 leaf depth (from the deeper of its two neighbour prefixes)
 //   heads      a binary node whose depth is deeper than its parent's heads a d3 cell (the binary
 //              nodes below it at the same depth are splits inside that cell); its d3 children
 //              are counted, and child slots are allocated by a scan (every cell's children are
 //              contiguous, so the walk reads them in one sweep)
-//   aggregate  bottom-up with atomic arrival flags: each cell's value and centre of mass from its
-//              children exactly as manyBody.js accumulate() does (value = sqrt(4 / 2^DIMS) * sum
-//              of the children's values; centroid weighted by |value|), through chains of
-//              one-child cells by powers of the same factor; FP64 sums for the top levels
-//   walk       one warp per 32 consecutive sorted points walks the union of their d3 traversals
-//              with a stack in shared memory; every point applies apply() of manyBody.js for
-//              itself: a cell is approximated at the first (widest) depth of its chain where
-//              w^2 / theta^2 < l, points are summed exactly, distanceMin / distanceMax as d3.
+//   cells      each cell's value and centre of mass as manyBody.js accumulate() defines them
+//              (value = sqrt(4 / 2^DIMS) times the sum of the children's values; centroid
+//              weighted by the children's |value|). When the strengths share one sign this
+//              recursion has a closed form, value(D) = sum_p s_p c^(leafDepth_p - D) and centroid
+//              weights |s_p| c^leafDepth_p, so every cell is a range sum of an FP64 prefix scan
+//              over the sorted points. With strengths of both signs the recursion itself runs,
+//              bottom-up with atomic arrival flags (FP64 sums for the top levels).
+//   slots      each cell writes its children (position or centroid, value at own depth, and for
+//              a child cell its child range and depth) into its slots
+//   walk       one warp per 32 consecutive sorted points walks the union of their d3 traversals:
+//              batches of up to 32 children are loaded lane-parallel into shared memory and
+//              every lane applies apply() of manyBody.js for its own point: a cell is
+//              approximated at the first (widest) depth of its chain where w^2 / theta^2 < l,
+//              points are summed exactly, distanceMin / distanceMax as d3; cells that some lane
+//              must open are pushed, with the mask of those lanes, on a stack in shared memory.
 //
 // Points with the same code at the finest level share the deepest cell as its children.
 #include <math.h>
+
+#include <cmath>
 
 #include "kernels.h"
 
@@ -32,12 +42,19 @@ namespace {
 
 constexpr uint32_t kLeaf = 0x80000000u;
 constexpr uint32_t kIndex = 0x7fffffffu;
-constexpr uint32_t kLeafMark = 0xffffffffu;
+constexpr uint32_t kLeafMark = 0x7fffffffu;  // meta word of a point (a cell's is count | depth << 26)
 constexpr uint32_t kCountMask = (1u << 26) - 1;
-constexpr int kFp64Depth = 6;  // cells at depths < 6 sum their children in FP64
+constexpr int kFp64Depth = 6;  // the recursion sums children in FP64 above this depth
 constexpr int kThreads = 256;
 
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+struct alignas(32) D4 {  // four exact fixed-point sums
+  long long x, y, z, w;
+};
+__host__ __device__ __forceinline__ D4 mk4(long long a, long long b, long long c, long long d) {
+  return {a, b, c, d};
+}
 
 __device__ __forceinline__ uint64_t spread3(uint64_t x) {  // 21 bits -> every third bit
   x &= 0x1fffffull;
@@ -68,6 +85,36 @@ __device__ __forceinline__ float damp(int ndim, int k) {
   const float odd = (e2 & 1) ? 1.41421356237309515f : 1.f;
   return ldexpf(odd, e2 >> 1);
 }
+__device__ __forceinline__ double damp64(int ndim, int k) {
+  const int e2 = k * (2 - ndim);
+  const double odd = (e2 & 1) ? 1.4142135623730951 : 1.0;
+  return ldexp(odd, e2 >> 1);
+}
+
+// (x - o) * 2^F as an exact integer: x - o is rounded once in FP32 and its rounding error
+// recovered exactly (Knuth's TwoSum); both parts scale exactly by the power of two 2^F.
+__device__ __forceinline__ long long fx_offset(float x, float o, float scaleF) {
+  const float s = x - o;
+  const float bb = s - x;
+  const float e = (x - (s - bb)) + (-o - bb);
+  const long long d = __float2ll_rn(s * scaleF) + __float2ll_rn(e * scaleF);
+  return d < 0 ? 0 : d;
+}
+// floor(W * D / 2^62) for W, D >= 0 (the 128-bit product's bits 62..125)
+__device__ __forceinline__ long long mulhi62(long long W, long long D) {
+  const unsigned long long hi = __umul64hi((unsigned long long)W, (unsigned long long)D);
+  const unsigned long long lo = (unsigned long long)W * (unsigned long long)D;
+  return (long long)((hi << 2) | (lo >> 62));
+}
+// 2^F of the fixed-point offsets: u = (x - origin) / size = offset / 2^62, F = 62 - log2(size)
+__device__ __forceinline__ float offset_scale(const float* cube) {
+  int F = 62 - (int)cube[4];
+  F = F < -100 ? -100 : F > 100 ? 100 : F;
+  return __int_as_float((F + 127) << 23);
+}
+
+// 4^-k as an exact float (k <= 31)
+__device__ __forceinline__ float pow4neg(uint32_t k) { return __int_as_float((127 - 2 * (int)k) << 23); }
 
 // The cell index of x at the finest level, floor((x - origin) * 2^e), in exact arithmetic:
 // e >= 0: floor(x * 2^e) and origin * 2^e are exact floats, and so is their difference, an
@@ -142,11 +189,8 @@ __global__ void __launch_bounds__(kThreads) k_morton(const float4* __restrict__ 
       keys[i] = key;
       vals[i] = (uint32_t)i;
     }
-    for (int p = 0; p < passes; ++p) {
-      uint32_t d = ok ? (uint32_t)(key >> (lo_bit + 8 * p)) & 255u : 256u + (threadIdx.x & 31);
-      uint32_t peers = __match_any_sync(FL_FULL, d);
-      if (ok && (int)(threadIdx.x & 31) == 31 - __clz(peers)) atomicAdd(&sh[p * 256 + d], __popc(peers));
-    }
+    for (int p = 0; p < passes; ++p)
+      fl::hist_add(sh + p * 256, (uint32_t)(key >> (lo_bit + 8 * p)) & 255u, ok);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < passes * 256; i += blockDim.x)
@@ -160,25 +204,71 @@ __device__ __forceinline__ int kdelta(const uint64_t* __restrict__ k, int n, uin
   return ki != kj ? __clzll(ki ^ kj) : 64 + __clz(i ^ j);
 }
 
+__device__ __forceinline__ D4 add4(D4 a, D4 b) { return mk4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+__device__ __forceinline__ D4 shfl_up4(D4 v, int o) {
+  return mk4(__shfl_up_sync(FL_FULL, v.x, o), __shfl_up_sync(FL_FULL, v.y, o),
+             __shfl_up_sync(FL_FULL, v.z, o), __shfl_up_sync(FL_FULL, v.w, o));
+}
+
+// Inclusive prefix of one D4 per thread over a 256-thread block: written to out[i] (i >= 0),
+// the block's total to tot[blockIdx.x]. Every thread of the block must call it.
+__device__ void block_prefix4(D4 v, D4* out, D4* tot, int i) {
+  __shared__ D4 s_warp[kThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    D4 y = shfl_up4(v, o);
+    if (lane >= o) v = add4(v, y);
+  }
+  if (lane == 31) s_warp[warp] = v;
+  __syncthreads();
+  if (warp) {
+    D4 b = s_warp[0];
+    for (int w = 1; w < warp; ++w) b = add4(b, s_warp[w]);
+    v = add4(v, b);
+  }
+  if (i >= 0) out[i] = v;
+  if (threadIdx.x == kThreads - 1) tot[blockIdx.x] = v;
+}
+
 // Karras (2012), "Maximizing parallelism in the construction of BVHs, octrees, and k-d trees":
 // internal node i covers sorted range [first, last] and splits it where the common prefix grows.
+// Thread i also gathers sorted point i and, for the closed-form cell sums, its record
+// (|a|, |a| u_x, |a| u_y, |a| u_z) with a = strength * c^leafDepth and u = (p - origin) / size in
+// [0, 1) the position in the d3 cube, as exact fixed point (scale 2^fx_exp, chosen so that no
+// sum over all points overflows), prefix-summed within the block. Integer sums are exact, and
+// cheap where FP64 is not.
 __global__ void __launch_bounds__(kThreads) k_build(
     const uint64_t* __restrict__ k, const uint32_t* __restrict__ perm,
     const float4* __restrict__ pos, const float* __restrict__ strength, int n, int ndim,
     uint32_t* __restrict__ left, uint32_t* __restrict__ right, uint32_t* __restrict__ parent,
     uint32_t* __restrict__ leaf_parent, uint32_t* __restrict__ range, uint8_t* __restrict__ depth,
-    float4* __restrict__ leaf) {
+    float4* __restrict__ leaf, D4* __restrict__ wsum, D4* __restrict__ wtot,
+    const float* __restrict__ cube, int fx_exp) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int L = levels_of(ndim), bits = L * ndim;
+  const uint64_t ki = i < n ? k[i] : 0;
+  const int up = i < n ? kdelta(k, n, ki, i, i + 1) : -1, dn = i < n ? kdelta(k, n, ki, i, i - 1) : -1;
+  D4 wrec = mk4(0, 0, 0, 0);
   if (i < n) {
     const uint32_t node = perm[i];
     float4 p = pos[node];
     p.w = strength[node];
     leaf[i] = p;
+    if (wsum) {
+      const int dmx = up > dn ? up : dn;
+      const int lD = (dmx >= bits ? L : dmx / ndim) + 1;  // the point's d3 leaf depth
+      const float sF = offset_scale(cube);
+      const long long W =
+          __float2ll_rn(fabsf(p.w * damp(ndim, lD)) * __int_as_float((fx_exp + 127) << 23));
+      wrec = mk4(W, mulhi62(W, fx_offset(p.x, cube[0], sF)),
+                 ndim > 1 ? mulhi62(W, fx_offset(p.y, cube[1], sF)) : 0,
+                 ndim > 2 ? mulhi62(W, fx_offset(p.z, cube[2], sF)) : 0);
+    }
   }
+  if (wsum)  // block-uniform
+    block_prefix4(wrec, wsum, wtot, i < n ? i : -1);
   if (i >= n - 1) return;
-  const int L = levels_of(ndim), bits = L * ndim;
-  const uint64_t ki = k[i];
-  const int up = kdelta(k, n, ki, i, i + 1), dn = kdelta(k, n, ki, i, i - 1);
   const int d = up > dn ? 1 : -1;
   const int dmin = up > dn ? dn : up;
   int64_t lmax = 2;
@@ -207,53 +297,170 @@ __global__ void __launch_bounds__(kThreads) k_build(
   depth[i] = (uint8_t)(dep > L ? L : dep);
 }
 
-// Whether internal node i heads a d3 cell, and how many d3 children that cell has.
+// Frontier children of head i (the first binary descendants outside its cell), left to right.
+template <typename F>
+__device__ __forceinline__ uint32_t for_children(uint32_t i, int D, int L,
+                                                 const uint32_t* __restrict__ left,
+                                                 const uint32_t* __restrict__ right,
+                                                 const uint32_t* __restrict__ range,
+                                                 const uint8_t* __restrict__ depth, F&& f) {
+  uint32_t c = 0;
+  if (D == L) {  // equal codes: all points of the range
+    const uint32_t a = range[2 * i], b = range[2 * i + 1];
+    for (uint32_t li = a; li <= b; ++li) f(kLeaf | li, c++);
+    return c;
+  }
+  uint32_t stack[16];
+  int sp = 0;
+  stack[sp++] = right[i];
+  stack[sp++] = left[i];
+  while (sp > 0) {
+    const uint32_t x = stack[--sp];
+    if (!(x & kLeaf) && depth[x] == D && sp < 15) {
+      stack[sp++] = right[x];
+      stack[sp++] = left[x];
+    } else {
+      f(x, c++);
+    }
+  }
+  return c;
+}
+
+// Whether internal node i heads a d3 cell, and how many d3 children that cell has; the counts'
+// exclusive prefix within the block (first[]) and the block's total (ctot[]), for the slots.
 __global__ void __launch_bounds__(kThreads) k_heads(int n, int ndim,
                                                     const uint32_t* __restrict__ left,
                                                     const uint32_t* __restrict__ right,
                                                     const uint32_t* __restrict__ parent,
                                                     const uint32_t* __restrict__ range,
                                                     const uint8_t* __restrict__ depth,
-                                                    uint32_t* __restrict__ count) {
+                                                    uint32_t* __restrict__ count,
+                                                    uint32_t* __restrict__ first,
+                                                    uint32_t* __restrict__ ctot) {
+  __shared__ uint32_t s_warp[kThreads / 32];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n - 1) return;
-  const int D = depth[i];
-  const bool head = i == 0 || depth[parent[i]] < D;
   uint32_t c = 0;
-  if (head) {
-    if (D == levels_of(ndim)) {
-      c = range[2 * i + 1] - range[2 * i] + 1;
-    } else {
-      uint32_t stack[16];
-      int sp = 0;
-      stack[sp++] = right[i];
-      stack[sp++] = left[i];
-      while (sp > 0) {
-        uint32_t x = stack[--sp];
-        if (!(x & kLeaf) && depth[x] == D && sp < 15) {
-          stack[sp++] = right[x];
-          stack[sp++] = left[x];
-        } else {
-          ++c;
-        }
-      }
-    }
+  if (i < n - 1) {
+    const int D = depth[i];
+    const bool head = i == 0 || depth[parent[i]] < D;
+    c = head ? for_children(i, D, levels_of(ndim), left, right, range, depth,
+                            [](uint32_t, uint32_t) {})
+             : 0u;
+    count[i] = c;
   }
-  count[i] = c;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = c;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(FL_FULL, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  uint32_t before = 0;
+  for (int w = 0; w < warp; ++w) before += s_warp[w];
+  if (i < n - 1) first[i] = before + x - c;
+  if (threadIdx.x == kThreads - 1) ctot[blockIdx.x] = before + x;
 }
 
-// Bottom-up aggregation with arrival flags (the second thread to reach a node proceeds).
-__global__ void __launch_bounds__(kThreads) k_aggregate(
+// Exclusive prefix of the block totals, in place, by one block: of the child counts (u32)...
+__global__ void __launch_bounds__(kThreads) k_top_u32(uint32_t* tot, int nb) {
+  __shared__ uint32_t s[kThreads];
+  const int per = (nb + kThreads - 1) / kThreads, a = threadIdx.x * per, b = min(nb, a + per);
+  uint32_t sum = 0;
+  for (int t = a; t < b; ++t) sum += tot[t];
+  s[threadIdx.x] = sum;
+  __syncthreads();
+  for (int o = 1; o < kThreads; o <<= 1) {  // Hillis-Steele, inclusive
+    const uint32_t y = threadIdx.x >= o ? s[threadIdx.x - o] : 0u;
+    __syncthreads();
+    s[threadIdx.x] += y;
+    __syncthreads();
+  }
+  uint32_t run = threadIdx.x ? s[threadIdx.x - 1] : 0u;
+  for (int t = a; t < b; ++t) {
+    const uint32_t v = tot[t];
+    tot[t] = run;
+    run += v;
+  }
+}
+
+// ... and of the fixed-point point records (D4)
+__global__ void __launch_bounds__(kThreads) k_top4(D4* tot, int nb) {
+  __shared__ D4 s[kThreads];
+  const int per = (nb + kThreads - 1) / kThreads, a = threadIdx.x * per, b = min(nb, a + per);
+  D4 sum = mk4(0, 0, 0, 0);
+  for (int t = a; t < b; ++t) sum = add4(sum, tot[t]);
+  s[threadIdx.x] = sum;
+  __syncthreads();
+  for (int o = 1; o < kThreads; o <<= 1) {
+    const D4 y = threadIdx.x >= o ? s[threadIdx.x - o] : mk4(0, 0, 0, 0);
+    __syncthreads();
+    s[threadIdx.x] = add4(s[threadIdx.x], y);
+    __syncthreads();
+  }
+  D4 run = threadIdx.x ? s[threadIdx.x - 1] : mk4(0, 0, 0, 0);
+  for (int t = a; t < b; ++t) {
+    const D4 v = tot[t];
+    tot[t] = run;
+    run = add4(run, v);
+  }
+}
+
+// first child slot of head x: slot 0 is the root's own; children follow in head order
+__device__ __forceinline__ uint32_t first_slot(const uint32_t* first, const uint32_t* ctot,
+                                               uint32_t x) {
+  return 1u + first[x] + ctot[x >> 8];
+}
+
+// Cells from the prefix sums (strengths of one sign, `sign`): value and centroid of every head.
+__global__ void __launch_bounds__(kThreads) k_cells_closed(int n, int ndim, float sign,
+                                                           const uint32_t* __restrict__ range,
+                                                           const uint8_t* __restrict__ depth,
+                                                           const uint32_t* __restrict__ count,
+                                                           const D4* __restrict__ P,
+                                                           const D4* __restrict__ Ptot,
+                                                           const float4* __restrict__ leaf,
+                                                           const float* __restrict__ cube,
+                                                           int fx_exp,
+                                                           float4* __restrict__ cell) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1 || !count[i]) return;
+  const uint32_t a = range[2 * i], b = range[2 * i + 1];
+  // prefix sums: within the 256-point block, plus the blocks before it; exact in fixed point
+  const D4 hi = add4(P[b], Ptot[b >> 8]);
+  const D4 lo = a ? add4(P[a - 1], Ptot[(a - 1) >> 8]) : mk4(0, 0, 0, 0);
+  const long long W = hi.x - lo.x;
+  const int D = depth[i];
+  float4 out;
+  if (W > 0) {
+    // centroid = p0 + size * sum(w (u - u0)) / sum(w), about the range's first point p0: the
+    // integer sums give the offsets exactly, so FP32 keeps the precision of the cell, not the cube
+    const float4 p0 = leaf[a];
+    const float sF = offset_scale(cube), r = cube[3] / (float)W;
+    out.x = p0.x + (float)(hi.y - lo.y - mulhi62(W, fx_offset(p0.x, cube[0], sF))) * r;
+    out.y = ndim > 1 ? p0.y + (float)(hi.z - lo.z - mulhi62(W, fx_offset(p0.y, cube[1], sF))) * r : 0.f;
+    out.z = ndim > 2 ? p0.z + (float)(hi.w - lo.w - mulhi62(W, fx_offset(p0.z, cube[2], sF))) * r : 0.f;
+    out.w = sign * (float)W * __int_as_float((127 - fx_exp) << 23) * damp(ndim, -D);
+  } else {
+    out = leaf[a];
+    out.w = 0.f;
+  }
+  cell[i] = out;
+}
+
+// The recursion itself (strengths of both signs), bottom-up with arrival flags: the second
+// thread to reach a node proceeds; a head combines its d3 children as accumulate() does.
+__global__ void __launch_bounds__(kThreads) k_cells_climb(
     int n, int ndim, const uint32_t* __restrict__ left, const uint32_t* __restrict__ right,
     const uint32_t* __restrict__ parent, const uint32_t* __restrict__ leaf_parent,
     const uint32_t* __restrict__ range, const uint8_t* __restrict__ depth,
-    const uint32_t* __restrict__ count, const uint32_t* __restrict__ first,
-    uint32_t* __restrict__ flag, float4* cell, const float4* __restrict__ leaf,
-    float4* __restrict__ cdata, uint2* __restrict__ cmeta, uint32_t* err) {
+    const uint32_t* __restrict__ count, uint32_t* __restrict__ flag, float4* cell,
+    const float4* __restrict__ leaf, uint32_t* err) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   const int L = levels_of(ndim);
-  const double c1 = sqrt(4.0 / (double)(1 << ndim));  // sqrt(4 / numChildren)
+  const double c1 = sqrt(4.0 / (double)(1 << ndim));
   uint32_t node = leaf_parent[s];
   for (int guard = 0;; ++guard) {
     if (guard > 256) {
@@ -263,201 +470,272 @@ __global__ void __launch_bounds__(kThreads) k_aggregate(
     __threadfence();
     if (atomicAdd(&flag[node], 1u) == 0) return;  // the sibling subtree is still working
     __threadfence();
-    const uint32_t cnt = count[node];
-    if (cnt) {
+    if (count[node]) {
       const int D = depth[node];
-      const uint32_t slot0 = first[node];
-      if ((uint64_t)slot0 + cnt > 2ull * (uint64_t)n + 1ull || D > L) {  // a malformed tree
-        atomicOr(err, FL_ERR_TREE);
-        return;
-      }
       const bool wide = D < kFp64Depth;
       double sv = 0, sa = 0, sx = 0, sy = 0, sz = 0;
       float fv = 0, fa = 0, fx = 0, fy = 0, fz = 0;
       float4 firstpos = make_float4(0, 0, 0, 0);
-      uint32_t j = 0;
-      auto take = [&](float4 q, float v, uint2 meta) {
-        // q: position (or centroid) and own value; v: value seen at depth D + 1
-        if (j == 0) firstpos = q;
-        if (j < cnt) {
-          cdata[slot0 + j] = q;
-          cmeta[slot0 + j] = meta;
+      for_children(node, D, L, left, right, range, depth, [&](uint32_t x, uint32_t j) {
+        float4 q;
+        float v;
+        if (x & kLeaf) {
+          q = leaf[x & kIndex];
+          v = q.w;
+        } else {
+          q = __ldcg(cell + x);
+          // the chain of one-child cells from D + 1 down to the child's depth scales by c
+          v = q.w * damp(ndim, depth[x] - D - 1);
         }
-        ++j;
+        if (j == 0) firstpos = q;
         const float a = fabsf(v);
         if (!(a > 0.f)) return;  // d3 skips children whose value is 0
-        if (wide) {
-          sv += v, sa += a, sx += (double)a * q.x, sy += (double)a * q.y, sz += (double)a * q.z;
-        } else {
-          fv += v, fa += a, fx += a * q.x, fy += a * q.y, fz += a * q.z;
-        }
-      };
-      auto child = [&](uint32_t x) {
-        if (x & kLeaf) {
-          const uint32_t li = x & kIndex;
-          const float4 q = leaf[li];
-          take(q, q.w, make_uint2(li, kLeafMark));
-        } else {
-          const float4 q = __ldcg(cell + x);
-          const int Dh = depth[x];
-          // the chain of one-child cells from D + 1 down to Dh scales the value by c per level
-          const float v = q.w * damp(ndim, Dh - D - 1);
-          take(q, v, make_uint2(first[x], count[x] | ((uint32_t)Dh << 26)));
-        }
-      };
-      if (D == L) {
-        const uint32_t a = range[2 * node], b = range[2 * node + 1];
-        for (uint32_t li = a; li <= b; ++li) child(kLeaf | li);
-      } else {
-        uint32_t stack[16];
-        int sp = 0;
-        stack[sp++] = right[node];
-        stack[sp++] = left[node];
-        while (sp > 0) {
-          uint32_t x = stack[--sp];
-          if (!(x & kLeaf) && depth[x] == D && sp < 15) {
-            stack[sp++] = right[x];
-            stack[sp++] = left[x];
-          } else {
-            child(x);
-          }
-        }
-      }
+        if (wide) sv += v, sa += a, sx += (double)a * q.x, sy += (double)a * q.y, sz += (double)a * q.z;
+        else fv += v, fa += a, fx += a * q.x, fy += a * q.y, fz += a * q.z;
+      });
       float4 out;
       double tv, ta;
       if (wide) {
         tv = sv, ta = sa;
-        if (sa > 0) out = make_float4((float)(sx / sa), (float)(sy / sa), (float)(sz / sa), 0.f);
-        else out = firstpos;
+        out = sa > 0 ? make_float4((float)(sx / sa), (float)(sy / sa), (float)(sz / sa), 0.f) : firstpos;
       } else {
         tv = fv, ta = fa;
-        if (fa > 0.f) out = make_float4(fx / fa, fy / fa, fz / fa, 0.f);
-        else out = firstpos;
+        out = fa > 0.f ? make_float4(fx / fa, fy / fa, fz / fa, 0.f) : firstpos;
       }
-      // d3 skips a cell whose children's values add up to 0 exactly; the sum here carries
-      // rounding, so a cancellation to within 2^-20 of the magnitudes counts as 0
       out.w = fabs(tv) <= ta * 0x1p-20 ? 0.f : (float)(tv * c1);
       cell[node] = out;
-      if (node == 0) {
-        cdata[0] = out;
-        cmeta[0] = make_uint2(slot0, cnt | ((uint32_t)D << 26));
-      }
     }
     if (node == 0) return;
     node = parent[node];
   }
 }
 
+// Every head writes its children into its slots; the root also fills slot 0.
+__global__ void __launch_bounds__(kThreads) k_slots(
+    int n, int ndim, const uint32_t* __restrict__ left, const uint32_t* __restrict__ right,
+    const uint32_t* __restrict__ range, const uint8_t* __restrict__ depth,
+    const uint32_t* __restrict__ count, const uint32_t* __restrict__ first,
+    const uint32_t* __restrict__ ctot, const float4* __restrict__ cell,
+    const float4* __restrict__ leaf, float4* __restrict__ cdata, uint2* __restrict__ cmeta,
+    uint32_t* err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1) return;
+  const uint32_t cnt = count[i];
+  if (!cnt) return;
+  const int D = depth[i], L = levels_of(ndim);
+  const uint32_t slot0 = first_slot(first, ctot, (uint32_t)i);
+  if ((uint64_t)slot0 + cnt > 2ull * (uint64_t)n + 1ull || D > L) {  // a malformed tree
+    atomicOr(err, FL_ERR_TREE);
+    return;
+  }
+  if (i == 0) {
+    cdata[0] = cell[0];
+    cmeta[0] = make_uint2(slot0, cnt | ((uint32_t)D << 26));
+  }
+  for_children(i, D, L, left, right, range, depth, [&](uint32_t x, uint32_t j) {
+    if (j >= cnt) return;
+    if (x & kLeaf) {
+      cdata[slot0 + j] = leaf[x & kIndex];
+      cmeta[slot0 + j] = make_uint2(x & kIndex, kLeafMark);
+    } else {
+      cdata[slot0 + j] = cell[x];
+      cmeta[slot0 + j] = make_uint2(first_slot(first, ctot, x), count[x] | ((uint32_t)depth[x] << 26));
+    }
+  });
+}
+
 constexpr int kWalkThreads = 128;
 constexpr int kWalkWarps = kWalkThreads / 32;
-constexpr int kStack = 160;
+constexpr int kStack = 96;  // entries per group; the deepest stack seen at 1M nodes in 3D is 67
+constexpr int kWalkGroup = 16;  // points per traversal
 
+template <int NG>
+struct WalkShared {
+  uint4 stack[kWalkWarps][NG][kStack];  // per point group: first child slot, count, top depth, lanes
+  float4 data[kWalkWarps][32];          // the batches: child position / centroid, value * alpha
+  uint4 info[kWalkWarps][32];           // the batches: threshold, lane mask, child meta (x, y)
+  uint32_t top[kWalkWarps][32];         // the batches: top depth of the child's chain
+};
+
+constexpr uint32_t kChain = 0x80000000u;  // set in a cell's meta word when its chain is > 1 cell
+
+// apply() of src/manyBody.js for the lane's own point against one staged child, written without
+// branches but for the rare cases (chains of cells, a zero component, distanceMin). Returns
+// whether the lane must open the child.
+template <int NDIM>
+__device__ __forceinline__ bool test_child(const float4 q, const uint4 r, const uint32_t* top,
+                                           const float4 me, int lane, float T0, float dmin2,
+                                           float dmax2, uint32_t myid, const uint32_t* perm,
+                                           int n, uint32_t step, uint32_t seed, float& ax,
+                                           float& ay, float& az) {
+  float dx = q.x - me.x;
+  float dy = NDIM > 1 ? q.y - me.y : 0.f;
+  float dz = NDIM > 2 ? q.z - me.z : 0.f;
+  float l = dx * dx + dy * dy + dz * dz;
+  const bool mine = (r.y >> lane) & 1u;
+  // a cell not far enough even at the deepest depth of its chain is opened
+  const bool open = mine && __uint_as_float(r.x) >= l;
+  const bool apply = mine && !open && l < dmax2;
+  float va = q.w;
+  if (apply && (int)r.w < 0) {
+    // the widest cell of the chain [top, D] that passes: d3 tests them in that order
+    const uint32_t D = (r.w >> 26) & 31u;
+    uint32_t k = *top;
+    while (k < D && T0 * pow4neg(k) >= l) ++k;
+    va *= damp(NDIM, (int)(D - k));
+  }
+  const float zprod = NDIM == 3 ? dx * dy * dz : NDIM == 2 ? dx * dy : dx;
+  if (apply && zprod == 0.f) {  // a zero component (or a product that underflowed)
+    const uint32_t other = r.w == kLeafMark ? perm[r.z < (uint32_t)n ? r.z : 0] : (uint32_t)n + r.z;
+    if (dx == 0.f) dx = fl::jiggle(myid, other, 0, step, seed), l += dx * dx;
+    if (NDIM > 1 && dy == 0.f) dy = fl::jiggle(myid, other, 1, step, seed), l += dy * dy;
+    if (NDIM > 2 && dz == 0.f) dz = fl::jiggle(myid, other, 2, step, seed), l += dz * dz;
+  }
+  if (l < dmin2) l = sqrtf(dmin2 * l);
+  const float w = apply ? __fdividef(va, l) : 0.f;
+  ax = fmaf(dx, w, ax);
+  if (NDIM > 1) ay = fmaf(dy, w, ay);
+  if (NDIM > 2) az = fmaf(dz, w, az);
+  return open;
+}
+
+// The walk of G consecutive sorted points (G = 32: a warp; 16: half a warp each, with its own
+// stack and batches, so that fewer points share, and pay for, one union of traversals).
+template <int NDIM, int G>
 __global__ void __launch_bounds__(kWalkThreads) k_walk(
     const float4* __restrict__ cdata, const uint2* __restrict__ cmeta,
     const float4* __restrict__ leaf, const uint32_t* __restrict__ perm,
-    const float* __restrict__ cube, float4* __restrict__ vel, int n, int ndim, float alpha,
-    double theta2, float dmin2, float dmax2, uint32_t step, uint32_t seed, uint32_t* err) {
-  __shared__ float s_T[32], s_damp[32];
-  __shared__ uint4 s_stack[kWalkWarps][kStack];
-  if (threadIdx.x < 32) {
-    const int k = threadIdx.x;
-    const double w = ldexp((double)cube[3], -k);
-    s_T[k] = (float)(w * w / theta2);
-    s_damp[k] = damp(ndim, k);
-  }
-  __syncthreads();
+    const float* __restrict__ cube, float4* __restrict__ vel, int n, float alpha,
+    double theta2, float dmin2, float dmax2, uint32_t step, uint32_t seed, uint32_t* err,
+    unsigned long long* stats) {
+  constexpr int NG = 32 / G;
+  __shared__ WalkShared<NG> sh;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int t = (blockIdx.x * kWalkWarps + warp) * 32 + lane;
+  const int grp = lane / G, gl = lane % G, gbase = grp * G;
+  const uint32_t gmask = G == 32 ? FL_FULL : (((1u << G) - 1u) << gbase);
+  const int base = (blockIdx.x * kWalkWarps + warp) * 32;
+  const int t = base + lane;
   const bool live = t < n;
-  const uint32_t act = __ballot_sync(FL_FULL, live);
-  if (!act) return;
+  const uint32_t act = __ballot_sync(FL_FULL, live) & gmask;
+  if (!__any_sync(FL_FULL, live)) return;
+  // (size / 2^k)^2 / theta^2 = T0 * 4^-k, exactly (a power-of-two scaling)
+  const float T0 = (float)((double)cube[3] * (double)cube[3] / theta2);
   const float4 me = live ? leaf[t] : make_float4(0, 0, 0, 0);
   const uint32_t myid = live ? perm[t] : 0;
-  float ax = 0.f, ay = 0.f, az = 0.f;
-  uint4* stk = s_stack[warp];
-  if (lane == 0) stk[0] = make_uint4(0u, 1u, 0u, act);  // the root: slot 0, top depth 0
-  int sp = 1;
+  const uint32_t slot_cap = 2u * (uint32_t)n + 1u;
+  float ax = 0.f, ay = 0.f, az = 0.f, bx = 0.f, by = 0.f, bz = 0.f;
+  unsigned long long tests = 0, useful = 0;
+  uint4* stk = sh.stack[warp][grp];
+  if (gl == 0 && act) stk[0] = make_uint4(0u, 1u, 0u, act);  // the root: slot 0, top depth 0
+  int sp = act ? 1 : 0, maxsp = sp;
   __syncwarp();
   uint32_t guard = 0;
   const uint32_t guard_max = 4u * (uint32_t)n + 64u;
-  const uint32_t slot_cap = 2u * (uint32_t)n + 1u;
-  while (sp > 0) {
-    const uint4 e = stk[--sp];
+  while (__any_sync(FL_FULL, sp > 0)) {
+    // each group gathers up to G children from the top of its stack; lane gl takes the gl-th
+    int total = 0;
+    uint32_t my_slot = 0, my_mask = 0, my_top = 0;
+    while (sp > 0 && total < G) {
+      const uint4 e = stk[sp - 1];
+      uint32_t cnt = e.y;
+      if (e.x >= slot_cap || cnt > slot_cap - e.x) {  // a malformed tree: never read past it
+        if (gl == 0) atomicOr(err, FL_ERR_TREE);
+        cnt = e.x >= slot_cap ? 0u : slot_cap - e.x;
+      }
+      const uint32_t take = cnt < (uint32_t)(G - total) ? cnt : (uint32_t)(G - total);
+      if (gl >= total && gl < total + (int)take) {
+        my_slot = e.x + (uint32_t)(gl - total);
+        my_mask = e.w;
+        my_top = e.z;
+      }
+      __syncwarp(gmask);
+      if (take == cnt) {
+        --sp;
+      } else if (gl == 0) {
+        stk[sp - 1] = make_uint4(e.x + take, cnt - take, e.z, e.w);
+      }
+      total += (int)take;
+      __syncwarp(gmask);
+    }
     __syncwarp();
-    const bool mine = (e.w >> lane) & 1u;
-    const uint32_t top = e.z;
-    uint32_t end = e.x + e.y;
-    if (end > slot_cap || e.x > end) {  // a malformed tree: report, never read out of bounds
-      if (lane == 0) atomicOr(err, FL_ERR_TREE);
-      end = e.x < slot_cap ? slot_cap : e.x;
+    if (gl < total) {
+      // what does not depend on the testing point, once per child
+      const float4 q = __ldg(cdata + my_slot);
+      uint2 m = __ldg(cmeta + my_slot);
+      const bool lf = m.y == kLeafMark;
+      const uint32_t D = (m.y >> 26) & 31u;
+      uint32_t mask = q.w != 0.f ? my_mask : 0u;  // d3 skips a zero value and all it holds
+      if (lf && m.x - (uint32_t)base < 32u) mask &= ~(1u << (m.x - (uint32_t)base));  // itself
+      if (!lf && my_top < D) m.y |= kChain;
+      sh.data[warp][lane] = make_float4(q.x, q.y, q.z, q.w * alpha);
+      sh.info[warp][lane] = make_uint4(__float_as_uint(lf ? -INFINITY : T0 * pow4neg(D)), mask, m.x, m.y);
+      sh.top[warp][lane] = my_top;
     }
-    for (uint32_t c0 = e.x; c0 < end; c0 += 8) {
-      float4 cd[8];
-      uint2 cm[8];
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        if (c0 + j < end) {
-          cd[j] = __ldg(cdata + c0 + j);
-          cm[j] = __ldg(cmeta + c0 + j);
-        }
+    __syncwarp();
+    auto push = [&](const uint4 r, uint32_t om) {
+      om &= gmask;
+      if (!om) return;
+      if (sp < kStack) {
+        if (gl == 0) stk[sp] = make_uint4(r.z, r.w & kCountMask, ((r.w >> 26) & 31u) + 1u, om);
+        ++sp;
+        if (sp > maxsp) maxsp = sp;
+      } else if (gl == 0) {
+        atomicOr(err, FL_ERR_STACK);
       }
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        if (c0 + j >= end) break;
-        const float4 q = cd[j];
-        const uint2 m = cm[j];
-        bool open = false;
-        if (mine && q.w != 0.f && !(m.y == kLeafMark && m.x == (uint32_t)t)) {
-          float dx = q.x - me.x, dy = q.y - me.y, dz = q.z - me.z;
-          float l = dx * dx + dy * dy + dz * dz;
-          float v = q.w;
-          bool apply = true;
-          if (m.y != kLeafMark) {
-            const uint32_t D = (m.y >> 26) & 31u;
-            if (s_T[D] >= l) {
-              open = true;  // not far enough even at the deepest cell of the chain
-              apply = false;
-            } else {
-              uint32_t k = top < D ? top : D;
-              while (k < D && s_T[k] >= l) ++k;  // the widest cell of the chain that passes
-              v *= s_damp[D - k];
-            }
-          }
-          if (apply && l < dmax2) {
-            if (dx == 0.f || (ndim > 1 && dy == 0.f) || (ndim > 2 && dz == 0.f)) {
-              const uint32_t other =
-                  m.y == kLeafMark ? perm[m.x < (uint32_t)n ? m.x : 0] : (uint32_t)n + c0 + j;
-              if (dx == 0.f) dx = fl::jiggle(myid, other, 0, step, seed), l += dx * dx;
-              if (ndim > 1 && dy == 0.f) dy = fl::jiggle(myid, other, 1, step, seed), l += dy * dy;
-              if (ndim > 2 && dz == 0.f) dz = fl::jiggle(myid, other, 2, step, seed), l += dz * dz;
-            }
-            if (l < dmin2) l = sqrtf(dmin2 * l);
-            const float w = __fdividef(v * alpha, l);
-            ax += dx * w, ay += dy * w, az += dz * w;
-          }
-        }
-        const uint32_t om = __ballot_sync(FL_FULL, open);
-        if (om) {
-          if (sp < kStack) {
-            if (lane == 0) stk[sp] = make_uint4(m.x, m.y & kCountMask, (m.y >> 26) + 1u, om);
-            ++sp;
-          } else if (lane == 0) {
-            atomicOr(err, FL_ERR_STACK);
-          }
-        }
-        __syncwarp();
+    };
+    const int jmax = G == 32 ? total : (int)__reduce_max_sync(FL_FULL, (unsigned)total);
+    int j = 0;
+    for (; j + 1 < jmax; j += 2) {  // two children at a time: independent work to overlap
+      const int s0 = gbase + j, s1 = gbase + j + 1;
+      bool o0 = false, o1 = false;
+      uint4 r0 = sh.info[warp][s0], r1 = sh.info[warp][s1];
+      if (j + 1 < total) {
+        const float4 q0 = sh.data[warp][s0], q1 = sh.data[warp][s1];
+        o0 = test_child<NDIM>(q0, r0, &sh.top[warp][s0], me, lane, T0, dmin2, dmax2, myid,
+                              perm, n, step, seed, ax, ay, az);
+        o1 = test_child<NDIM>(q1, r1, &sh.top[warp][s1], me, lane, T0, dmin2, dmax2, myid,
+                              perm, n, step, seed, bx, by, bz);
+      } else if (j < total) {
+        const float4 q0 = sh.data[warp][s0];
+        o0 = test_child<NDIM>(q0, r0, &sh.top[warp][s0], me, lane, T0, dmin2, dmax2, myid,
+                              perm, n, step, seed, ax, ay, az);
+      }
+      push(r0, __ballot_sync(FL_FULL, o0));
+      push(r1, __ballot_sync(FL_FULL, o1));
+      if (stats && gl == 0) {
+        if (j < total) tests += G, useful += __popc(r0.y & gmask);
+        if (j + 1 < total) tests += G, useful += __popc(r1.y & gmask);
       }
     }
+    if (j < jmax) {
+      const int s0 = gbase + j;
+      bool o = false;
+      const uint4 r = sh.info[warp][s0];
+      if (j < total) {
+        const float4 q = sh.data[warp][s0];
+        o = test_child<NDIM>(q, r, &sh.top[warp][s0], me, lane, T0, dmin2, dmax2, myid, perm, n,
+                             step, seed, ax, ay, az);
+      }
+      push(r, __ballot_sync(FL_FULL, o));
+      if (stats && gl == 0 && j < total) tests += G, useful += __popc(r.y & gmask);
+    }
+    __syncwarp();
     if (++guard > guard_max) {
       if (lane == 0) atomicOr(err, FL_ERR_STACK);
       break;
     }
   }
+  if (stats && gl == 0) {
+    atomicAdd(stats, tests);
+    atomicAdd(stats + 1, useful);
+    atomicMax(stats + 2, (unsigned long long)maxsp);
+  }
   if (!live) return;
+  ax += bx, ay += by, az += bz;
   float4 v = vel[myid];
   v.x += ax;
-  if (ndim > 1) v.y += ay;
-  if (ndim > 2) v.z += az;
+  if (NDIM > 1) v.y += ay;
+  if (NDIM > 2) v.z += az;
   vel[myid] = v;
 }
 
@@ -523,13 +801,16 @@ __global__ void __launch_bounds__(kPairThreads) k_allpairs(const float4* __restr
 
 size_t fl_tree_bytes(int64_t n) {
   const size_t m = (size_t)(n > 1 ? n - 1 : 1), N = (size_t)(n > 0 ? n : 1);
+  const size_t blocks = (N + kThreads - 1) / kThreads;
   return align256(4 * m) * 3 + align256(4 * N) + align256(8 * m) + align256(m) +
          align256(4 * m) * 3 + align256(16 * m) + align256(16 * N) + align256(16 * (2 * N + 1)) +
-         align256(8 * (2 * N + 1)) + fl_scan_bytes((int64_t)m) + 256;
+         align256(8 * (2 * N + 1)) + align256(4 * blocks) + align256(32 * N) +
+         align256(32 * blocks) + 256;
 }
 
 void fl_tree_carve(FlTreeBufs* t, void* base, int64_t n, int ndim) {
   const size_t m = (size_t)(n > 1 ? n - 1 : 1), N = (size_t)(n > 0 ? n : 1);
+  const size_t blocks = (N + kThreads - 1) / kThreads;
   char* p = static_cast<char*>(base);
   auto take = [&](size_t bytes) {
     void* r = p;
@@ -552,51 +833,87 @@ void fl_tree_carve(FlTreeBufs* t, void* base, int64_t n, int ndim) {
   t->leaf = (float4*)take(16 * N);
   t->child_data = (float4*)take(16 * (2 * N + 1));
   t->child_meta = (uint2*)take(8 * (2 * N + 1));
-  t->scan_scratch = take(fl_scan_bytes((int64_t)m));
+  t->scan_scratch = take(4 * blocks);  // per-block totals of the child counts
+  t->wsum = (double*)take(32 * N);
+  t->wtiles = (double*)take(32 * blocks);  // per-block totals of the point records
 }
 
 void fl_launch_morton(const float4* pos, int n, int ndim, const FlReduce* red, uint64_t* keys,
                       uint32_t* vals, uint32_t* hist, int lo_bit, float* cube_out,
                       cudaStream_t st) {
+  // two blocks per SM: each flushes its digit histograms with up to 2048 global atomics, so
+  // fewer, longer blocks keep that flush small
   int g = (n + kThreads - 1) / kThreads;
-  if (g > 8 * 152) g = 8 * 152;
+  if (g > 2 * 152) g = 2 * 152;
   if (g < 1) g = 1;
   k_morton<<<g, kThreads, 0, st>>>(pos, n, ndim, red, keys, vals, hist, lo_bit, cube_out);
 }
 
-void fl_launch_build(const FlTreeBufs* t, const uint64_t* skeys, const uint32_t* perm,
-                     const float4* pos, const float* strength, cudaStream_t st, int64_t* launches) {
-  const int n = t->n;
-  k_build<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(skeys, perm, pos, strength, n, t->ndim,
-                                                              t->left, t->right, t->parent,
-                                                              t->leaf_parent, t->range, t->depth,
-                                                              t->leaf);
-  ++*launches;
+int fl_fixed_exponent(int64_t n, double wmax) {
+  if (!(wmax > 0)) return 32;
+  const int e = 62 - (int)std::ceil(std::log2((double)(n > 1 ? n : 1) * wmax));
+  return e < 0 ? 0 : e > 100 ? 100 : e;
 }
 
-void fl_launch_aggregate(const FlTreeBufs* t, uint32_t* err, cudaStream_t st, int64_t* launches) {
+void fl_launch_build(const FlTreeBufs* t, const uint64_t* skeys, const uint32_t* perm,
+                     const float4* pos, const float* strength, bool closed, const float* cube,
+                     int fx_exp, cudaStream_t st, int64_t* launches) {
+  const int n = t->n;
+  const int nb = (n + kThreads - 1) / kThreads;
+  k_build<<<nb, kThreads, 0, st>>>(skeys, perm, pos, strength, n, t->ndim, t->left, t->right,
+                                   t->parent, t->leaf_parent, t->range, t->depth, t->leaf,
+                                   closed ? reinterpret_cast<D4*>(t->wsum) : nullptr,
+                                   reinterpret_cast<D4*>(t->wtiles), cube, fx_exp);
+  ++*launches;
+  if (closed) {
+    k_top4<<<1, kThreads, 0, st>>>(reinterpret_cast<D4*>(t->wtiles), nb);
+    ++*launches;
+  }
+}
+
+void fl_launch_aggregate(const FlTreeBufs* t, bool closed, float sign, const float* cube,
+                         int fx_exp, uint32_t* err, cudaStream_t st, int64_t* launches) {
   const int n = t->n, m = n - 1;
   const int g = (m + kThreads - 1) / kThreads;
+  uint32_t* ctot = static_cast<uint32_t*>(t->scan_scratch);
   k_heads<<<g, kThreads, 0, st>>>(n, t->ndim, t->left, t->right, t->parent, t->range, t->depth,
-                                  t->count);
-  ++*launches;
-  fl_scan_exclusive(t->count, t->first, m, 1u, t->scan_scratch, err, st, launches);
-  cudaMemsetAsync(t->flag, 0, 4 * (size_t)m, st);
-  k_aggregate<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(
-      n, t->ndim, t->left, t->right, t->parent, t->leaf_parent, t->range, t->depth, t->count,
-      t->first, t->flag, t->cell, t->leaf, t->child_data, t->child_meta, err);
+                                  t->count, t->first, ctot);
+  k_top_u32<<<1, kThreads, 0, st>>>(ctot, g);
+  *launches += 2;
+  if (closed) {
+    k_cells_closed<<<g, kThreads, 0, st>>>(n, t->ndim, sign, t->range, t->depth, t->count,
+                                           reinterpret_cast<const D4*>(t->wsum),
+                                           reinterpret_cast<const D4*>(t->wtiles), t->leaf, cube,
+                                           fx_exp, t->cell);
+    ++*launches;
+  } else {
+    cudaMemsetAsync(t->flag, 0, 4 * (size_t)m, st);
+    k_cells_climb<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(
+        n, t->ndim, t->left, t->right, t->parent, t->leaf_parent, t->range, t->depth, t->count,
+        t->flag, t->cell, t->leaf, err);
+    ++*launches;
+  }
+  k_slots<<<g, kThreads, 0, st>>>(n, t->ndim, t->left, t->right, t->range, t->depth, t->count,
+                                  t->first, ctot, t->cell, t->leaf, t->child_data, t->child_meta,
+                                  err);
   ++*launches;
 }
 
 void fl_launch_walk(const FlTreeBufs* t, const uint32_t* perm, const float* cube, float4* vel,
                     float alpha, double theta2, double dmin2, double dmax2, uint32_t step,
-                    uint32_t seed, uint32_t* err, cudaStream_t st) {
+                    uint32_t seed, uint32_t* err, unsigned long long* stats, cudaStream_t st) {
   const int n = t->n;
   const int warps = (n + 31) / 32;
   const int g = (warps + kWalkWarps - 1) / kWalkWarps;
   const float fmax2 = dmax2 > 3e38 ? INFINITY : (float)dmax2;
-  k_walk<<<g, kWalkThreads, 0, st>>>(t->child_data, t->child_meta, t->leaf, perm, cube, vel, n,
-                                     t->ndim, alpha, theta2, (float)dmin2, fmax2, step, seed, err);
+#define FL_WALK(D)                                                                             \
+  k_walk<D, kWalkGroup><<<g, kWalkThreads, 0, st>>>(t->child_data, t->child_meta, t->leaf, perm, cube, vel, \
+                                        n, alpha, theta2, (float)dmin2, fmax2, step, seed, err,  \
+                                        stats)
+  if (t->ndim == 3) FL_WALK(3);
+  else if (t->ndim == 2) FL_WALK(2);
+  else FL_WALK(1);
+#undef FL_WALK
 }
 
 void fl_launch_allpairs(const float4* pos, const float* strength, float4* vel, int n, int ndim,

@@ -17,7 +17,7 @@ FL_OK, FL_E_ARG, FL_E_OOM, FL_E_DEVICE, FL_E_TIMEOUT, FL_E_OVERFLOW, FL_E_STATE,
 STATUS_NAMES = ["FL_OK", "FL_E_ARG", "FL_E_OOM", "FL_E_DEVICE", "FL_E_TIMEOUT", "FL_E_OVERFLOW",
                 "FL_E_STATE", "FL_E_UNSUPPORTED"]
 FORCE_TYPES = {"manyBody": 1, "link": 2, "collide": 3, "center": 4, "radial": 5, "position": 6}
-Q_LAUNCHES, Q_TICKS, Q_NODES, Q_ERRWORD, Q_DEVICE_BYTES = 1, 2, 3, 4, 5
+Q_LAUNCHES, Q_TICKS, Q_NODES, Q_ERRWORD, Q_DEVICE_BYTES, Q_WALK_TESTS, Q_WALK_USEFUL = 1, 2, 3, 4, 5, 6, 7
 
 # every symbol include/forcegpu.h declares
 EXPORTS = ["fl_create", "fl_destroy", "fl_last_error", "fl_fits", "fl_set_nodes",
@@ -210,7 +210,7 @@ class Engine:
         return out.value
 
     def profile(self, enable):
-        self._check(self.L.fl_profile(self.h, 1 if enable else 0))
+        self._check(self.L.fl_profile(self.h, int(enable)))
 
     def debug_tree(self, index):
         """The last tick's tree of force `index`: (keys, perm, left, right, depth, cube5)."""

@@ -139,11 +139,16 @@ int32_t fl_buffers(fl_sim* sim, fl_buffer_info* out);
 /* The cudaStream_t every kernel of this simulation runs on. */
 int32_t fl_stream(fl_sim* sim, void** stream);
 /* Queries: FL_Q_LAUNCHES kernels launched so far, FL_Q_TICKS ticks queued so far, FL_Q_NODES,
- * FL_Q_ERRWORD the raw device error word, FL_Q_DEVICE_BYTES device memory held. */
-enum { FL_Q_LAUNCHES = 1, FL_Q_TICKS = 2, FL_Q_NODES = 3, FL_Q_ERRWORD = 4, FL_Q_DEVICE_BYTES = 5 };
+ * FL_Q_ERRWORD the raw device error word, FL_Q_DEVICE_BYTES device memory held;
+ * FL_Q_WALK_TESTS / FL_Q_WALK_USEFUL / FL_Q_WALK_MAX_STACK (profiling level 2): child tests the
+ * tree walks made (32 lanes each), of those the tests a point's own d3 traversal needed, and
+ * the deepest walk stack. */
+enum { FL_Q_LAUNCHES = 1, FL_Q_TICKS = 2, FL_Q_NODES = 3, FL_Q_ERRWORD = 4, FL_Q_DEVICE_BYTES = 5,
+       FL_Q_WALK_TESTS = 6, FL_Q_WALK_USEFUL = 7, FL_Q_WALK_MAX_STACK = 8 };
 int32_t fl_query(fl_sim* sim, int32_t what, int64_t* out);
-/* Per-kernel timing with CUDA events on the simulation's stream: enable, then read the summed
- * milliseconds and launch count of each kernel group since it was enabled. */
+/* Per-kernel timing with CUDA events on the simulation's stream: enable (1), or enable with
+ * the walk's counters too (2); then read the summed milliseconds and launch count of each
+ * kernel group since it was enabled. */
 int32_t fl_profile(fl_sim* sim, int32_t enable);
 /* Fills up to `cap` entries; returns the number of groups in *count. Names live as long as sim. */
 int32_t fl_profile_read(fl_sim* sim, int32_t cap, const char** names, double* ms,
