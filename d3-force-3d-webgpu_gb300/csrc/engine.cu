@@ -103,6 +103,7 @@ struct fl_sim {
   std::vector<std::unique_ptr<Pass>> plan;
   uint32_t seed = 0, step = 0;
   int64_t ticks = 0, launches = 0;
+  int walk_group = 16;  // points per tree-walk traversal (tuning: 16 or 32)
   bool profiling = false;
   int prof_level = 0;
   DevMem wstats;  // walk counters (profiling level 2)
@@ -372,7 +373,8 @@ void encode_manybody(fl_sim* s, Pass* p, float alpha, const FlReduce* box) {
     fl_launch_walk(t, p->sb.vals[r], p->cube.as<float>(), vel_cur(s), alpha, p->d.theta2,
                    p->d.distance_min2, p->d.distance_max2, s->step, s->seed,
                    s->errw.as<uint32_t>(),
-                   s->prof_level >= 2 ? s->wstats.as<unsigned long long>() : nullptr, s->st);
+                   s->prof_level >= 2 ? s->wstats.as<unsigned long long>() : nullptr,
+                   s->walk_group, s->st);
     ++s->launches;
   }
 }
@@ -735,6 +737,19 @@ int32_t fl_buffers(fl_sim* s, fl_buffer_info* out) {
   out->count = s->n;
   out->stride = 16;
   return FL_OK;
+}
+
+int32_t fl_set_tuning(fl_sim* s, int32_t key, int32_t value) {
+  int32_t rc = check_sim(s);
+  if (rc) return rc;
+  switch (key) {
+    case FL_TUNE_WALK_GROUP:
+      if (value != 16 && value != 32) return fail(s, FL_E_ARG, "walk group must be 16 or 32");
+      s->walk_group = value;
+      return FL_OK;
+    default:
+      return fail(s, FL_E_ARG, "unknown tuning key");
+  }
 }
 
 int32_t fl_stream(fl_sim* s, void** stream) {

@@ -107,9 +107,11 @@ void fl_launch_aggregate(const FlTreeBufs* t, bool closed, float sign, const flo
 int fl_fixed_exponent(int64_t n, double wmax);
 // stats (optional): [0] child tests made by the warps (32 per child), [1] of those, tests by a
 // lane whose point needed them (the d3 traversal's own work)
+// group: points per traversal (16 or 32)
 void fl_launch_walk(const FlTreeBufs* t, const uint32_t* perm, const float* cube, float4* vel,
                     float alpha, double theta2, double dmin2, double dmax2, uint32_t step,
-                    uint32_t seed, uint32_t* err, unsigned long long* stats, cudaStream_t st);
+                    uint32_t seed, uint32_t* err, unsigned long long* stats, int group,
+                    cudaStream_t st);
 // Exact all-pairs sum (theta ~ 0): O(n^2), tiled through shared memory.
 void fl_launch_allpairs(const float4* pos, const float* strength, float4* vel, int n, int ndim,
                         float alpha, float dmin2, float dmax2, uint32_t step, uint32_t seed,

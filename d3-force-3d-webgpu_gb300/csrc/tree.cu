@@ -547,7 +547,6 @@ __global__ void __launch_bounds__(kThreads) k_slots(
 constexpr int kWalkThreads = 128;
 constexpr int kWalkWarps = kWalkThreads / 32;
 constexpr int kStack = 96;  // entries per group; the deepest stack seen at 1M nodes in 3D is 67
-constexpr int kWalkGroup = 16;  // points per traversal
 
 template <int NG>
 struct WalkShared {
@@ -559,49 +558,32 @@ struct WalkShared {
 
 constexpr uint32_t kChain = 0x80000000u;  // set in a cell's meta word when its chain is > 1 cell
 
-// apply() of src/manyBody.js for the lane's own point against one staged child, written without
-// branches but for the rare cases (chains of cells, a zero component, distanceMin). Returns
-// whether the lane must open the child.
+// The less common cases of apply() (src/manyBody.js:73-115) for one child: a chain of cells
+// (approximated at its widest cell that passes the theta test), a zero component of the
+// displacement (d3 replaces it with a jiggle) and distanceMin.
 template <int NDIM>
-__device__ __forceinline__ bool test_child(const float4 q, const uint4 r, const uint32_t* top,
-                                           const float4 me, int lane, float T0, float dmin2,
-                                           float dmax2, uint32_t myid, const uint32_t* perm,
-                                           int n, uint32_t step, uint32_t seed, float& ax,
-                                           float& ay, float& az) {
-  float dx = q.x - me.x;
-  float dy = NDIM > 1 ? q.y - me.y : 0.f;
-  float dz = NDIM > 2 ? q.z - me.z : 0.f;
-  float l = dx * dx + dy * dy + dz * dz;
-  const bool mine = (r.y >> lane) & 1u;
-  // a cell not far enough even at the deepest depth of its chain is opened
-  const bool open = mine && __uint_as_float(r.x) >= l;
-  const bool apply = mine && !open && l < dmax2;
-  float va = q.w;
-  if (apply && (int)r.w < 0) {
-    // the widest cell of the chain [top, D] that passes: d3 tests them in that order
+__device__ __forceinline__ void rare_case(const uint4 r, uint32_t top, float T0, float dmin2,
+                                          uint32_t myid, const uint32_t* __restrict__ perm, int n,
+                                          uint32_t step, uint32_t seed, float& va, float& dx,
+                                          float& dy, float& dz, float& l) {
+  if ((int)r.w < 0) {  // the widest cell of the chain [top, D] that passes: d3's order
     const uint32_t D = (r.w >> 26) & 31u;
-    uint32_t k = *top;
+    uint32_t k = top;
     while (k < D && T0 * pow4neg(k) >= l) ++k;
     va *= damp(NDIM, (int)(D - k));
   }
-  const float zprod = NDIM == 3 ? dx * dy * dz : NDIM == 2 ? dx * dy : dx;
-  if (apply && zprod == 0.f) {  // a zero component (or a product that underflowed)
+  if (dx == 0.f || (NDIM > 1 && dy == 0.f) || (NDIM > 2 && dz == 0.f)) {
     const uint32_t other = r.w == kLeafMark ? perm[r.z < (uint32_t)n ? r.z : 0] : (uint32_t)n + r.z;
     if (dx == 0.f) dx = fl::jiggle(myid, other, 0, step, seed), l += dx * dx;
     if (NDIM > 1 && dy == 0.f) dy = fl::jiggle(myid, other, 1, step, seed), l += dy * dy;
     if (NDIM > 2 && dz == 0.f) dz = fl::jiggle(myid, other, 2, step, seed), l += dz * dz;
   }
   if (l < dmin2) l = sqrtf(dmin2 * l);
-  const float w = apply ? __fdividef(va, l) : 0.f;
-  ax = fmaf(dx, w, ax);
-  if (NDIM > 1) ay = fmaf(dy, w, ay);
-  if (NDIM > 2) az = fmaf(dz, w, az);
-  return open;
 }
 
 // The walk of G consecutive sorted points (G = 32: a warp; 16: half a warp each, with its own
 // stack and batches, so that fewer points share, and pay for, one union of traversals).
-template <int NDIM, int G>
+template <int NDIM, int G, bool STATS, bool DMAX>
 __global__ void __launch_bounds__(kWalkThreads) k_walk(
     const float4* __restrict__ cdata, const uint2* __restrict__ cmeta,
     const float4* __restrict__ leaf, const uint32_t* __restrict__ perm,
@@ -613,6 +595,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int grp = lane / G, gl = lane % G, gbase = grp * G;
   const uint32_t gmask = G == 32 ? FL_FULL : (((1u << G) - 1u) << gbase);
+  const uint32_t lanebit = 1u << lane;
   const int base = (blockIdx.x * kWalkWarps + warp) * 32;
   const int t = base + lane;
   const bool live = t < n;
@@ -631,6 +614,9 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
   __syncwarp();
   uint32_t guard = 0;
   const uint32_t guard_max = 4u * (uint32_t)n + 64u;
+  float4* sdata = sh.data[warp] + gbase;
+  uint4* sinfo = sh.info[warp] + gbase;
+  uint32_t* stop = sh.top[warp] + gbase;
   while (__any_sync(FL_FULL, sp > 0)) {
     // each group gathers up to G children from the top of its stack; lane gl takes the gl-th
     int total = 0;
@@ -658,6 +644,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
       __syncwarp(gmask);
     }
     __syncwarp();
+    const int jmax = G == 32 ? total : (int)__reduce_max_sync(FL_FULL, (unsigned)total);
     if (gl < total) {
       // what does not depend on the testing point, once per child
       const float4 q = __ldg(cdata + my_slot);
@@ -667,57 +654,60 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
       uint32_t mask = q.w != 0.f ? my_mask : 0u;  // d3 skips a zero value and all it holds
       if (lf && m.x - (uint32_t)base < 32u) mask &= ~(1u << (m.x - (uint32_t)base));  // itself
       if (!lf && my_top < D) m.y |= kChain;
-      sh.data[warp][lane] = make_float4(q.x, q.y, q.z, q.w * alpha);
-      sh.info[warp][lane] = make_uint4(__float_as_uint(lf ? -INFINITY : T0 * pow4neg(D)), mask, m.x, m.y);
-      sh.top[warp][lane] = my_top;
+      sdata[gl] = make_float4(q.x, q.y, q.z, q.w * alpha);
+      sinfo[gl] = make_uint4(__float_as_uint(lf ? -INFINITY : T0 * pow4neg(D)), mask, m.x, m.y);
+      stop[gl] = my_top;
+    } else if (gl < ((jmax + 1) & ~1)) {  // pad the group's batch: a child no lane tests
+      sdata[gl] = make_float4(0.f, 0.f, 0.f, 0.f);
+      sinfo[gl] = make_uint4(0u, 0u, 0u, kLeafMark);
     }
     __syncwarp();
-    auto push = [&](const uint4 r, uint32_t om) {
-      om &= gmask;
-      if (!om) return;
-      if (sp < kStack) {
-        if (gl == 0) stk[sp] = make_uint4(r.z, r.w & kCountMask, ((r.w >> 26) & 31u) + 1u, om);
-        ++sp;
-        if (sp > maxsp) maxsp = sp;
-      } else if (gl == 0) {
-        atomicOr(err, FL_ERR_STACK);
+    for (int j = 0; j < jmax; j += 2) {  // two children per round: independent work to overlap
+      const float4 q0 = sdata[j], q1 = sdata[j + 1];
+      const uint4 r0 = sinfo[j], r1 = sinfo[j + 1];
+      float dx0 = q0.x - me.x, dy0 = NDIM > 1 ? q0.y - me.y : 0.f, dz0 = NDIM > 2 ? q0.z - me.z : 0.f;
+      float dx1 = q1.x - me.x, dy1 = NDIM > 1 ? q1.y - me.y : 0.f, dz1 = NDIM > 2 ? q1.z - me.z : 0.f;
+      float l0 = dx0 * dx0 + dy0 * dy0 + dz0 * dz0;
+      float l1 = dx1 * dx1 + dy1 * dy1 + dz1 * dz1;
+      const bool m0 = r0.y & lanebit, m1 = r1.y & lanebit;
+      // a cell not far enough even at the deepest depth of its chain is opened
+      const bool o0 = m0 && __uint_as_float(r0.x) >= l0, o1 = m1 && __uint_as_float(r1.x) >= l1;
+      const bool a0 = m0 && !o0 && (!DMAX || l0 < dmax2), a1 = m1 && !o1 && (!DMAX || l1 < dmax2);
+      float v0 = q0.w, v1 = q1.w;
+      const float z0 = NDIM == 3 ? dx0 * dy0 * dz0 : NDIM == 2 ? dx0 * dy0 : dx0;
+      const float z1 = NDIM == 3 ? dx1 * dy1 * dz1 : NDIM == 2 ? dx1 * dy1 : dx1;
+      const bool c0 = a0 && ((int)r0.w < 0 || z0 == 0.f || l0 < dmin2);
+      const bool c1 = a1 && ((int)r1.w < 0 || z1 == 0.f || l1 < dmin2);
+      // a warp-uniform branch: the common path never executes the uncommon code, even predicated
+      if (__any_sync(FL_FULL, c0 || c1)) {
+        if (c0) rare_case<NDIM>(r0, stop[j], T0, dmin2, myid, perm, n, step, seed, v0, dx0, dy0, dz0, l0);
+        if (c1) rare_case<NDIM>(r1, stop[j + 1], T0, dmin2, myid, perm, n, step, seed, v1, dx1, dy1, dz1, l1);
       }
-    };
-    const int jmax = G == 32 ? total : (int)__reduce_max_sync(FL_FULL, (unsigned)total);
-    int j = 0;
-    for (; j + 1 < jmax; j += 2) {  // two children at a time: independent work to overlap
-      const int s0 = gbase + j, s1 = gbase + j + 1;
-      bool o0 = false, o1 = false;
-      uint4 r0 = sh.info[warp][s0], r1 = sh.info[warp][s1];
-      if (j + 1 < total) {
-        const float4 q0 = sh.data[warp][s0], q1 = sh.data[warp][s1];
-        o0 = test_child<NDIM>(q0, r0, &sh.top[warp][s0], me, lane, T0, dmin2, dmax2, myid,
-                              perm, n, step, seed, ax, ay, az);
-        o1 = test_child<NDIM>(q1, r1, &sh.top[warp][s1], me, lane, T0, dmin2, dmax2, myid,
-                              perm, n, step, seed, bx, by, bz);
-      } else if (j < total) {
-        const float4 q0 = sh.data[warp][s0];
-        o0 = test_child<NDIM>(q0, r0, &sh.top[warp][s0], me, lane, T0, dmin2, dmax2, myid,
-                              perm, n, step, seed, ax, ay, az);
+      const float w0 = a0 ? __fdividef(v0, l0) : 0.f, w1 = a1 ? __fdividef(v1, l1) : 0.f;
+      ax = fmaf(dx0, w0, ax), bx = fmaf(dx1, w1, bx);
+      if (NDIM > 1) ay = fmaf(dy0, w0, ay), by = fmaf(dy1, w1, by);
+      if (NDIM > 2) az = fmaf(dz0, w0, az), bz = fmaf(dz1, w1, bz);
+      const uint32_t om0 = __ballot_sync(FL_FULL, o0) & gmask;
+      const uint32_t om1 = __ballot_sync(FL_FULL, o1) & gmask;
+      if (om0 | om1) {  // push the children some lanes must open (rare next to the tests)
+        if (om0) {
+          if (sp < kStack && gl == 0) stk[sp] = make_uint4(r0.z, r0.w & kCountMask, ((r0.w >> 26) & 31u) + 1u, om0);
+          ++sp;
+        }
+        if (om1) {
+          if (sp < kStack && gl == 0) stk[sp] = make_uint4(r1.z, r1.w & kCountMask, ((r1.w >> 26) & 31u) + 1u, om1);
+          ++sp;
+        }
+        if (sp > kStack) {
+          if (gl == 0) atomicOr(err, FL_ERR_STACK);
+          sp = kStack;
+        }
+        if (STATS && sp > maxsp) maxsp = sp;
       }
-      push(r0, __ballot_sync(FL_FULL, o0));
-      push(r1, __ballot_sync(FL_FULL, o1));
-      if (stats && gl == 0) {
+      if (STATS && gl == 0) {
         if (j < total) tests += G, useful += __popc(r0.y & gmask);
         if (j + 1 < total) tests += G, useful += __popc(r1.y & gmask);
       }
-    }
-    if (j < jmax) {
-      const int s0 = gbase + j;
-      bool o = false;
-      const uint4 r = sh.info[warp][s0];
-      if (j < total) {
-        const float4 q = sh.data[warp][s0];
-        o = test_child<NDIM>(q, r, &sh.top[warp][s0], me, lane, T0, dmin2, dmax2, myid, perm, n,
-                             step, seed, ax, ay, az);
-      }
-      push(r, __ballot_sync(FL_FULL, o));
-      if (stats && gl == 0 && j < total) tests += G, useful += __popc(r.y & gmask);
     }
     __syncwarp();
     if (++guard > guard_max) {
@@ -725,7 +715,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
       break;
     }
   }
-  if (stats && gl == 0) {
+  if (STATS && gl == 0) {
     atomicAdd(stats, tests);
     atomicAdd(stats + 1, useful);
     atomicMax(stats + 2, (unsigned long long)maxsp);
@@ -901,18 +891,36 @@ void fl_launch_aggregate(const FlTreeBufs* t, bool closed, float sign, const flo
 
 void fl_launch_walk(const FlTreeBufs* t, const uint32_t* perm, const float* cube, float4* vel,
                     float alpha, double theta2, double dmin2, double dmax2, uint32_t step,
-                    uint32_t seed, uint32_t* err, unsigned long long* stats, cudaStream_t st) {
+                    uint32_t seed, uint32_t* err, unsigned long long* stats, int group,
+                    cudaStream_t st) {
   const int n = t->n;
   const int warps = (n + 31) / 32;
   const int g = (warps + kWalkWarps - 1) / kWalkWarps;
   const float fmax2 = dmax2 > 3e38 ? INFINITY : (float)dmax2;
-#define FL_WALK(D)                                                                             \
-  k_walk<D, kWalkGroup><<<g, kWalkThreads, 0, st>>>(t->child_data, t->child_meta, t->leaf, perm, cube, vel, \
-                                        n, alpha, theta2, (float)dmin2, fmax2, step, seed, err,  \
-                                        stats)
-  if (t->ndim == 3) FL_WALK(3);
-  else if (t->ndim == 2) FL_WALK(2);
-  else FL_WALK(1);
+#define FL_WALK(D, G)                                                                          \
+  do {                                                                                         \
+    if (stats)                                                                                 \
+      k_walk<D, G, true, true><<<g, kWalkThreads, 0, st>>>(                                    \
+          t->child_data, t->child_meta, t->leaf, perm, cube, vel, n, alpha, theta2,            \
+          (float)dmin2, fmax2, step, seed, err, stats);                                        \
+    else if (fmax2 < INFINITY)                                                                 \
+      k_walk<D, G, false, true><<<g, kWalkThreads, 0, st>>>(                                   \
+          t->child_data, t->child_meta, t->leaf, perm, cube, vel, n, alpha, theta2,            \
+          (float)dmin2, fmax2, step, seed, err, stats);                                        \
+    else                                                                                       \
+      k_walk<D, G, false, false><<<g, kWalkThreads, 0, st>>>(                                  \
+          t->child_data, t->child_meta, t->leaf, perm, cube, vel, n, alpha, theta2,            \
+          (float)dmin2, fmax2, step, seed, err, stats);                                        \
+  } while (0)
+  if (group == 32) {
+    if (t->ndim == 3) FL_WALK(3, 32);
+    else if (t->ndim == 2) FL_WALK(2, 32);
+    else FL_WALK(1, 32);
+  } else {
+    if (t->ndim == 3) FL_WALK(3, 16);
+    else if (t->ndim == 2) FL_WALK(2, 16);
+    else FL_WALK(1, 16);
+  }
 #undef FL_WALK
 }
 

@@ -24,7 +24,8 @@ EXPORTS = ["fl_create", "fl_destroy", "fl_last_error", "fl_fits", "fl_set_nodes"
            "fl_update_positions", "fl_update_pins", "fl_update_velocities", "fl_set_forces",
            "fl_set_seed", "fl_enqueue", "fl_sync", "fl_idle", "fl_busy", "fl_buffers",
            "fl_stream", "fl_query", "fl_profile", "fl_profile_read", "fl_radix_sort",
-           "fl_debug_tree"]
+           "fl_debug_tree", "fl_set_tuning"]
+TUNE_WALK_GROUP = 1
 
 
 class FlError(RuntimeError):
@@ -89,6 +90,7 @@ def load():
         "fl_profile_read": (I32, [P, I32, P, P, P, ctypes.POINTER(I32)]),
         "fl_radix_sort": (I32, [P, P, I64, I32, P, P]),
         "fl_debug_tree": (I32, [P, I32, P, P, P, P, P, P]),
+        "fl_set_tuning": (I32, [P, I32, I32]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -198,6 +200,9 @@ class Engine:
         self._check(self.L.fl_buffers(self.h, ctypes.byref(b)))
         return {"positions": b.positions, "velocities": b.velocities, "count": b.count,
                 "stride": b.stride}
+
+    def set_tuning(self, key, value):
+        self._check(self.L.fl_set_tuning(self.h, int(key), int(value)))
 
     def stream(self):
         out = ctypes.c_void_p()

@@ -136,6 +136,12 @@ int32_t fl_buffers(fl_sim* sim, fl_buffer_info* out);
 /* ---- measurement (no reference counterpart: the reference times only with performance.now()
  *      around tickAsync, examples/benchmark.html:105-132) ---- */
 
+/* Tuning parameters (no reference counterpart; the reference's closest are its fixed
+ * constants, e.g. src/gpu/passes/barnesHut.js:49-58): FL_TUNE_WALK_GROUP, points that share one
+ * tree-walk traversal, 16 (default) or 32. */
+enum { FL_TUNE_WALK_GROUP = 1 };
+int32_t fl_set_tuning(fl_sim* sim, int32_t key, int32_t value);
+
 /* The cudaStream_t every kernel of this simulation runs on. */
 int32_t fl_stream(fl_sim* sim, void** stream);
 /* Queries: FL_Q_LAUNCHES kernels launched so far, FL_Q_TICKS ticks queued so far, FL_Q_NODES,
