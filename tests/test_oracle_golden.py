@@ -130,7 +130,7 @@ def benchmark_graph(n):
     return np.array(links, dtype=np.int32)
 
 
-@pytest.mark.parametrize("dims,theta_index", [(2, 0), (3, 0), (3, 1)])
+@pytest.mark.parametrize("dims,theta_index", [(d, t) for d in (2, 3) for t in range(4)])
 def test_published_layout_sizes(dims, theta_index):
     """RMS radius after 300 ticks of link(30) + charge + center on the 1,000-node graph: the
     CPU row of docs/differences.md:35-40, to the published integer."""
