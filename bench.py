@@ -187,7 +187,8 @@ def main():
         dist.init_process_group("nccl")
     import forcegpu
     from forcegpu import Engine
-    from forcegpu._lib import Q_DEVICE_BYTES, Q_LAUNCHES, desc_from_gpu
+    from forcegpu._lib import (Q_DEVICE_BYTES, Q_LAUNCHES, Q_WALK_APPLIES, Q_WALK_OPENS,
+                               Q_WALK_RARE, Q_WALK_TESTS, Q_WALK_USEFUL, desc_from_gpu)
 
     n = args.nodes
     xyz, src, dst, bias, strength = workload(n)
@@ -207,7 +208,7 @@ def main():
     eng.set_seed(12345)
     decay = 0.6
     total = args.warmup + args.steps
-    al, _ = alphas(total + 2 * args.steps + 8)
+    al, _ = alphas(total + 2 * args.steps + 9)
 
     stream = torch.cuda.ExternalStream(eng.stream(), device=local)
     # warm-up
@@ -243,6 +244,16 @@ def main():
     ms_tick = ms_total / args.steps
     value = ms_total / (args.steps * world)
 
+    # the walk's counted work, from one more tick with the walk's counters on (outside the
+    # timed region): FP32 operations per launch for the FP32-pipe view of the roofline
+    eng.profile(2)
+    eng.enqueue(al[total:total + 1], decay)
+    eng.idle()
+    walk_count = {k: eng.query(q) for k, q in (("tests", Q_WALK_TESTS), ("useful", Q_WALK_USEFUL),
+                                              ("opens", Q_WALK_OPENS), ("applies", Q_WALK_APPLIES),
+                                              ("rare_rounds", Q_WALK_RARE))}
+    eng.profile(False)
+
     # e2e through the C ABI with pinned host buffers
     e2e = None
     if not args.no_e2e:
@@ -251,7 +262,7 @@ def main():
         eng.sync_into(hp.data_ptr(), hv.data_ptr())
         hpn = hp.numpy()
         k = args.steps
-        a2 = al[total:total + k]
+        a2 = al[total + 1:total + 1 + k]
         barrier()
         t0 = time.perf_counter()
         for i in range(k):
@@ -279,6 +290,15 @@ def main():
             "algorithmic_bytes_per_launch": walk_bytes, "avg_launch_ms": walk_avg,
             "tick_bytes": BYTES_PER_NODE_TICK * n,
             "tick_hbm_frac": BYTES_PER_NODE_TICK * n / (ms_tick * 1e-3) / 1e9 / peaks["hbm_gbs"]}
+    flops = FLOPS_PER_INTERACTION * walk_count["applies"] + FLOPS_PER_OPEN * walk_count["opens"]
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    mhz = clk["sm_mhz"] or 2070.0
+    fp32_peak = sms * 128 * 2 * mhz * 1e6 / 1e12  # TFLOP/s at the median sampled SM clock
+    fp32_achieved = flops / (walk_avg * 1e-3) / 1e12 if walk_avg else None
+    roof["fp32"] = {"achieved": fp32_achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                    "frac": fp32_achieved / fp32_peak if fp32_achieved else None,
+                    "flops_per_launch": flops, "sms": sms, "sm_mhz": mhz,
+                    "per_point": {k: v / n for k, v in walk_count.items()}}
     kernels = {k: {"ms_per_tick": v[0] / args.steps, "launches": v[1]} for k, v in prof.items()}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

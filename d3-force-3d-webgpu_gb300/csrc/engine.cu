@@ -781,11 +781,14 @@ int32_t fl_query(fl_sim* s, int32_t what, int64_t* out) {
     }
     case FL_Q_WALK_TESTS:
     case FL_Q_WALK_USEFUL:
-    case FL_Q_WALK_MAX_STACK: {
-      unsigned long long w[3] = {0, 0, 0};
+    case FL_Q_WALK_MAX_STACK:
+    case FL_Q_WALK_OPENS:
+    case FL_Q_WALK_APPLIES:
+    case FL_Q_WALK_RARE: {
+      unsigned long long w[6] = {0, 0, 0, 0, 0, 0};
       if (s->wstats.p) {
         FL_CK(s, cudaStreamSynchronize(s->st));
-        FL_CK(s, cudaMemcpy(w, s->wstats.p, 24, cudaMemcpyDeviceToHost));
+        FL_CK(s, cudaMemcpy(w, s->wstats.p, sizeof w, cudaMemcpyDeviceToHost));
       }
       *out = (int64_t)w[what - FL_Q_WALK_TESTS];
       break;
@@ -805,7 +808,7 @@ int32_t fl_profile(fl_sim* s, int32_t enable) {
   for (int g = 0; g < G_COUNT; ++g) s->prof_ms[g] = 0, s->prof_count[g] = 0;
   if (enable >= 2) {
     if (!s->wstats.p) FL_CK(s, s->wstats.alloc(256));
-    FL_CK(s, cudaMemset(s->wstats.p, 0, 24));
+    FL_CK(s, cudaMemset(s->wstats.p, 0, 48));
   }
   return FL_OK;
 }

@@ -551,29 +551,34 @@ constexpr int kStack = 96;  // entries per group; the deepest stack seen at 1M n
 template <int NG>
 struct WalkShared {
   uint4 stack[kWalkWarps][NG][kStack];  // per point group: first child slot, count, top depth, lanes
-  float4 data[kWalkWarps][32];          // the batches: child position / centroid, value * alpha
-  uint4 info[kWalkWarps][32];           // the batches: threshold, lane mask, child meta (x, y)
-  uint32_t top[kWalkWarps][32];         // the batches: top depth of the child's chain
+  // the batches, one entry per child: what every test reads ...
+  float4 data[kWalkWarps][32];  // position / centroid, value at the chain's top depth * alpha
+  uint4 test[kWalkWarps][32];   // open threshold, uncommon-case bound, lane mask, slot / index
+  // ... and what only a push or an uncommon case reads
+  uint2 cold[kWalkWarps][32];   // meta word (count | depth << 26, or kLeafMark), chain top depth
+  uint32_t own[kWalkWarps][32];  // the gather: which stack entry each child of the batch is from
 };
 
-constexpr uint32_t kChain = 0x80000000u;  // set in a cell's meta word when its chain is > 1 cell
-
 // The less common cases of apply() (src/manyBody.js:73-115) for one child: a chain of cells
-// (approximated at its widest cell that passes the theta test), a zero component of the
-// displacement (d3 replaces it with a jiggle) and distanceMin.
+// whose widest cell is too close (the child is approximated at the first, widest, depth of the
+// chain that passes the theta test), a zero component of the displacement (d3 replaces it with
+// a jiggle) and distanceMin. `va` arrives as the value at the chain's top depth.
 template <int NDIM>
-__device__ __forceinline__ void rare_case(const uint4 r, uint32_t top, float T0, float dmin2,
-                                          uint32_t myid, const uint32_t* __restrict__ perm, int n,
-                                          uint32_t step, uint32_t seed, float& va, float& dx,
-                                          float& dy, float& dz, float& l) {
-  if ((int)r.w < 0) {  // the widest cell of the chain [top, D] that passes: d3's order
-    const uint32_t D = (r.w >> 26) & 31u;
-    uint32_t k = top;
-    while (k < D && T0 * pow4neg(k) >= l) ++k;
-    va *= damp(NDIM, (int)(D - k));
+__device__ __forceinline__ void rare_case(uint32_t meta, uint32_t top, uint32_t idx, float T0,
+                                          float dmin2, uint32_t myid,
+                                          const uint32_t* __restrict__ perm, int n, uint32_t step,
+                                          uint32_t seed, float& va, float& dx, float& dy,
+                                          float& dz, float& l) {
+  if (meta != kLeafMark) {
+    const uint32_t D = (meta >> 26) & 31u;
+    if (top < D && T0 * pow4neg(top) >= l) {
+      uint32_t k = top + 1;
+      while (k < D && T0 * pow4neg(k) >= l) ++k;
+      va *= damp(NDIM, (int)top - (int)k);  // value(k) = value(top) c^(top - k)
+    }
   }
   if (dx == 0.f || (NDIM > 1 && dy == 0.f) || (NDIM > 2 && dz == 0.f)) {
-    const uint32_t other = r.w == kLeafMark ? perm[r.z < (uint32_t)n ? r.z : 0] : (uint32_t)n + r.z;
+    const uint32_t other = meta == kLeafMark ? perm[idx < (uint32_t)n ? idx : 0] : (uint32_t)n + idx;
     if (dx == 0.f) dx = fl::jiggle(myid, other, 0, step, seed), l += dx * dx;
     if (NDIM > 1 && dy == 0.f) dy = fl::jiggle(myid, other, 1, step, seed), l += dy * dy;
     if (NDIM > 2 && dz == 0.f) dz = fl::jiggle(myid, other, 2, step, seed), l += dz * dz;
@@ -583,6 +588,14 @@ __device__ __forceinline__ void rare_case(const uint4 r, uint32_t top, float T0,
 
 // The walk of G consecutive sorted points (G = 32: a warp; 16: half a warp each, with its own
 // stack and batches, so that fewer points share, and pay for, one union of traversals).
+//
+// Per child and testing lane, the common case costs one theta compare (opened?), one compare
+// against the uncommon-case bound, the force and two ballots. The bound folds two tests into
+// one: a chain cell whose widest depth is too close for this point (l <= threshold at the top
+// depth) and distanceMin (l < dmin2, i.e. l <= the float below dmin2).
+// stats (STATS): [0] child tests (G per child), [1] tests a lane's own traversal needed,
+// [2] deepest stack, [3] lanes that opened a cell, [4] lanes that applied a cell or point,
+// [5] pair rounds that took the uncommon-case branch.
 template <int NDIM, int G, bool STATS, bool DMAX>
 __global__ void __launch_bounds__(kWalkThreads) k_walk(
     const float4* __restrict__ cdata, const uint2* __restrict__ cmeta,
@@ -603,11 +616,13 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
   if (!__any_sync(FL_FULL, live)) return;
   // (size / 2^k)^2 / theta^2 = T0 * 4^-k, exactly (a power-of-two scaling)
   const float T0 = (float)((double)cube[3] * (double)cube[3] / theta2);
+  // l < dmin2  <=>  l <= the largest float below dmin2 (l >= 0)
+  const float dmin_le = dmin2 > 0.f ? __uint_as_float(__float_as_uint(dmin2) - 1u) : -1.f;
   const float4 me = live ? leaf[t] : make_float4(0, 0, 0, 0);
   const uint32_t myid = live ? perm[t] : 0;
   const uint32_t slot_cap = 2u * (uint32_t)n + 1u;
   float ax = 0.f, ay = 0.f, az = 0.f, bx = 0.f, by = 0.f, bz = 0.f;
-  unsigned long long tests = 0, useful = 0;
+  unsigned long long st_tests = 0, st_useful = 0, st_open = 0, st_apply = 0, st_rare = 0;
   uint4* stk = sh.stack[warp][grp];
   if (gl == 0 && act) stk[0] = make_uint4(0u, 1u, 0u, act);  // the root: slot 0, top depth 0
   int sp = act ? 1 : 0, maxsp = sp;
@@ -615,73 +630,99 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
   uint32_t guard = 0;
   const uint32_t guard_max = 4u * (uint32_t)n + 64u;
   float4* sdata = sh.data[warp] + gbase;
-  uint4* sinfo = sh.info[warp] + gbase;
-  uint32_t* stop = sh.top[warp] + gbase;
+  uint4* stest = sh.test[warp] + gbase;
+  uint2* scold = sh.cold[warp] + gbase;
   while (__any_sync(FL_FULL, sp > 0)) {
-    // each group gathers up to G children from the top of its stack; lane gl takes the gl-th
-    int total = 0;
-    uint32_t my_slot = 0, my_mask = 0, my_top = 0;
-    while (sp > 0 && total < G) {
-      const uint4 e = stk[sp - 1];
-      uint32_t cnt = e.y;
-      if (e.x >= slot_cap || cnt > slot_cap - e.x) {  // a malformed tree: never read past it
-        if (gl == 0) atomicOr(err, FL_ERR_TREE);
-        cnt = e.x >= slot_cap ? 0u : slot_cap - e.x;
-      }
-      const uint32_t take = cnt < (uint32_t)(G - total) ? cnt : (uint32_t)(G - total);
-      if (gl >= total && gl < total + (int)take) {
-        my_slot = e.x + (uint32_t)(gl - total);
-        my_mask = e.w;
-        my_top = e.z;
-      }
-      __syncwarp(gmask);
-      if (take == cnt) {
-        --sp;
-      } else if (gl == 0) {
-        stk[sp - 1] = make_uint4(e.x + take, cnt - take, e.z, e.w);
-      }
-      total += (int)take;
-      __syncwarp(gmask);
+    // each group gathers the first G children from the top of its stack, in parallel: lane gl
+    // reads the gl-th entry from the top, a prefix sum of the entries' child counts places each
+    // entry's children in the batch, and lane gl then finds the entry of the batch's gl-th child
+    const bool has = gl < sp;
+    uint4 e = has ? stk[sp - 1 - gl] : make_uint4(0u, 0u, 0u, 0u);
+    if (has && (e.x >= slot_cap || e.y > slot_cap - e.x)) {  // a malformed tree: never read past it
+      atomicOr(err, FL_ERR_TREE);
+      e.y = e.x >= slot_cap ? 0u : slot_cap - e.x;
     }
+    uint32_t inc = e.y;
+#pragma unroll
+    for (int o = 1; o < G; o <<= 1) {
+      const uint32_t u = __shfl_up_sync(FL_FULL, inc, o, G);
+      if (gl >= o) inc += u;
+    }
+    const uint32_t exc = inc - e.y;
+    const uint32_t avail = __shfl_sync(FL_FULL, inc, G - 1, G);
+    const int total = avail < (uint32_t)G ? (int)avail : G;
+    // entries taken whole leave the stack; one taken in part keeps the rest (the new top)
+    const uint32_t taken = __ballot_sync(FL_FULL, has && inc <= (uint32_t)total) & gmask;
+    if (has && exc < (uint32_t)total && inc > (uint32_t)total)
+      stk[sp - 1 - gl] = make_uint4(e.x + ((uint32_t)total - exc), inc - (uint32_t)total, e.z, e.w);
+    sp -= __popc(taken);
+    // each entry marks where its children start; a running max carries the mark to the rest
+    uint32_t* sown = sh.own[warp] + gbase;
+    sown[gl] = 0u;
+    __syncwarp();
+    if (e.y && exc < (uint32_t)total) sown[exc] = (uint32_t)gl;
+    __syncwarp();
+    uint32_t own = sown[gl];
+#pragma unroll
+    for (int o = 1; o < G; o <<= 1) {
+      const uint32_t u = __shfl_up_sync(FL_FULL, own, o, G);
+      if (gl >= o && u > own) own = u;
+    }
+    const uint32_t own_first = __shfl_sync(FL_FULL, e.x, (int)own, G);
+    const uint32_t own_exc = __shfl_sync(FL_FULL, exc, (int)own, G);
+    const uint32_t my_mask = __shfl_sync(FL_FULL, e.w, (int)own, G);
+    const uint32_t my_top = __shfl_sync(FL_FULL, e.z, (int)own, G);
+    const uint32_t my_slot = own_first + ((uint32_t)gl - own_exc);
     __syncwarp();
     const int jmax = G == 32 ? total : (int)__reduce_max_sync(FL_FULL, (unsigned)total);
     if (gl < total) {
       // what does not depend on the testing point, once per child
       const float4 q = __ldg(cdata + my_slot);
-      uint2 m = __ldg(cmeta + my_slot);
+      const uint2 m = __ldg(cmeta + my_slot);
       const bool lf = m.y == kLeafMark;
       const uint32_t D = (m.y >> 26) & 31u;
       uint32_t mask = q.w != 0.f ? my_mask : 0u;  // d3 skips a zero value and all it holds
       if (lf && m.x - (uint32_t)base < 32u) mask &= ~(1u << (m.x - (uint32_t)base));  // itself
-      if (!lf && my_top < D) m.y |= kChain;
-      sdata[gl] = make_float4(q.x, q.y, q.z, q.w * alpha);
-      sinfo[gl] = make_uint4(__float_as_uint(lf ? -INFINITY : T0 * pow4neg(D)), mask, m.x, m.y);
-      stop[gl] = my_top;
+      const bool chain = !lf && my_top < D;
+      // a point is never approximated (its sum is the same either way); a cell is opened when
+      // even its deepest depth fails the theta test
+      const float topen = lf ? -INFINITY : T0 * pow4neg(D);
+      const float ttop = chain ? T0 * pow4neg(my_top) : topen;
+      const float va = chain ? q.w * alpha * damp(NDIM, (int)(D - my_top)) : q.w * alpha;
+      sdata[gl] = make_float4(q.x, q.y, q.z, va);
+      stest[gl] = make_uint4(__float_as_uint(topen), __float_as_uint(fmaxf(ttop, dmin_le)), mask, m.x);
+      scold[gl] = make_uint2(m.y, my_top);
     } else if (gl < ((jmax + 1) & ~1)) {  // pad the group's batch: a child no lane tests
       sdata[gl] = make_float4(0.f, 0.f, 0.f, 0.f);
-      sinfo[gl] = make_uint4(0u, 0u, 0u, kLeafMark);
+      stest[gl] = make_uint4(0u, 0u, 0u, 0u);
     }
     __syncwarp();
     for (int j = 0; j < jmax; j += 2) {  // two children per round: independent work to overlap
       const float4 q0 = sdata[j], q1 = sdata[j + 1];
-      const uint4 r0 = sinfo[j], r1 = sinfo[j + 1];
+      const uint4 r0 = stest[j], r1 = stest[j + 1];
       float dx0 = q0.x - me.x, dy0 = NDIM > 1 ? q0.y - me.y : 0.f, dz0 = NDIM > 2 ? q0.z - me.z : 0.f;
       float dx1 = q1.x - me.x, dy1 = NDIM > 1 ? q1.y - me.y : 0.f, dz1 = NDIM > 2 ? q1.z - me.z : 0.f;
       float l0 = dx0 * dx0 + dy0 * dy0 + dz0 * dz0;
       float l1 = dx1 * dx1 + dy1 * dy1 + dz1 * dz1;
-      const bool m0 = r0.y & lanebit, m1 = r1.y & lanebit;
-      // a cell not far enough even at the deepest depth of its chain is opened
+      const bool m0 = r0.z & lanebit, m1 = r1.z & lanebit;
       const bool o0 = m0 && __uint_as_float(r0.x) >= l0, o1 = m1 && __uint_as_float(r1.x) >= l1;
       const bool a0 = m0 && !o0 && (!DMAX || l0 < dmax2), a1 = m1 && !o1 && (!DMAX || l1 < dmax2);
       float v0 = q0.w, v1 = q1.w;
       const float z0 = NDIM == 3 ? dx0 * dy0 * dz0 : NDIM == 2 ? dx0 * dy0 : dx0;
       const float z1 = NDIM == 3 ? dx1 * dy1 * dz1 : NDIM == 2 ? dx1 * dy1 : dx1;
-      const bool c0 = a0 && ((int)r0.w < 0 || z0 == 0.f || l0 < dmin2);
-      const bool c1 = a1 && ((int)r1.w < 0 || z1 == 0.f || l1 < dmin2);
+      const bool c0 = a0 && (l0 <= __uint_as_float(r0.y) || z0 == 0.f);
+      const bool c1 = a1 && (l1 <= __uint_as_float(r1.y) || z1 == 0.f);
       // a warp-uniform branch: the common path never executes the uncommon code, even predicated
       if (__any_sync(FL_FULL, c0 || c1)) {
-        if (c0) rare_case<NDIM>(r0, stop[j], T0, dmin2, myid, perm, n, step, seed, v0, dx0, dy0, dz0, l0);
-        if (c1) rare_case<NDIM>(r1, stop[j + 1], T0, dmin2, myid, perm, n, step, seed, v1, dx1, dy1, dz1, l1);
+        if (STATS && lane == 0) ++st_rare;
+        if (c0) {
+          const uint2 k0 = scold[j];
+          rare_case<NDIM>(k0.x, k0.y, r0.w, T0, dmin2, myid, perm, n, step, seed, v0, dx0, dy0, dz0, l0);
+        }
+        if (c1) {
+          const uint2 k1 = scold[j + 1];
+          rare_case<NDIM>(k1.x, k1.y, r1.w, T0, dmin2, myid, perm, n, step, seed, v1, dx1, dy1, dz1, l1);
+        }
       }
       const float w0 = a0 ? __fdividef(v0, l0) : 0.f, w1 = a1 ? __fdividef(v1, l1) : 0.f;
       ax = fmaf(dx0, w0, ax), bx = fmaf(dx1, w1, bx);
@@ -691,11 +732,13 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
       const uint32_t om1 = __ballot_sync(FL_FULL, o1) & gmask;
       if (om0 | om1) {  // push the children some lanes must open (rare next to the tests)
         if (om0) {
-          if (sp < kStack && gl == 0) stk[sp] = make_uint4(r0.z, r0.w & kCountMask, ((r0.w >> 26) & 31u) + 1u, om0);
+          const uint32_t k0 = scold[j].x;
+          if (sp < kStack && gl == 0) stk[sp] = make_uint4(r0.w, k0 & kCountMask, ((k0 >> 26) & 31u) + 1u, om0);
           ++sp;
         }
         if (om1) {
-          if (sp < kStack && gl == 0) stk[sp] = make_uint4(r1.z, r1.w & kCountMask, ((r1.w >> 26) & 31u) + 1u, om1);
+          const uint32_t k1 = scold[j + 1].x;
+          if (sp < kStack && gl == 0) stk[sp] = make_uint4(r1.w, k1 & kCountMask, ((k1 >> 26) & 31u) + 1u, om1);
           ++sp;
         }
         if (sp > kStack) {
@@ -704,9 +747,14 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
         }
         if (STATS && sp > maxsp) maxsp = sp;
       }
-      if (STATS && gl == 0) {
-        if (j < total) tests += G, useful += __popc(r0.y & gmask);
-        if (j + 1 < total) tests += G, useful += __popc(r1.y & gmask);
+      if (STATS) {
+        const uint32_t ap = __ballot_sync(FL_FULL, a0) & gmask, aq = __ballot_sync(FL_FULL, a1) & gmask;
+        if (gl == 0) {
+          if (j < total) st_tests += G, st_useful += __popc(r0.z & gmask);
+          if (j + 1 < total) st_tests += G, st_useful += __popc(r1.z & gmask);
+          st_open += __popc(om0) + __popc(om1);
+          st_apply += __popc(ap) + __popc(aq);
+        }
       }
     }
     __syncwarp();
@@ -715,10 +763,15 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
       break;
     }
   }
-  if (STATS && gl == 0) {
-    atomicAdd(stats, tests);
-    atomicAdd(stats + 1, useful);
-    atomicMax(stats + 2, (unsigned long long)maxsp);
+  if (STATS) {
+    if (gl == 0) {
+      atomicAdd(stats, st_tests);
+      atomicAdd(stats + 1, st_useful);
+      atomicMax(stats + 2, (unsigned long long)maxsp);
+      atomicAdd(stats + 3, st_open);
+      atomicAdd(stats + 4, st_apply);
+    }
+    if (lane == 0) atomicAdd(stats + 5, st_rare);
   }
   if (!live) return;
   ax += bx, ay += by, az += bz;

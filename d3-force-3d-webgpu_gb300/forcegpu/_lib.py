@@ -18,6 +18,7 @@ STATUS_NAMES = ["FL_OK", "FL_E_ARG", "FL_E_OOM", "FL_E_DEVICE", "FL_E_TIMEOUT", 
                 "FL_E_STATE", "FL_E_UNSUPPORTED"]
 FORCE_TYPES = {"manyBody": 1, "link": 2, "collide": 3, "center": 4, "radial": 5, "position": 6}
 Q_LAUNCHES, Q_TICKS, Q_NODES, Q_ERRWORD, Q_DEVICE_BYTES, Q_WALK_TESTS, Q_WALK_USEFUL = 1, 2, 3, 4, 5, 6, 7
+Q_WALK_MAX_STACK, Q_WALK_OPENS, Q_WALK_APPLIES, Q_WALK_RARE = 8, 9, 10, 11
 
 # every symbol include/forcegpu.h declares
 EXPORTS = ["fl_create", "fl_destroy", "fl_last_error", "fl_fits", "fl_set_nodes",

@@ -145,12 +145,15 @@ int32_t fl_set_tuning(fl_sim* sim, int32_t key, int32_t value);
 /* The cudaStream_t every kernel of this simulation runs on. */
 int32_t fl_stream(fl_sim* sim, void** stream);
 /* Queries: FL_Q_LAUNCHES kernels launched so far, FL_Q_TICKS ticks queued so far, FL_Q_NODES,
- * FL_Q_ERRWORD the raw device error word, FL_Q_DEVICE_BYTES device memory held;
- * FL_Q_WALK_TESTS / FL_Q_WALK_USEFUL / FL_Q_WALK_MAX_STACK (profiling level 2): child tests the
- * tree walks made (32 lanes each), of those the tests a point's own d3 traversal needed, and
- * the deepest walk stack. */
+ * FL_Q_ERRWORD the raw device error word, FL_Q_DEVICE_BYTES device memory held. Walk counters,
+ * summed over the tree walks since profiling level 2 was enabled: FL_Q_WALK_TESTS child tests
+ * made (one per point of the walking group and child), FL_Q_WALK_USEFUL of those, the tests a
+ * point's own d3 traversal needed, FL_Q_WALK_MAX_STACK the deepest walk stack,
+ * FL_Q_WALK_OPENS cells opened and FL_Q_WALK_APPLIES cells or points applied (both per point),
+ * FL_Q_WALK_RARE rounds of two children that took the uncommon-case path. */
 enum { FL_Q_LAUNCHES = 1, FL_Q_TICKS = 2, FL_Q_NODES = 3, FL_Q_ERRWORD = 4, FL_Q_DEVICE_BYTES = 5,
-       FL_Q_WALK_TESTS = 6, FL_Q_WALK_USEFUL = 7, FL_Q_WALK_MAX_STACK = 8 };
+       FL_Q_WALK_TESTS = 6, FL_Q_WALK_USEFUL = 7, FL_Q_WALK_MAX_STACK = 8, FL_Q_WALK_OPENS = 9,
+       FL_Q_WALK_APPLIES = 10, FL_Q_WALK_RARE = 11 };
 int32_t fl_query(fl_sim* sim, int32_t what, int64_t* out);
 /* Per-kernel timing with CUDA events on the simulation's stream: enable (1), or enable with
  * the walk's counters too (2); then read the summed milliseconds and launch count of each
