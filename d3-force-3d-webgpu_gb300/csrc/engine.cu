@@ -524,6 +524,9 @@ int32_t collect_errors(fl_sim* s) {
 
 }  // namespace
 
+// The message fl_last_error(NULL) returns, set by entry points that take no simulation.
+void fl_set_sim_free_error(const std::string& msg) { g_create_error = msg; }
+
 extern "C" {
 
 int32_t fl_create(int32_t device, fl_sim** out) {

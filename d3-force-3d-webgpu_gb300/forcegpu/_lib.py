@@ -25,7 +25,8 @@ EXPORTS = ["fl_create", "fl_destroy", "fl_last_error", "fl_fits", "fl_set_nodes"
            "fl_update_positions", "fl_update_pins", "fl_update_velocities", "fl_set_forces",
            "fl_set_seed", "fl_enqueue", "fl_sync", "fl_idle", "fl_busy", "fl_buffers",
            "fl_stream", "fl_query", "fl_profile", "fl_profile_read", "fl_radix_sort",
-           "fl_debug_tree", "fl_set_tuning"]
+           "fl_debug_tree", "fl_set_tuning", "fl_radix_sort_noalloc"]
+SORT_NOALLOC_MAX_PAIRS = 262144  # FL_SORT_NOALLOC_MAX_PAIRS
 TUNE_WALK_GROUP = 1
 
 
@@ -92,6 +93,7 @@ def load():
         "fl_radix_sort": (I32, [P, P, I64, I32, P, P]),
         "fl_debug_tree": (I32, [P, I32, P, P, P, P, P, P]),
         "fl_set_tuning": (I32, [P, I32, I32]),
+        "fl_radix_sort_noalloc": (I32, [P, P, I64, I32, P, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -255,6 +257,16 @@ def radix_sort(keys, vals, lo_bit=0):
     if rc != FL_OK:
         raise FlError(rc, (L.fl_last_error(None) or b"").decode())
     return ko, vo
+
+
+def radix_sort_noalloc(keys_ptr, vals_ptr, n, lo_bit, keys_out_ptr, vals_out_ptr, stream=0):
+    """fl_radix_sort_noalloc on device buffers (addresses as integers): the sort without any
+    device allocation, for callers whose device memory all comes from their own pool."""
+    L = load()
+    rc = L.fl_radix_sort_noalloc(keys_ptr, vals_ptr, int(n), int(lo_bit), keys_out_ptr,
+                                 vals_out_ptr, stream)
+    if rc != FL_OK:
+        raise FlError(rc, (L.fl_last_error(None) or b"").decode())
 
 
 def desc_from_gpu(g, key, n):

@@ -172,6 +172,23 @@ int32_t fl_profile_read(fl_sim* sim, int32_t cap, const char** names, double* ms
 int32_t fl_radix_sort(const uint64_t* keys, const uint32_t* vals, int64_t n, int32_t lo_bit,
                       uint64_t* keys_out, uint32_t* vals_out);
 
+/* fl_radix_sort for callers that cannot allocate device memory: those whose device memory is
+ * all owned by their own pool or fixed budget (a renderer's or plugin host's allocator), those
+ * that must not stall the device with cudaMalloc/cudaFree, and those that must not fail for lack
+ * of memory mid-frame. No counterpart in the reference. keys/vals and keys_out/vals_out are
+ * DEVICE buffers of n pairs on the calling thread's current device (the outputs may be the
+ * inputs, sorted in place; they must not otherwise overlap); the sort runs on `stream` (NULL:
+ * the default stream) and the call returns when it has finished. Its scratch is a built-in
+ * device array of about 3.6 MB, present on every device that loads this library until the
+ * process exits, so n may not exceed FL_SORT_NOALLOC_MAX_PAIRS (FL_E_ARG otherwise). The first
+ * call on a device looks the array's address up (cudaGetSymbolAddress): make that first call
+ * before any stream capture. Calls share the array, so calls that overlap on the GPU (from
+ * several host threads, or on several streams) race and corrupt each other's results. */
+#define FL_SORT_NOALLOC_MAX_PAIRS 262144
+int32_t fl_radix_sort_noalloc(const uint64_t* keys, const uint32_t* vals, int64_t n,
+                              int32_t lo_bit, uint64_t* keys_out, uint32_t* vals_out,
+                              void* stream);
+
 /* The many-body tree the last tick built for force `index` of the list (a Barnes-Hut pass,
  * src/gpu/passes/barnesHut.js:934-1126): sorted left-aligned Morton keys [n], the sort
  * permutation [n] (node index per sorted position), and per internal node [n-1] its children
