@@ -61,6 +61,8 @@ def parse():
     p.add_argument("--nodes", type=int, default=1_000_000)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--walk-group", type=int, default=32, choices=[16, 32],
+                   help="points per tree-walk traversal (FL_TUNE_WALK_GROUP)")
     return p.parse_args()
 
 
@@ -188,7 +190,8 @@ def main():
     import forcegpu
     from forcegpu import Engine
     from forcegpu._lib import (Q_DEVICE_BYTES, Q_LAUNCHES, Q_WALK_APPLIES, Q_WALK_OPENS,
-                               Q_WALK_RARE, Q_WALK_TESTS, Q_WALK_USEFUL, desc_from_gpu)
+                               Q_WALK_RARE, Q_WALK_TESTS, Q_WALK_USEFUL, TUNE_WALK_GROUP,
+                               desc_from_gpu)
 
     n = args.nodes
     xyz, src, dst, bias, strength = workload(n)
@@ -206,6 +209,7 @@ def main():
     descs = [(d_link, keep_l), (d_charge, keep_c), (d_center, keep_x)]
     eng.set_forces(descs)
     eng.set_seed(12345)
+    eng.set_tuning(TUNE_WALK_GROUP, args.walk_group)
     decay = 0.6
     total = args.warmup + args.steps
     al, _ = alphas(total + 2 * args.steps + 9)

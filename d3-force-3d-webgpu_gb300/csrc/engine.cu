@@ -103,7 +103,7 @@ struct fl_sim {
   std::vector<std::unique_ptr<Pass>> plan;
   uint32_t seed = 0, step = 0;
   int64_t ticks = 0, launches = 0;
-  int walk_group = 16;  // points per tree-walk traversal (tuning: 16 or 32)
+  int walk_group = 32;  // points per tree-walk traversal (tuning: 16 or 32)
   bool profiling = false;
   int prof_level = 0;
   DevMem wstats;  // walk counters (profiling level 2)

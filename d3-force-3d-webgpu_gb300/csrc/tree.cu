@@ -19,17 +19,19 @@
 //              (value = sqrt(4 / 2^DIMS) times the sum of the children's values; centroid
 //              weighted by the children's |value|). When the strengths share one sign this
 //              recursion has a closed form, value(D) = sum_p s_p c^(leafDepth_p - D) and centroid
-//              weights |s_p| c^leafDepth_p, so every cell is a range sum of an FP64 prefix scan
-//              over the sorted points. With strengths of both signs the recursion itself runs,
-//              bottom-up with atomic arrival flags (FP64 sums for the top levels).
+//              weights |s_p| c^leafDepth_p, so every cell is a range sum of exact int64
+//              fixed-point prefix sums over the sorted points. With strengths of both signs the
+//              recursion itself runs, bottom-up with atomic arrival flags (FP64 sums for the top
+//              levels).
 //   slots      each cell writes its children (position or centroid, value at own depth, and for
 //              a child cell its child range and depth) into its slots
-//   walk       one warp per 32 consecutive sorted points walks the union of their d3 traversals:
-//              batches of up to 32 children are loaded lane-parallel into shared memory and
-//              every lane applies apply() of manyBody.js for its own point: a cell is
-//              approximated at the first (widest) depth of its chain where w^2 / theta^2 < l,
-//              points are summed exactly, distanceMin / distanceMax as d3; cells that some lane
-//              must open are pushed, with the mask of those lanes, on a stack in shared memory.
+//   walk       a group of G consecutive sorted points (G = 32: a warp, or 16) walks the union of
+//              their d3 traversals: batches of up to G children are gathered from the group's
+//              stack in shared memory and loaded lane-parallel, and every lane applies apply()
+//              of manyBody.js for its own point, two children per round in packed FP32 pairs:
+//              a cell is approximated at the first (widest) depth of its chain where
+//              w^2 / theta^2 < l, points are summed exactly, distanceMin / distanceMax as d3;
+//              cells that some lane must open are pushed with the mask of those lanes.
 //
 // Points with the same code at the finest level share the deepest cell as its children.
 #include <math.h>
@@ -84,11 +86,6 @@ __device__ __forceinline__ float damp(int ndim, int k) {
   const int e2 = k * (2 - ndim);
   const float odd = (e2 & 1) ? 1.41421356237309515f : 1.f;
   return ldexpf(odd, e2 >> 1);
-}
-__device__ __forceinline__ double damp64(int ndim, int k) {
-  const int e2 = k * (2 - ndim);
-  const double odd = (e2 & 1) ? 1.4142135623730951 : 1.0;
-  return ldexp(odd, e2 >> 1);
 }
 
 // (x - o) * 2^F as an exact integer: x - o is rounded once in FP32 and its rounding error
@@ -548,11 +545,45 @@ constexpr int kWalkThreads = 128;
 constexpr int kWalkWarps = kWalkThreads / 32;
 constexpr int kStack = 96;  // entries per group; the deepest stack seen at 1M nodes in 3D is 67
 
+// Packed FP32 pairs (the f32x2 arithmetic of sm_100 and later): two children per instruction.
+__device__ __forceinline__ uint64_t pk2(float a, float b) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float2 up2(uint64_t x) {
+  float2 r;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(x));
+  return r;
+}
+__device__ __forceinline__ uint64_t sub2(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ float rcp_approx(float x) {  // the reciprocal __fdividef multiplies by
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 template <int NG>
 struct WalkShared {
   uint4 stack[kWalkWarps][NG][kStack];  // per point group: first child slot, count, top depth, lanes
   // the batches, one entry per child: what every test reads ...
-  float4 data[kWalkWarps][32];  // position / centroid, value at the chain's top depth * alpha
+  // per pair of children (2j, 2j + 1): {x, x', y, y'} and {z, z', value, value'}, the value at
+  // the chain's top depth times alpha, in the packed layout the f32x2 arithmetic reads
+  float4 data[kWalkWarps][32];
   uint4 test[kWalkWarps][32];   // open threshold, uncommon-case bound, lane mask, slot / index
   // ... and what only a push or an uncommon case reads
   uint2 cold[kWalkWarps][32];   // meta word (count | depth << 26, or kLeafMark), chain top depth
@@ -621,7 +652,8 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
   const float4 me = live ? leaf[t] : make_float4(0, 0, 0, 0);
   const uint32_t myid = live ? perm[t] : 0;
   const uint32_t slot_cap = 2u * (uint32_t)n + 1u;
-  float ax = 0.f, ay = 0.f, az = 0.f, bx = 0.f, by = 0.f, bz = 0.f;
+  uint64_t AX = 0, AY = 0, AZ = 0;  // force sums, one per child of a round's pair
+  const uint64_t MX = pk2(me.x, me.x), MY = pk2(me.y, me.y), MZ = pk2(me.z, me.z);
   unsigned long long st_tests = 0, st_useful = 0, st_open = 0, st_apply = 0, st_rare = 0;
   uint4* stk = sh.stack[warp][grp];
   if (gl == 0 && act) stk[0] = make_uint4(0u, 1u, 0u, act);  // the root: slot 0, top depth 0
@@ -629,7 +661,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
   __syncwarp();
   uint32_t guard = 0;
   const uint32_t guard_max = 4u * (uint32_t)n + 64u;
-  float4* sdata = sh.data[warp] + gbase;
+  float4* spair = sh.data[warp] + gbase;
   uint4* stest = sh.test[warp] + gbase;
   uint2* scold = sh.cold[warp] + gbase;
   while (__any_sync(FL_FULL, sp > 0)) {
@@ -689,45 +721,52 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
       const float topen = lf ? -INFINITY : T0 * pow4neg(D);
       const float ttop = chain ? T0 * pow4neg(my_top) : topen;
       const float va = chain ? q.w * alpha * damp(NDIM, (int)(D - my_top)) : q.w * alpha;
-      sdata[gl] = make_float4(q.x, q.y, q.z, va);
+      float* pa = reinterpret_cast<float*>(spair + (gl & ~1));
+      pa[gl & 1] = q.x, pa[2 + (gl & 1)] = q.y, pa[4 + (gl & 1)] = q.z, pa[6 + (gl & 1)] = va;
       stest[gl] = make_uint4(__float_as_uint(topen), __float_as_uint(fmaxf(ttop, dmin_le)), mask, m.x);
       scold[gl] = make_uint2(m.y, my_top);
     } else if (gl < ((jmax + 1) & ~1)) {  // pad the group's batch: a child no lane tests
-      sdata[gl] = make_float4(0.f, 0.f, 0.f, 0.f);
+      float* pa = reinterpret_cast<float*>(spair + (gl & ~1));
+      pa[gl & 1] = 0.f, pa[2 + (gl & 1)] = 0.f, pa[4 + (gl & 1)] = 0.f, pa[6 + (gl & 1)] = 0.f;
       stest[gl] = make_uint4(0u, 0u, 0u, 0u);
     }
     __syncwarp();
     for (int j = 0; j < jmax; j += 2) {  // two children per round: independent work to overlap
-      const float4 q0 = sdata[j], q1 = sdata[j + 1];
+      const float4 pa = spair[j], pb = spair[j + 1];
       const uint4 r0 = stest[j], r1 = stest[j + 1];
-      float dx0 = q0.x - me.x, dy0 = NDIM > 1 ? q0.y - me.y : 0.f, dz0 = NDIM > 2 ? q0.z - me.z : 0.f;
-      float dx1 = q1.x - me.x, dy1 = NDIM > 1 ? q1.y - me.y : 0.f, dz1 = NDIM > 2 ? q1.z - me.z : 0.f;
-      float l0 = dx0 * dx0 + dy0 * dy0 + dz0 * dz0;
-      float l1 = dx1 * dx1 + dy1 * dy1 + dz1 * dz1;
+      uint64_t DX = sub2(pk2(pa.x, pa.y), MX);
+      uint64_t DY = NDIM > 1 ? sub2(pk2(pa.z, pa.w), MY) : 0ull;
+      uint64_t DZ = NDIM > 2 ? sub2(pk2(pb.x, pb.y), MZ) : 0ull;
+      uint64_t L = mul2(DX, DX);
+      if (NDIM > 1) L = fma2(DY, DY, L);
+      if (NDIM > 2) L = fma2(DZ, DZ, L);
+      const float2 zp = up2(NDIM == 3 ? mul2(mul2(DX, DY), DZ) : NDIM == 2 ? mul2(DX, DY) : DX);
+      float2 l = up2(L);
       const bool m0 = r0.z & lanebit, m1 = r1.z & lanebit;
-      const bool o0 = m0 && __uint_as_float(r0.x) >= l0, o1 = m1 && __uint_as_float(r1.x) >= l1;
-      const bool a0 = m0 && !o0 && (!DMAX || l0 < dmax2), a1 = m1 && !o1 && (!DMAX || l1 < dmax2);
-      float v0 = q0.w, v1 = q1.w;
-      const float z0 = NDIM == 3 ? dx0 * dy0 * dz0 : NDIM == 2 ? dx0 * dy0 : dx0;
-      const float z1 = NDIM == 3 ? dx1 * dy1 * dz1 : NDIM == 2 ? dx1 * dy1 : dx1;
-      const bool c0 = a0 && (l0 <= __uint_as_float(r0.y) || z0 == 0.f);
-      const bool c1 = a1 && (l1 <= __uint_as_float(r1.y) || z1 == 0.f);
+      const bool o0 = m0 && __uint_as_float(r0.x) >= l.x, o1 = m1 && __uint_as_float(r1.x) >= l.y;
+      const bool a0 = m0 && !o0 && (!DMAX || l.x < dmax2), a1 = m1 && !o1 && (!DMAX || l.y < dmax2);
+      float v0 = pb.z, v1 = pb.w;
+      const bool c0 = a0 && (l.x <= __uint_as_float(r0.y) || zp.x == 0.f);
+      const bool c1 = a1 && (l.y <= __uint_as_float(r1.y) || zp.y == 0.f);
       // a warp-uniform branch: the common path never executes the uncommon code, even predicated
       if (__any_sync(FL_FULL, c0 || c1)) {
         if (STATS && lane == 0) ++st_rare;
+        float2 dx = up2(DX), dy = up2(DY), dz = up2(DZ);
         if (c0) {
           const uint2 k0 = scold[j];
-          rare_case<NDIM>(k0.x, k0.y, r0.w, T0, dmin2, myid, perm, n, step, seed, v0, dx0, dy0, dz0, l0);
+          rare_case<NDIM>(k0.x, k0.y, r0.w, T0, dmin2, myid, perm, n, step, seed, v0, dx.x, dy.x, dz.x, l.x);
         }
         if (c1) {
           const uint2 k1 = scold[j + 1];
-          rare_case<NDIM>(k1.x, k1.y, r1.w, T0, dmin2, myid, perm, n, step, seed, v1, dx1, dy1, dz1, l1);
+          rare_case<NDIM>(k1.x, k1.y, r1.w, T0, dmin2, myid, perm, n, step, seed, v1, dx.y, dy.y, dz.y, l.y);
         }
+        DX = pk2(dx.x, dx.y), DY = pk2(dy.x, dy.y), DZ = pk2(dz.x, dz.y);
       }
-      const float w0 = a0 ? __fdividef(v0, l0) : 0.f, w1 = a1 ? __fdividef(v1, l1) : 0.f;
-      ax = fmaf(dx0, w0, ax), bx = fmaf(dx1, w1, bx);
-      if (NDIM > 1) ay = fmaf(dy0, w0, ay), by = fmaf(dy1, w1, by);
-      if (NDIM > 2) az = fmaf(dz0, w0, az), bz = fmaf(dz1, w1, bz);
+      const float2 w = up2(mul2(pk2(v0, v1), pk2(rcp_approx(l.x), rcp_approx(l.y))));
+      const uint64_t W = pk2(a0 ? w.x : 0.f, a1 ? w.y : 0.f);
+      AX = fma2(DX, W, AX);
+      if (NDIM > 1) AY = fma2(DY, W, AY);
+      if (NDIM > 2) AZ = fma2(DZ, W, AZ);
       const uint32_t om0 = __ballot_sync(FL_FULL, o0) & gmask;
       const uint32_t om1 = __ballot_sync(FL_FULL, o1) & gmask;
       if (om0 | om1) {  // push the children some lanes must open (rare next to the tests)
@@ -774,7 +813,8 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
     if (lane == 0) atomicAdd(stats + 5, st_rare);
   }
   if (!live) return;
-  ax += bx, ay += by, az += bz;
+  const float2 ax2 = up2(AX), ay2 = up2(AY), az2 = up2(AZ);
+  const float ax = ax2.x + ax2.y, ay = ay2.x + ay2.y, az = az2.x + az2.y;
   float4 v = vel[myid];
   v.x += ax;
   if (NDIM > 1) v.y += ay;

@@ -138,7 +138,7 @@ int32_t fl_buffers(fl_sim* sim, fl_buffer_info* out);
 
 /* Tuning parameters (no reference counterpart; the reference's closest are its fixed
  * constants, e.g. src/gpu/passes/barnesHut.js:49-58): FL_TUNE_WALK_GROUP, points that share one
- * tree-walk traversal, 16 (default) or 32. */
+ * tree-walk traversal, 16 or 32 (default). */
 enum { FL_TUNE_WALK_GROUP = 1 };
 int32_t fl_set_tuning(fl_sim* sim, int32_t key, int32_t value);
 
