@@ -48,6 +48,9 @@ BYTES_PER_NODE_TICK = 64 + 4 + 140 + 4 + 48
 # the walk's compulsory traffic per point: its sorted point (16) and permutation entry (4),
 # the child slots of the tree read once (24 B x ~2 per point), the velocity read + write (32)
 WALK_BYTES_PER_NODE = 16 + 4 + 48 + 32
+# DRAM bytes (read + write) of one walk launch at the default 1M-node workload, from ncu
+# (profiles/walk_1m_3d.md); reported as the roofline's measured traffic at that size only
+WALK_DRAM_BYTES_1M = 74.3e6
 FLOPS_PER_INTERACTION = 20  # FP32 ops per accepted cell or point interaction
 FLOPS_PER_OPEN = 8          # per opened-cell test
 
@@ -290,7 +293,7 @@ def main():
     achieved = walk_bytes / (walk_avg * 1e-3) / 1e9 if walk_avg else None
     roof = {"bound": "hbm", "kernel": "k_walk", "achieved": achieved, "peak": peaks["hbm_gbs"],
             "unit": "GB/s", "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
-            "traffic": None, "peak_kind": peak_kind,
+            "traffic": WALK_DRAM_BYTES_1M if n == 1_000_000 else None, "peak_kind": peak_kind,
             "algorithmic_bytes_per_launch": walk_bytes, "avg_launch_ms": walk_avg,
             "tick_bytes": BYTES_PER_NODE_TICK * n,
             "tick_hbm_frac": BYTES_PER_NODE_TICK * n / (ms_tick * 1e-3) / 1e9 / peaks["hbm_gbs"]}

@@ -365,7 +365,7 @@ void encode_manybody(fl_sim* s, Pass* p, float alpha, const FlReduce* box) {
   }
   {
     Scope sc(s, G_AGGREGATE);
-    fl_launch_aggregate(t, !p->mixed, p->sign, p->cube.as<float>(), p->fx_exp,
+    fl_launch_aggregate(t, p->sb.keys[r], !p->mixed, p->sign, p->cube.as<float>(), p->fx_exp,
                         s->errw.as<uint32_t>(), s->st, &s->launches);
   }
   {

@@ -19,7 +19,9 @@ struct FlSortBufs {
   int64_t cap;         // pairs the buffers hold
   int64_t tiles_cap;
 };
-int fl_sort_tile();  // pairs per onesweep tile
+constexpr int kSortThreads = 256, kSortItems = 16;  // threads of a onesweep tile, pairs each
+constexpr int kSortTile = kSortThreads * kSortItems;  // pairs per onesweep tile
+int fl_sort_tile();  // kSortTile
 size_t fl_sort_bytes(int64_t n);
 // Carve the buffers out of one allocation of fl_sort_bytes(n) bytes.
 void fl_sort_carve(FlSortBufs* b, void* base, int64_t n);
@@ -79,6 +81,8 @@ struct FlTreeBufs {
   void* scan_scratch;
   double* wsum;          // [5n] per sorted point |a|, |a| x, |a| y, |a| z, a; then their prefix sums
   double* wtiles;        // [5 tiles] partial sums of the prefix scan
+  uint32_t* omask;       // [n-1] occupied octants of each head's cell
+  uint32_t* head_of;     // [2n-1] d3 child: its head | octant << 27 | 1 << 31 (internal, then points)
 };
 struct FlWalkParams {
   float thresh[32];   // (cube size / 2^k)^2 / theta^2
@@ -101,8 +105,9 @@ void fl_launch_build(const FlTreeBufs* t, const uint64_t* skeys, const uint32_t*
                      int fx_exp, cudaStream_t st, int64_t* launches);
 // Heads, child counts and slots; cell values and centroids in closed form (strengths of one
 // sign, fixed-point sums at scale 2^fx_exp) or by the bottom-up recursion (both signs).
-void fl_launch_aggregate(const FlTreeBufs* t, bool closed, float sign, const float* cube,
-                         int fx_exp, uint32_t* err, cudaStream_t st, int64_t* launches);
+void fl_launch_aggregate(const FlTreeBufs* t, const uint64_t* skeys, bool closed, float sign,
+                         const float* cube, int fx_exp, uint32_t* err, cudaStream_t st,
+                         int64_t* launches);
 // Scale exponent of the fixed-point cell sums: no sum over n points of weight <= wmax overflows.
 int fl_fixed_exponent(int64_t n, double wmax);
 // stats (optional): [0] child tests made by the warps (32 per child), [1] of those, tests by a

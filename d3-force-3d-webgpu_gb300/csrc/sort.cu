@@ -3,7 +3,7 @@
 // Replaces the reference's three-dispatch-per-digit sort (src/gpu/sort.js:4-20, 139-190) with
 // the GB300 form of Adinets & Merrill's "Onesweep" (2022): the digit histograms of every pass
 // come from one read of the keys (fused into the key producer where possible); each pass is one
-// kernel that ranks a tile of 4096 keys by digit with warp match (__match_any_sync), publishes
+// kernel that ranks a tile of kSortTile keys by digit with warp match (__match_any_sync), publishes
 // the tile's digit counts, and takes its global offsets from a decoupled look-back over the
 // preceding tiles (bounded: a wait gives up after FL_SPIN_LIMIT polls and raises an error bit
 // instead of hanging); keys are then staged in shared memory in digit order and written out in
@@ -12,10 +12,10 @@
 
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = kSortThreads;
 constexpr int kWarps = kThreads / 32;
-constexpr int kItems = 16;
-constexpr int kTile = kThreads * kItems;
+constexpr int kItems = kSortItems;
+constexpr int kTile = kSortTile;
 constexpr uint32_t kValMask = (1u << 30) - 1;
 constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagPre = 2u << 30;

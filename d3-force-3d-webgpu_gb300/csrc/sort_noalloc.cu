@@ -25,7 +25,7 @@ void fl_set_sim_free_error(const std::string& msg);  // engine.cu: the message o
 namespace {
 
 constexpr int64_t kMaxPairs = FL_SORT_NOALLOC_MAX_PAIRS;
-constexpr int64_t kTile = 4096;  // pairs per onesweep tile (checked against fl_sort_tile())
+constexpr int64_t kTile = kSortTile;  // pairs per onesweep tile
 constexpr int64_t kTiles = (kMaxPairs + kTile - 1) / kTile;
 constexpr size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
 constexpr size_t kErrOff = 0;
@@ -61,7 +61,6 @@ int32_t scratch_of_current_device(char** out) {
   if (dev < 0 || dev >= kMaxDevices) return fail(FL_E_DEVICE, "device index out of range");
   std::lock_guard<std::mutex> g(g_setup_lock);
   if (!g_scratch_ptr[dev]) {
-    if (fl_sort_tile() != kTile) return fail(FL_E_STATE, "sort tile size differs from the scratch layout");
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_sort_scratch);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress");

@@ -323,14 +323,55 @@ __device__ __forceinline__ uint32_t for_children(uint32_t i, int D, int L,
   return c;
 }
 
-// Whether internal node i heads a d3 cell, and how many d3 children that cell has; the counts'
-// exclusive prefix within the block (first[]) and the block's total (ctot[]), for the slots.
+// Every binary node below the root that is a d3 child (a point, or an internal node deeper than
+// its parent: the first node of another cell) finds the head of its parent's cell, climbing the
+// binary nodes of equal depth, and marks its octant (its keys' digit at the parent's depth) in
+// the head's octant mask. head_of[] keeps head | octant << 27 | 1 << 31 for the slots.
+// Threads [0, n-1) take the internal nodes, [n-1, 2n-1) the points (sorted order).
+__global__ void __launch_bounds__(kThreads) k_frontier(
+    int n, int ndim, const uint64_t* __restrict__ skeys, const uint32_t* __restrict__ parent,
+    const uint32_t* __restrict__ leaf_parent, const uint32_t* __restrict__ range,
+    const uint8_t* __restrict__ depth, uint32_t* __restrict__ omask,
+    uint32_t* __restrict__ head_of, uint32_t* err) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 2 * n - 1) return;
+  const bool pt = t >= n - 1;
+  const uint32_t x = pt ? (uint32_t)(t - (n - 1)) : (uint32_t)t;
+  uint32_t rec = 0;
+  if (pt || x != 0) {
+    const uint32_t p = pt ? leaf_parent[x] : parent[x];
+    const int Dp = depth[p];
+    if (pt || depth[x] > Dp) {
+      uint32_t h = p;
+      for (int guard = 0; h != 0; ++guard) {  // equal depths: splits inside one cell
+        const uint32_t up = parent[h];
+        if (depth[up] < Dp) break;
+        h = up;
+        if (guard > 64) {
+          atomicOr(err, FL_ERR_TREE);
+          break;
+        }
+      }
+      uint32_t oct = 0;
+      if (Dp < levels_of(ndim)) {
+        const uint64_t k = skeys[pt ? x : range[2 * x]];
+        oct = (uint32_t)(k >> (64 - ndim * (Dp + 1))) & ((1u << ndim) - 1u);
+        atomicOr(omask + h, 1u << oct);
+      }
+      rec = h | (oct << 27) | 0x80000000u;
+    }
+  }
+  head_of[t] = rec;
+}
+
+// Whether internal node i heads a d3 cell, and how many d3 children that cell has (its occupied
+// octants; at the deepest level, where the keys are equal, its points); the counts' exclusive
+// prefix within the block (first[]) and the block's total (ctot[]), for the slots.
 __global__ void __launch_bounds__(kThreads) k_heads(int n, int ndim,
-                                                    const uint32_t* __restrict__ left,
-                                                    const uint32_t* __restrict__ right,
                                                     const uint32_t* __restrict__ parent,
                                                     const uint32_t* __restrict__ range,
                                                     const uint8_t* __restrict__ depth,
+                                                    const uint32_t* __restrict__ omask,
                                                     uint32_t* __restrict__ count,
                                                     uint32_t* __restrict__ first,
                                                     uint32_t* __restrict__ ctot) {
@@ -340,9 +381,7 @@ __global__ void __launch_bounds__(kThreads) k_heads(int n, int ndim,
   if (i < n - 1) {
     const int D = depth[i];
     const bool head = i == 0 || depth[parent[i]] < D;
-    c = head ? for_children(i, D, levels_of(ndim), left, right, range, depth,
-                            [](uint32_t, uint32_t) {})
-             : 0u;
+    if (head) c = D >= levels_of(ndim) ? range[2 * i + 1] - range[2 * i] + 1 : __popc(omask[i]);
     count[i] = c;
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -507,38 +546,42 @@ __global__ void __launch_bounds__(kThreads) k_cells_climb(
   }
 }
 
-// Every head writes its children into its slots; the root also fills slot 0.
+// Every d3 child writes itself into its slot of its head's cell: the head's first slot plus the
+// child's rank (occupied octants before its own; at the deepest level, its place in the range);
+// the root also fills slot 0. Threads as in k_frontier.
 __global__ void __launch_bounds__(kThreads) k_slots(
-    int n, int ndim, const uint32_t* __restrict__ left, const uint32_t* __restrict__ right,
+    int n, int ndim, const uint32_t* __restrict__ head_of, const uint32_t* __restrict__ omask,
     const uint32_t* __restrict__ range, const uint8_t* __restrict__ depth,
     const uint32_t* __restrict__ count, const uint32_t* __restrict__ first,
     const uint32_t* __restrict__ ctot, const float4* __restrict__ cell,
     const float4* __restrict__ leaf, float4* __restrict__ cdata, uint2* __restrict__ cmeta,
     uint32_t* err) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n - 1) return;
-  const uint32_t cnt = count[i];
-  if (!cnt) return;
-  const int D = depth[i], L = levels_of(ndim);
-  const uint32_t slot0 = first_slot(first, ctot, (uint32_t)i);
-  if ((uint64_t)slot0 + cnt > 2ull * (uint64_t)n + 1ull || D > L) {  // a malformed tree
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 2 * n - 1) return;
+  const bool pt = t >= n - 1;
+  const uint32_t x = pt ? (uint32_t)(t - (n - 1)) : (uint32_t)t;
+  if (!pt && x == 0) {
+    cdata[0] = cell[0];
+    cmeta[0] = make_uint2(first_slot(first, ctot, 0u), count[0] | ((uint32_t)depth[0] << 26));
+  }
+  const uint32_t rec = head_of[t];
+  if (!(rec & 0x80000000u)) return;
+  const uint32_t h = rec & kCountMask, oct = (rec >> 27) & 15u;
+  const uint32_t rank = depth[h] >= levels_of(ndim)
+                            ? (pt ? x : range[2 * x]) - range[2 * h]
+                            : (uint32_t)__popc(omask[h] & ((1u << oct) - 1u));
+  const uint32_t slot = first_slot(first, ctot, h) + rank;
+  if (rank >= count[h] || slot >= 2u * (uint32_t)n + 1u) {  // a malformed tree
     atomicOr(err, FL_ERR_TREE);
     return;
   }
-  if (i == 0) {
-    cdata[0] = cell[0];
-    cmeta[0] = make_uint2(slot0, cnt | ((uint32_t)D << 26));
+  if (pt) {
+    cdata[slot] = leaf[x];
+    cmeta[slot] = make_uint2(x, kLeafMark);
+  } else {
+    cdata[slot] = cell[x];
+    cmeta[slot] = make_uint2(first_slot(first, ctot, x), count[x] | ((uint32_t)depth[x] << 26));
   }
-  for_children(i, D, L, left, right, range, depth, [&](uint32_t x, uint32_t j) {
-    if (j >= cnt) return;
-    if (x & kLeaf) {
-      cdata[slot0 + j] = leaf[x & kIndex];
-      cmeta[slot0 + j] = make_uint2(x & kIndex, kLeafMark);
-    } else {
-      cdata[slot0 + j] = cell[x];
-      cmeta[slot0 + j] = make_uint2(first_slot(first, ctot, x), count[x] | ((uint32_t)depth[x] << 26));
-    }
-  });
 }
 
 constexpr int kWalkThreads = 128;
@@ -888,7 +931,7 @@ size_t fl_tree_bytes(int64_t n) {
   return align256(4 * m) * 3 + align256(4 * N) + align256(8 * m) + align256(m) +
          align256(4 * m) * 3 + align256(16 * m) + align256(16 * N) + align256(16 * (2 * N + 1)) +
          align256(8 * (2 * N + 1)) + align256(4 * blocks) + align256(32 * N) +
-         align256(32 * blocks) + 256;
+         align256(32 * blocks) + align256(4 * m) + align256(4 * (2 * N)) + 256;
 }
 
 void fl_tree_carve(FlTreeBufs* t, void* base, int64_t n, int ndim) {
@@ -919,6 +962,8 @@ void fl_tree_carve(FlTreeBufs* t, void* base, int64_t n, int ndim) {
   t->scan_scratch = take(4 * blocks);  // per-block totals of the child counts
   t->wsum = (double*)take(32 * N);
   t->wtiles = (double*)take(32 * blocks);  // per-block totals of the point records
+  t->omask = (uint32_t*)take(4 * m);
+  t->head_of = (uint32_t*)take(4 * (2 * N));
 }
 
 void fl_launch_morton(const float4* pos, int n, int ndim, const FlReduce* red, uint64_t* keys,
@@ -954,15 +999,19 @@ void fl_launch_build(const FlTreeBufs* t, const uint64_t* skeys, const uint32_t*
   }
 }
 
-void fl_launch_aggregate(const FlTreeBufs* t, bool closed, float sign, const float* cube,
-                         int fx_exp, uint32_t* err, cudaStream_t st, int64_t* launches) {
+void fl_launch_aggregate(const FlTreeBufs* t, const uint64_t* skeys, bool closed, float sign,
+                         const float* cube, int fx_exp, uint32_t* err, cudaStream_t st,
+                         int64_t* launches) {
   const int n = t->n, m = n - 1;
-  const int g = (m + kThreads - 1) / kThreads;
+  const int g = (m + kThreads - 1) / kThreads, g2 = (2 * n - 1 + kThreads - 1) / kThreads;
   uint32_t* ctot = static_cast<uint32_t*>(t->scan_scratch);
-  k_heads<<<g, kThreads, 0, st>>>(n, t->ndim, t->left, t->right, t->parent, t->range, t->depth,
-                                  t->count, t->first, ctot);
+  cudaMemsetAsync(t->omask, 0, 4 * (size_t)m, st);
+  k_frontier<<<g2, kThreads, 0, st>>>(n, t->ndim, skeys, t->parent, t->leaf_parent, t->range,
+                                      t->depth, t->omask, t->head_of, err);
+  k_heads<<<g, kThreads, 0, st>>>(n, t->ndim, t->parent, t->range, t->depth, t->omask, t->count,
+                                  t->first, ctot);
   k_top_u32<<<1, kThreads, 0, st>>>(ctot, g);
-  *launches += 2;
+  *launches += 3;
   if (closed) {
     k_cells_closed<<<g, kThreads, 0, st>>>(n, t->ndim, sign, t->range, t->depth, t->count,
                                            reinterpret_cast<const D4*>(t->wsum),
@@ -976,9 +1025,9 @@ void fl_launch_aggregate(const FlTreeBufs* t, bool closed, float sign, const flo
         t->flag, t->cell, t->leaf, err);
     ++*launches;
   }
-  k_slots<<<g, kThreads, 0, st>>>(n, t->ndim, t->left, t->right, t->range, t->depth, t->count,
-                                  t->first, ctot, t->cell, t->leaf, t->child_data, t->child_meta,
-                                  err);
+  k_slots<<<g2, kThreads, 0, st>>>(n, t->ndim, t->head_of, t->omask, t->range, t->depth,
+                                   t->count, t->first, ctot, t->cell, t->leaf, t->child_data,
+                                   t->child_meta, err);
   ++*launches;
 }
 
