@@ -12,14 +12,24 @@ inline int grid_for(int n, int per_block) {
   return g;
 }
 
-// Bounding box (ordered-uint atomics) and FP64 sum of the positions, one pass.
+// Knuth's TwoSum: s + x = t + e exactly, t = fl(s + x).
+__device__ __forceinline__ void two_sum(float s, float x, float& t, float& e) {
+  t = s + x;
+  const float bp = t - s;
+  e = (s - (t - bp)) + (x - bp);
+}
+
+// Bounding box (ordered-uint atomics) and sum of the positions, one pass.
 // d3 computes the cube from the extent of the points (d3-octree cover) and the centre force
-// sums positions in FP64 (src/center.js:8-26); both come from this one read.
+// sums positions in FP64 (src/center.js:8-26); both come from this one read. Each thread sums
+// its positions as an FP32 value plus an FP32 compensation (TwoSum: every rounding error is
+// kept), about 48 bits, and only the per-thread totals are added in FP64, which runs at a
+// small fraction of the FP32 rate on this part.
 __global__ void __launch_bounds__(kThreads) k_reduce(const float4* __restrict__ pos, int n,
                                                      int ndim, int want_box, int want_sum,
                                                      FlReduce* red) {
   float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-  double sum[3] = {0, 0, 0};
+  float fs[3] = {0.f, 0.f, 0.f}, fc[3] = {0.f, 0.f, 0.f};
   // a few blocks, many positions per thread: the warp shuffles and atomics of the reduction
   // are paid once per warp, not per handful of positions
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -29,9 +39,15 @@ __global__ void __launch_bounds__(kThreads) k_reduce(const float4* __restrict__ 
     for (int k = 0; k < 3; ++k) {
       lo[k] = fminf(lo[k], c[k]);
       hi[k] = fmaxf(hi[k], c[k]);
+      if (want_sum) {
+        float t, e;
+        two_sum(fs[k], c[k], t, e);
+        fs[k] = t, fc[k] += e;
+      }
     }
-    if (want_sum) sum[0] += (double)c[0], sum[1] += (double)c[1], sum[2] += (double)c[2];
   }
+  double sum[3] = {(double)fs[0] + (double)fc[0], (double)fs[1] + (double)fc[1],
+                   (double)fs[2] + (double)fc[2]};
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
 #pragma unroll
@@ -62,30 +78,40 @@ __global__ void __launch_bounds__(kThreads) k_reduce(const float4* __restrict__ 
   }
 }
 
-// The centre force's shift, (mean - c) * strength per active axis, computed once per block
-// (FP64 divisions are slow on this part) and shared.
+// The centre force's shift, (mean - c) * strength per active axis, computed in FP64 once per
+// block and shared as a pair of floats (hi + lo), which the threads subtract in FP32.
 __device__ __forceinline__ void center_shift(const FlReduce* red, int n, int ndim, double cx,
-                                             double cy, double cz, double strength, double* sh) {
-  __shared__ double s_shift[3];
+                                             double cy, double cz, double strength, float2* sh) {
+  __shared__ float2 s_shift[3];
   if (threadIdx.x < 3) {
     const int k = threadIdx.x;
     const double c = k == 0 ? cx : k == 1 ? cy : cz;
-    s_shift[k] = k < ndim ? (red->sum[k] / n - c) * strength : 0.0;
+    const double d = k < ndim ? (red->sum[k] / n - c) * strength : 0.0;
+    const float h = (float)d;
+    s_shift[k] = make_float2(h, (float)(d - (double)h));
   }
   __syncthreads();
   sh[0] = s_shift[0], sh[1] = s_shift[1], sh[2] = s_shift[2];
 }
 
+// x - (hi + lo), rounded once in all but the rarest cases: the first subtraction's rounding
+// error is recovered exactly (TwoSum) and folded in with lo
+__device__ __forceinline__ float sub_shift(float x, float2 s) {
+  float t, e;
+  two_sum(x, -s.x, t, e);
+  return t + (e - s.y);
+}
+
 __global__ void k_center_apply(float4* __restrict__ pos, int n, int ndim, const FlReduce* red,
                                double cx, double cy, double cz, double strength) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double sh[3];
+  float2 sh[3];
   center_shift(red, n, ndim, cx, cy, cz, strength, sh);
   if (i >= n) return;
   float4 p = pos[i];
-  p.x = (float)((double)p.x - sh[0]);
-  p.y = (float)((double)p.y - sh[1]);
-  p.z = (float)((double)p.z - sh[2]);
+  p.x = sub_shift(p.x, sh[0]);
+  p.y = sub_shift(p.y, sh[1]);
+  p.z = sub_shift(p.z, sh[2]);
   pos[i] = p;
 }
 
@@ -100,14 +126,14 @@ __global__ void __launch_bounds__(kThreads) k_integrate(float4* __restrict__ pos
                                                         double cx, double cy, double cz,
                                                         double strength) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double sh[3] = {0, 0, 0};
+  float2 sh[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
   if (red) center_shift(red, n, ndim, cx, cy, cz, strength, sh);  // block-uniform branch
   if (i >= n) return;
   float4 p = pos[i], v = vel[i];
   if (red) {
-    p.x = (float)((double)p.x - sh[0]);
-    p.y = (float)((double)p.y - sh[1]);
-    p.z = (float)((double)p.z - sh[2]);
+    p.x = sub_shift(p.x, sh[0]);
+    p.y = sub_shift(p.y, sh[1]);
+    p.z = sub_shift(p.z, sh[2]);
   }
   uint32_t m = mask[i];
   v.x *= decay, v.y *= decay, v.z *= decay;
