@@ -19,7 +19,7 @@ struct FlSortBufs {
   int64_t cap;         // pairs the buffers hold
   int64_t tiles_cap;
 };
-constexpr int kSortThreads = 256, kSortItems = 16;  // threads of a onesweep tile, pairs each
+constexpr int kSortThreads = 512, kSortItems = 8;  // threads of a onesweep tile, pairs each
 constexpr int kSortTile = kSortThreads * kSortItems;  // pairs per onesweep tile
 int fl_sort_tile();  // kSortTile
 size_t fl_sort_bytes(int64_t n);
@@ -32,11 +32,6 @@ void fl_sort_histogram(const FlSortBufs* b, int64_t n, int lo_bit, cudaStream_t 
 // Run the passes from keys[0]/vals[0]; returns which buffer (0/1) holds the result.
 int fl_sort_passes(const FlSortBufs* b, int64_t n, int lo_bit, uint32_t* err, cudaStream_t st,
                    int64_t* launches);
-
-// Single-pass exclusive scan of n uint32 values (decoupled look-back); out[i] = base + sum(in[<i]).
-size_t fl_scan_bytes(int64_t n);
-void fl_scan_exclusive(const uint32_t* in, uint32_t* out, int64_t n, uint32_t base, void* scratch,
-                       uint32_t* err, cudaStream_t st, int64_t* launches);
 
 // ---------------------------------------------------------------- state kernels (state.cu)
 void fl_launch_reduce(const float4* pos, int n, int ndim, int want_box, int want_sum,

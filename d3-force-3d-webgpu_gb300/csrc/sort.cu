@@ -1,4 +1,4 @@
-// Onesweep LSD radix sort of (uint64 key, uint32 value) pairs, and a single-pass exclusive scan.
+// Onesweep LSD radix sort of (uint64 key, uint32 value) pairs.
 //
 // Replaces the reference's three-dispatch-per-digit sort (src/gpu/sort.js:4-20, 139-190) with
 // the GB300 form of Adinets & Merrill's "Onesweep" (2022): the digit histograms of every pass
@@ -20,7 +20,7 @@ constexpr uint32_t kValMask = (1u << 30) - 1;
 constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagPre = 2u << 30;
 
-// Block-wide exclusive scan of one value per thread (256 threads); returns the exclusive prefix,
+// Block-wide exclusive scan of one value per thread (kThreads); returns the exclusive prefix,
 // and the block total in *total.
 __device__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_warp, uint32_t* total) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -84,7 +84,10 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(
   if (tid == 0) s_tile = atomicAdd(ticket, 1u);
   for (int i = tid; i < kWarps * 256; i += kThreads) (&s_whist[0][0])[i] = 0;
   uint32_t total;
-  s_gexcl[tid] = block_excl_scan(ghist[tid], s_warp, &total);  // syncs inside
+  // digit-wise phases: threads 0..255 take one digit each (a block of 256 or more threads)
+  const bool dt = tid < 256;
+  const uint32_t gx = block_excl_scan(dt ? ghist[tid] : 0u, s_warp, &total);  // syncs inside
+  if (dt) s_gexcl[tid] = gx;
   const uint32_t tile = s_tile;
   const int64_t tbase = (int64_t)tile * kTile;
 
@@ -120,21 +123,24 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(
   }
   __syncthreads();
 
-  // per digit (one thread each): exclusive prefix over warps, the tile's count
-  const uint32_t d = tid;
+  // per digit: exclusive prefix over warps, the tile's count
+  const uint32_t d = dt ? (uint32_t)tid : 0u;
   uint32_t run = 0;
-#pragma unroll
-  for (int w = 0; w < kWarps; ++w) {
-    uint32_t t = s_whist[w][d];
-    s_whist[w][d] = run;
-    run += t;
-  }
   uint32_t* mine = status + (size_t)tile * 256 + d;
-  fl::st_relaxed(mine, (tile == 0 ? kFlagPre : kFlagAgg) | run);
-  s_texcl[d] = block_excl_scan(run, s_warp, &total);
+  if (dt) {
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) {
+      uint32_t t = s_whist[w][d];
+      s_whist[w][d] = run;
+      run += t;
+    }
+    fl::st_relaxed(mine, (tile == 0 ? kFlagPre : kFlagAgg) | run);
+  }
+  const uint32_t tx = block_excl_scan(run, s_warp, &total);
+  if (dt) s_texcl[d] = tx;
 
   uint32_t prefix = 0;
-  if (tile > 0) {
+  if (dt && tile > 0) {
     // look back four tiles per round (independent loads), up to the nearest inclusive prefix
     int64_t p = (int64_t)tile - 1;
     uint32_t spins = 0;
@@ -167,7 +173,7 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(
     }
     fl::st_relaxed(mine, kFlagPre | (prefix + run));
   }
-  s_base[d] = s_gexcl[d] + prefix - s_texcl[d];
+  if (dt) s_base[d] = s_gexcl[d] + prefix - s_texcl[d];
   __syncthreads();
 
 #pragma unroll
@@ -187,63 +193,6 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(
       kout[g] = k;
       vout[g] = sv[i];
     }
-  }
-}
-
-constexpr int kScanItems = 8;
-constexpr int kScanTile = kThreads * kScanItems;
-
-__global__ void __launch_bounds__(kThreads) k_scan(const uint32_t* __restrict__ in,
-                                                   uint32_t* __restrict__ out, int64_t n,
-                                                   uint32_t base, uint32_t* status,
-                                                   uint32_t* ticket, uint32_t* err) {
-  __shared__ uint32_t s_warp[kWarps];
-  __shared__ uint32_t s_tile, s_prefix;
-  const int tid = threadIdx.x;
-  if (tid == 0) s_tile = atomicAdd(ticket, 1u);
-  __syncthreads();
-  const uint32_t tile = s_tile;
-  const int64_t first = (int64_t)tile * kScanTile + (int64_t)tid * kScanItems;
-  uint32_t v[kScanItems], sum = 0;
-#pragma unroll
-  for (int j = 0; j < kScanItems; ++j) {
-    v[j] = first + j < n ? in[first + j] : 0;
-    sum += v[j];
-  }
-  uint32_t total;
-  uint32_t before = block_excl_scan(sum, s_warp, &total);
-  if (tid == 0) {
-    uint32_t* mine = status + tile;
-    fl::st_relaxed(mine, (tile == 0 ? kFlagPre : kFlagAgg) | total);
-    uint32_t prefix = 0;
-    if (tile > 0) {
-      int64_t p = (int64_t)tile - 1;
-      uint32_t spins = 0;
-      for (;;) {
-        uint32_t w = fl::ld_relaxed(status + p);
-        uint32_t f = w & ~kValMask;
-        if (f == 0) {
-          if (++spins > FL_SPIN_LIMIT) {
-            atomicOr(err, FL_ERR_LOOKBACK);
-            break;
-          }
-          if (spins > 64) __nanosleep(100);
-          continue;
-        }
-        prefix += w & kValMask;
-        if (f == kFlagPre || p == 0) break;
-        --p;
-      }
-      fl::st_relaxed(mine, kFlagPre | (prefix + total));
-    }
-    s_prefix = prefix;
-  }
-  __syncthreads();
-  uint32_t acc = base + s_prefix + before;
-#pragma unroll
-  for (int j = 0; j < kScanItems; ++j) {
-    if (first + j < n) out[first + j] = acc;
-    acc += v[j];
   }
 }
 
@@ -317,20 +266,4 @@ int fl_sort_passes(const FlSortBufs* b, int64_t n, int lo_bit, uint32_t* err, cu
     cur = 1 - cur;
   }
   return cur;
-}
-
-size_t fl_scan_bytes(int64_t n) {
-  int64_t tiles = (n + kScanTile - 1) / kScanTile + 1;
-  return align256(4 * (size_t)tiles) + 256;
-}
-
-void fl_scan_exclusive(const uint32_t* in, uint32_t* out, int64_t n, uint32_t base, void* scratch,
-                       uint32_t* err, cudaStream_t st, int64_t* launches) {
-  if (n <= 0) return;
-  int64_t tiles = (n + kScanTile - 1) / kScanTile;
-  uint32_t* status = static_cast<uint32_t*>(scratch);
-  uint32_t* ticket = status + align256(4 * (size_t)(tiles + 1)) / 4;
-  cudaMemsetAsync(scratch, 0, align256(4 * (size_t)(tiles + 1)) + 4, st);
-  k_scan<<<(int)tiles, kThreads, 0, st>>>(in, out, n, base, status, ticket, err);
-  ++*launches;
 }

@@ -399,48 +399,58 @@ __global__ void __launch_bounds__(kThreads) k_heads(int n, int ndim,
   if (threadIdx.x == kThreads - 1) ctot[blockIdx.x] = before + x;
 }
 
-// Exclusive prefix of the block totals, in place, by one block: of the child counts (u32)...
-__global__ void __launch_bounds__(kThreads) k_top_u32(uint32_t* tot, int nb) {
-  __shared__ uint32_t s[kThreads];
-  const int per = (nb + kThreads - 1) / kThreads, a = threadIdx.x * per, b = min(nb, a + per);
-  uint32_t sum = 0;
-  for (int t = a; t < b; ++t) sum += tot[t];
-  s[threadIdx.x] = sum;
-  __syncthreads();
-  for (int o = 1; o < kThreads; o <<= 1) {  // Hillis-Steele, inclusive
-    const uint32_t y = threadIdx.x >= o ? s[threadIdx.x - o] : 0u;
-    __syncthreads();
-    s[threadIdx.x] += y;
-    __syncthreads();
+// Exclusive prefix of the block totals, in place, by one block of kTopThreads: each thread sums
+// a run of consecutive totals, a warp-shuffle scan of the threads' sums (two levels) gives each
+// run its start, and the thread rewrites its run. For the child counts (u32) and the
+// fixed-point point records (D4).
+constexpr int kTopThreads = 1024;
+__device__ __forceinline__ uint32_t top_add(uint32_t a, uint32_t b) { return a + b; }
+__device__ __forceinline__ D4 top_add(D4 a, D4 b) { return add4(a, b); }
+__device__ __forceinline__ uint32_t top_up(uint32_t v, int o) { return __shfl_up_sync(FL_FULL, v, o); }
+__device__ __forceinline__ D4 top_up(D4 v, int o) { return shfl_up4(v, o); }
+
+template <typename T>
+__device__ __forceinline__ void top_scan(T* tot, int nb, T zero) {
+  __shared__ T s_warp[kTopThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int per = (nb + kTopThreads - 1) / kTopThreads, a = threadIdx.x * per;
+  const int b = a + per < nb ? a + per : nb;
+  T sum = zero;
+  for (int t = a; t < b; ++t) sum = top_add(sum, tot[t]);
+  T x = sum;  // inclusive scan within the warp
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const T y = top_up(x, o);
+    if (lane >= o) x = top_add(x, y);
   }
-  uint32_t run = threadIdx.x ? s[threadIdx.x - 1] : 0u;
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {  // inclusive scan of the warp totals
+    T w = s_warp[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const T y = top_up(w, o);
+      if (lane >= o) w = top_add(w, y);
+    }
+    s_warp[lane] = w;
+  }
+  __syncthreads();
+  T run = warp ? s_warp[warp - 1] : zero;
+  const T y = top_up(x, 1);  // exclusive within the warp: the previous lane's inclusive sum
+  if (lane) run = top_add(run, y);
   for (int t = a; t < b; ++t) {
-    const uint32_t v = tot[t];
+    const T v = tot[t];
     tot[t] = run;
-    run += v;
+    run = top_add(run, v);
   }
 }
 
-// ... and of the fixed-point point records (D4)
-__global__ void __launch_bounds__(kThreads) k_top4(D4* tot, int nb) {
-  __shared__ D4 s[kThreads];
-  const int per = (nb + kThreads - 1) / kThreads, a = threadIdx.x * per, b = min(nb, a + per);
-  D4 sum = mk4(0, 0, 0, 0);
-  for (int t = a; t < b; ++t) sum = add4(sum, tot[t]);
-  s[threadIdx.x] = sum;
-  __syncthreads();
-  for (int o = 1; o < kThreads; o <<= 1) {
-    const D4 y = threadIdx.x >= o ? s[threadIdx.x - o] : mk4(0, 0, 0, 0);
-    __syncthreads();
-    s[threadIdx.x] = add4(s[threadIdx.x], y);
-    __syncthreads();
-  }
-  D4 run = threadIdx.x ? s[threadIdx.x - 1] : mk4(0, 0, 0, 0);
-  for (int t = a; t < b; ++t) {
-    const D4 v = tot[t];
-    tot[t] = run;
-    run = add4(run, v);
-  }
+__global__ void __launch_bounds__(kTopThreads) k_top_u32(uint32_t* tot, int nb) {
+  top_scan<uint32_t>(tot, nb, 0u);
+}
+
+__global__ void __launch_bounds__(kTopThreads) k_top4(D4* tot, int nb) {
+  top_scan<D4>(tot, nb, mk4(0, 0, 0, 0));
 }
 
 // first child slot of head x: slot 0 is the root's own; children follow in head order
@@ -994,7 +1004,7 @@ void fl_launch_build(const FlTreeBufs* t, const uint64_t* skeys, const uint32_t*
                                    reinterpret_cast<D4*>(t->wtiles), cube, fx_exp);
   ++*launches;
   if (closed) {
-    k_top4<<<1, kThreads, 0, st>>>(reinterpret_cast<D4*>(t->wtiles), nb);
+    k_top4<<<1, kTopThreads, 0, st>>>(reinterpret_cast<D4*>(t->wtiles), nb);
     ++*launches;
   }
 }
@@ -1010,7 +1020,7 @@ void fl_launch_aggregate(const FlTreeBufs* t, const uint64_t* skeys, bool closed
                                       t->depth, t->omask, t->head_of, err);
   k_heads<<<g, kThreads, 0, st>>>(n, t->ndim, t->parent, t->range, t->depth, t->omask, t->count,
                                   t->first, ctot);
-  k_top_u32<<<1, kThreads, 0, st>>>(ctot, g);
+  k_top_u32<<<1, kTopThreads, 0, st>>>(ctot, g);
   *launches += 3;
   if (closed) {
     k_cells_closed<<<g, kThreads, 0, st>>>(n, t->ndim, sign, t->range, t->depth, t->count,
