@@ -66,6 +66,9 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--walk-group", type=int, default=32, choices=[16, 32],
                    help="points per tree-walk traversal (FL_TUNE_WALK_GROUP)")
+    p.add_argument("--precision", action="store_true",
+                   help="print the many-body force accuracy report instead of the timing line")
+    p.add_argument("--precision-ticks", type=int, default=100)
     return p.parse_args()
 
 
@@ -177,10 +180,108 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def rel_errors(got, ref):
+    """Max over targets of |got - ref| / |ref| (vector norms), and the RMS relative error
+    ||got - ref|| / ||ref|| over all targets."""
+    diff = np.linalg.norm(got - ref, axis=1)
+    norm = np.linalg.norm(ref, axis=1)
+    ok = norm > 0
+    return {"max_rel": float((diff[ok] / norm[ok]).max()) if ok.any() else 0.0,
+            "rms_rel": float(np.sqrt((diff ** 2).sum()) / max(np.sqrt((norm ** 2).sum()), 1e-300))}
+
+
+def gpu_manybody_dv(pos4, theta2, alpha, targets, cells, local=0, dmin2=1.0):
+    """The velocity change the engine's many-body force gives the targets from positions pos4
+    (velocities 0, decay 1: one tick's velocity is exactly the force's change)."""
+    from forcegpu import Engine
+    from forcegpu._lib import TUNE_CELL_SUMS, desc_from_gpu
+    n = len(pos4)
+    eng = Engine(local)
+    eng.set_nodes(pos4, 3)
+    d, keep = desc_from_gpu({"type": "manyBody", "version": 1, "strengths": np.full(n, -30.0),
+                             "distanceMin2": dmin2, "distanceMax2": math.inf, "theta2": theta2}, 1, n)
+    eng.set_forces([(d, keep)])
+    eng.set_tuning(TUNE_CELL_SUMS, cells)
+    eng.set_seed(12345)
+    eng.enqueue(np.array([alpha]), 1.0)
+    _, vel = eng.sync()
+    eng.close()
+    return vel[targets, :3].astype(np.float64)
+
+
+def run_precision(args):
+    """--precision: accuracy of the many-body force from one captured state of the layout.
+
+    The 1M-node workload runs `--precision-ticks` ticks on the GPU; from that state (positions,
+    the next tick's alpha) the many-body velocity change of 8,192 random target nodes is taken
+    from the GPU (each cell-sum variant), from the oracle's d3 walk (the reference's CPU
+    Barnes-Hut) and from the oracle's FP64 exact sum over all pairs, for theta 0.5 and 0.9; and
+    for theta 0 (the exact path) on a 20,000-node layout. Prints one JSON line."""
+    import oracle
+    from forcegpu import Engine
+    from forcegpu._lib import CELLS_AUTO, CELLS_FP32, CELLS_FP64_TOP, desc_from_gpu
+    threads = os.cpu_count() or 1
+    out = {"report": "many-body force accuracy", "targets": 8192, "host_threads": threads,
+           "metric": "relative error of the velocity change vs the FP64 exact all-pairs sum",
+           "cases": []}
+
+    def layout_state(n, ticks):
+        xyz, src, dst, bias, strength = workload(n)
+        pos4 = np.zeros((n, 4), np.float32)
+        pos4[:, :3] = xyz
+        eng = Engine(0)
+        eng.set_nodes(pos4, 3)
+        links = {"type": "link", "version": 1, "source": src, "target": dst, "iterations": 1,
+                 "strengths": strength, "distances": np.full(len(src), 30.0), "bias": bias}
+        charge = {"type": "manyBody", "version": 1, "strengths": np.full(n, -30.0),
+                  "distanceMin2": 1.0, "distanceMax2": math.inf, "theta2": 0.81}
+        eng.set_forces([desc_from_gpu(links, 1, n), desc_from_gpu(charge, 2, n),
+                        desc_from_gpu({"type": "center", "x": 0, "y": 0, "z": 0, "strength": 1.0}, 3, n)])
+        eng.set_seed(12345)
+        al, _ = alphas(ticks + 1)
+        if ticks:
+            eng.enqueue(al[:ticks], 0.6)
+        pos, _ = eng.sync()
+        eng.close()
+        return pos, float(al[ticks])
+
+    rng = np.random.default_rng(7)
+    for n, thetas, ticks in ((args.nodes, (0.5, 0.9), args.precision_ticks), (20_000, (0.0,), args.precision_ticks)):
+        pos, alpha = layout_state(n, ticks)
+        targets = np.sort(rng.choice(n, min(8192, n), replace=False)).astype(np.int32)
+        o = oracle.OracleSim(n, 3, xyz=pos[:, :3].astype(np.float64))
+        o.manybody(theta=0.9)
+        t0 = time.perf_counter()
+        exact = o.manybody_probe(0, alpha, targets, oracle.MODE_EXACT, threads=threads)
+        t_exact = time.perf_counter() - t0
+        for theta in thetas:
+            case = {"nodes": n, "theta": theta, "ticks": ticks, "alpha": alpha,
+                    "exact_seconds": t_exact}
+            if theta > 0:
+                ot = oracle.OracleSim(n, 3, xyz=pos[:, :3].astype(np.float64))
+                ot.manybody(theta=theta)
+                d3 = ot.manybody_probe(0, alpha, targets, oracle.MODE_D3)
+                case["cpu_barnes_hut_vs_exact"] = rel_errors(d3, exact)
+                for name, cells in (("fixed_point", CELLS_AUTO), ("fp64_top", CELLS_FP64_TOP),
+                                    ("fp32", CELLS_FP32)):
+                    g = gpu_manybody_dv(pos, theta * theta, alpha, targets, cells)
+                    case["gpu_%s_vs_exact" % name] = rel_errors(g, exact)
+                    case["gpu_%s_vs_cpu_barnes_hut" % name] = rel_errors(g, d3)
+            else:
+                g = gpu_manybody_dv(pos, 0.0, alpha, targets, CELLS_AUTO)
+                case["gpu_exact_path_vs_exact"] = rel_errors(g, exact)
+            out["cases"].append(case)
+            print(json.dumps(case), file=sys.stderr, flush=True)
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.precision:
+        run_precision(args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -25,6 +25,7 @@ namespace {
 constexpr int64_t kMaxNodes = (int64_t(1) << 26) - 1;  // child slot / stack index width
 constexpr double kExactTheta2 = 1e-6;                  // src/gpu/passes/manyBody.js:20-21
 constexpr int kGridMin = 8192;                         // pairs by grid from this many nodes
+constexpr int kRecursionFp64Depth = 6;  // the recursion sums cells above this depth in FP64
 
 struct DevMem {
   void* p = nullptr;
@@ -104,6 +105,7 @@ struct fl_sim {
   uint32_t seed = 0, step = 0;
   int64_t ticks = 0, launches = 0;
   int walk_group = 32;  // points per tree-walk traversal (tuning: 16 or 32)
+  int cell_sums = 0;    // tuning FL_TUNE_CELL_SUMS
   bool profiling = false;
   int prof_level = 0;
   DevMem wstats;  // walk counters (profiling level 2)
@@ -358,14 +360,18 @@ void encode_manybody(fl_sim* s, Pass* p, float alpha, const FlReduce* box) {
     r = fl_sort_passes(&p->sb, n, lo_bit, s->errw.as<uint32_t>(), s->st, &s->launches);
     p->sorted_in = r;
   }
+  // the closed form (exact fixed-point sums) when the strengths share one sign, unless a
+  // recursion was asked for
+  const bool closed = !p->mixed && s->cell_sums == FL_CELLS_AUTO;
   {
     Scope sc(s, G_BUILD);
-    fl_launch_build(t, p->sb.keys[r], p->sb.vals[r], s->pos.as<float4>(), strength, !p->mixed,
+    fl_launch_build(t, p->sb.keys[r], p->sb.vals[r], s->pos.as<float4>(), strength, closed,
                     p->cube.as<float>(), p->fx_exp, s->st, &s->launches);
   }
   {
     Scope sc(s, G_AGGREGATE);
-    fl_launch_aggregate(t, p->sb.keys[r], !p->mixed, p->sign, p->cube.as<float>(), p->fx_exp,
+    fl_launch_aggregate(t, p->sb.keys[r], closed, p->sign, p->cube.as<float>(), p->fx_exp,
+                        s->cell_sums == FL_CELLS_FP32 ? 0 : kRecursionFp64Depth,
                         s->errw.as<uint32_t>(), s->st, &s->launches);
   }
   {
@@ -749,6 +755,11 @@ int32_t fl_set_tuning(fl_sim* s, int32_t key, int32_t value) {
     case FL_TUNE_WALK_GROUP:
       if (value != 16 && value != 32) return fail(s, FL_E_ARG, "walk group must be 16 or 32");
       s->walk_group = value;
+      return FL_OK;
+    case FL_TUNE_CELL_SUMS:
+      if (value != FL_CELLS_AUTO && value != FL_CELLS_FP64_TOP && value != FL_CELLS_FP32)
+        return fail(s, FL_E_ARG, "cell sums must be FL_CELLS_AUTO, FL_CELLS_FP64_TOP or FL_CELLS_FP32");
+      s->cell_sums = value;
       return FL_OK;
     default:
       return fail(s, FL_E_ARG, "unknown tuning key");

@@ -78,6 +78,10 @@ struct FlTreeBufs {
   double* wtiles;        // [5 tiles] partial sums of the prefix scan
   uint32_t* omask;       // [n-1] occupied octants of each head's cell
   uint32_t* head_of;     // [2n-1] d3 child: its head | octant << 27 | 1 << 31 (internal, then points)
+  uint4* spill;          // the walk stacks' overflow, one region per warp slot of its grid
+  uint32_t* work;        // the walk's next group of 32 points to hand out
+  int walk_slots;        // warp slots of the persistent walk grid
+  int sms;               // SMs of the device
 };
 struct FlWalkParams {
   float thresh[32];   // (cube size / 2^k)^2 / theta^2
@@ -87,6 +91,8 @@ struct FlWalkParams {
   uint32_t step, seed;
 };
 size_t fl_tree_bytes(int64_t n);
+// Warp slots of the persistent walk grid for n points on the current device.
+int fl_walk_slots(int64_t n);
 void fl_tree_carve(FlTreeBufs* t, void* base, int64_t n, int ndim);
 // Bounding box -> d3 cube -> Morton keys (left-aligned) + values = node index, fused with the
 // sort's digit histogram. Also sets the walk's per-depth thresholds on the device.
@@ -99,10 +105,11 @@ void fl_launch_build(const FlTreeBufs* t, const uint64_t* skeys, const uint32_t*
                      const float4* pos, const float* strength, bool closed, const float* cube,
                      int fx_exp, cudaStream_t st, int64_t* launches);
 // Heads, child counts and slots; cell values and centroids in closed form (strengths of one
-// sign, fixed-point sums at scale 2^fx_exp) or by the bottom-up recursion (both signs).
+// sign, fixed-point sums at scale 2^fx_exp) or by the bottom-up recursion (both signs; FP64 sums
+// for the cells above depth fp64_depth, FP32 below).
 void fl_launch_aggregate(const FlTreeBufs* t, const uint64_t* skeys, bool closed, float sign,
-                         const float* cube, int fx_exp, uint32_t* err, cudaStream_t st,
-                         int64_t* launches);
+                         const float* cube, int fx_exp, int fp64_depth, uint32_t* err,
+                         cudaStream_t st, int64_t* launches);
 // Scale exponent of the fixed-point cell sums: no sum over n points of weight <= wmax overflows.
 int fl_fixed_exponent(int64_t n, double wmax);
 // stats (optional): [0] child tests made by the warps (32 per child), [1] of those, tests by a

@@ -46,7 +46,6 @@ constexpr uint32_t kLeaf = 0x80000000u;
 constexpr uint32_t kIndex = 0x7fffffffu;
 constexpr uint32_t kLeafMark = 0x7fffffffu;  // meta word of a point (a cell's is count | depth << 26)
 constexpr uint32_t kCountMask = (1u << 26) - 1;
-constexpr int kFp64Depth = 6;  // the recursion sums children in FP64 above this depth
 constexpr int kThreads = 256;
 
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -502,7 +501,7 @@ __global__ void __launch_bounds__(kThreads) k_cells_climb(
     const uint32_t* __restrict__ parent, const uint32_t* __restrict__ leaf_parent,
     const uint32_t* __restrict__ range, const uint8_t* __restrict__ depth,
     const uint32_t* __restrict__ count, uint32_t* __restrict__ flag, float4* cell,
-    const float4* __restrict__ leaf, uint32_t* err) {
+    const float4* __restrict__ leaf, int fp64_depth, uint32_t* err) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   const int L = levels_of(ndim);
@@ -518,7 +517,7 @@ __global__ void __launch_bounds__(kThreads) k_cells_climb(
     __threadfence();
     if (count[node]) {
       const int D = depth[node];
-      const bool wide = D < kFp64Depth;
+      const bool wide = D < fp64_depth;
       double sv = 0, sa = 0, sx = 0, sy = 0, sz = 0;
       float fv = 0, fa = 0, fx = 0, fy = 0, fz = 0;
       float4 firstpos = make_float4(0, 0, 0, 0);
@@ -596,7 +595,13 @@ __global__ void __launch_bounds__(kThreads) k_slots(
 
 constexpr int kWalkThreads = 128;
 constexpr int kWalkWarps = kWalkThreads / 32;
-constexpr int kStack = 96;  // entries per group; the deepest stack seen at 1M nodes in 3D is 67
+constexpr int kStack = 96;  // entries per group in shared memory; deeper entries spill to global
+// A group's stack never holds more than (levels + 1) * G entries: every batch pushes at most G
+// entries (the cells its lanes open), and the entries on the stack form layers, one per batch
+// whose pushes are not yet consumed, holding cells of strictly increasing depth.
+__host__ __device__ constexpr int kWalkStackLayers(int ndim) { return (ndim == 3 ? 21 : 24) + 1; }
+constexpr int kWalkSpillPerWarp = 704;  // max over dims and group sizes of NG ((levels+1) G - kStack)
+constexpr int kWalkBlocksPerSm = 10;    // blocks of the persistent walk grid per SM
 
 // Packed FP32 pairs (the f32x2 arithmetic of sm_100 and later): two children per instruction.
 __device__ __forceinline__ uint64_t pk2(float a, float b) {
@@ -686,43 +691,60 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
     const float4* __restrict__ leaf, const uint32_t* __restrict__ perm,
     const float* __restrict__ cube, float4* __restrict__ vel, int n, float alpha,
     double theta2, float dmin2, float dmax2, uint32_t step, uint32_t seed, uint32_t* err,
-    unsigned long long* stats) {
+    unsigned long long* stats, uint4* __restrict__ spill, int nwarps, uint32_t* work) {
   constexpr int NG = 32 / G;
+  // the stack of a group: kStack entries in shared memory, then up to kWalkStack(NDIM, G) in
+  // all, the rest in this warp slot's region of the spill buffer
+  constexpr int kAll = kWalkStackLayers(NDIM) * G, kSpilled = kAll - kStack;
+  static_assert(NG * kSpilled <= kWalkSpillPerWarp, "spill region too small");
   __shared__ WalkShared<NG> sh;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int grp = lane / G, gl = lane % G, gbase = grp * G;
   const uint32_t gmask = G == 32 ? FL_FULL : (((1u << G) - 1u) << gbase);
   const uint32_t lanebit = 1u << lane;
-  const int base = (blockIdx.x * kWalkWarps + warp) * 32;
-  const int t = base + lane;
-  const bool live = t < n;
-  const uint32_t act = __ballot_sync(FL_FULL, live) & gmask;
-  if (!__any_sync(FL_FULL, live)) return;
   // (size / 2^k)^2 / theta^2 = T0 * 4^-k, exactly (a power-of-two scaling)
   const float T0 = (float)((double)cube[3] * (double)cube[3] / theta2);
   // l < dmin2  <=>  l <= the largest float below dmin2 (l >= 0)
   const float dmin_le = dmin2 > 0.f ? __uint_as_float(__float_as_uint(dmin2) - 1u) : -1.f;
-  const float4 me = live ? leaf[t] : make_float4(0, 0, 0, 0);
-  const uint32_t myid = live ? perm[t] : 0;
   const uint32_t slot_cap = 2u * (uint32_t)n + 1u;
-  uint64_t AX = 0, AY = 0, AZ = 0;  // force sums, one per child of a round's pair
-  const uint64_t MX = pk2(me.x, me.x), MY = pk2(me.y, me.y), MZ = pk2(me.z, me.z);
   unsigned long long st_tests = 0, st_useful = 0, st_open = 0, st_apply = 0, st_rare = 0;
+  int maxsp = 0;
+  const int wslot = blockIdx.x * kWalkWarps + warp;  // this warp's slot of a persistent grid
   uint4* stk = sh.stack[warp][grp];
-  if (gl == 0 && act) stk[0] = make_uint4(0u, 1u, 0u, act);  // the root: slot 0, top depth 0
-  int sp = act ? 1 : 0, maxsp = sp;
-  __syncwarp();
-  uint32_t guard = 0;
-  const uint32_t guard_max = 4u * (uint32_t)n + 64u;
+  uint4* spl = spill + (size_t)wslot * kWalkSpillPerWarp + grp * kSpilled;
+  auto sget = [&](int i) { return i < kStack ? stk[i] : spl[i - kStack]; };
+  auto sset = [&](int i, uint4 v) {
+    if (i < kStack) stk[i] = v;
+    else spl[i - kStack] = v;
+  };
   float4* spair = sh.data[warp] + gbase;
   uint4* stest = sh.test[warp] + gbase;
   uint2* scold = sh.cold[warp] + gbase;
+  // groups of 32 points are handed out one at a time (the walk's cost varies a lot between
+  // groups, so a fixed share per warp would leave some warps working long after the rest)
+  int wi = lane == 0 ? (int)atomicAdd(work, 1u) : 0;
+  wi = __shfl_sync(FL_FULL, wi, 0);
+  while (wi < nwarps) {
+  const int base = wi * 32;
+  const int t = base + lane;
+  const bool live = t < n;
+  const uint32_t act = __ballot_sync(FL_FULL, live) & gmask;
+  const float4 me = live ? leaf[t] : make_float4(0, 0, 0, 0);
+  const uint32_t myid = live ? perm[t] : 0;
+  uint64_t AX = 0, AY = 0, AZ = 0;  // force sums, one per child of a round's pair
+  const uint64_t MX = pk2(me.x, me.x), MY = pk2(me.y, me.y), MZ = pk2(me.z, me.z);
+  if (gl == 0 && act) sset(0, make_uint4(0u, 1u, 0u, act));  // the root: slot 0, top depth 0
+  int sp = act ? 1 : 0;
+  if (sp > maxsp) maxsp = sp;
+  __syncwarp();
+  uint32_t guard = 0;
+  const uint32_t guard_max = 4u * (uint32_t)n + 64u;
   while (__any_sync(FL_FULL, sp > 0)) {
     // each group gathers the first G children from the top of its stack, in parallel: lane gl
     // reads the gl-th entry from the top, a prefix sum of the entries' child counts places each
     // entry's children in the batch, and lane gl then finds the entry of the batch's gl-th child
     const bool has = gl < sp;
-    uint4 e = has ? stk[sp - 1 - gl] : make_uint4(0u, 0u, 0u, 0u);
+    uint4 e = has ? sget(sp - 1 - gl) : make_uint4(0u, 0u, 0u, 0u);
     if (has && (e.x >= slot_cap || e.y > slot_cap - e.x)) {  // a malformed tree: never read past it
       atomicOr(err, FL_ERR_TREE);
       e.y = e.x >= slot_cap ? 0u : slot_cap - e.x;
@@ -739,7 +761,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
     // entries taken whole leave the stack; one taken in part keeps the rest (the new top)
     const uint32_t taken = __ballot_sync(FL_FULL, has && inc <= (uint32_t)total) & gmask;
     if (has && exc < (uint32_t)total && inc > (uint32_t)total)
-      stk[sp - 1 - gl] = make_uint4(e.x + ((uint32_t)total - exc), inc - (uint32_t)total, e.z, e.w);
+      sset(sp - 1 - gl, make_uint4(e.x + ((uint32_t)total - exc), inc - (uint32_t)total, e.z, e.w));
     sp -= __popc(taken);
     // each entry marks where its children start; a running max carries the mark to the rest
     uint32_t* sown = sh.own[warp] + gbase;
@@ -825,17 +847,17 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
       if (om0 | om1) {  // push the children some lanes must open (rare next to the tests)
         if (om0) {
           const uint32_t k0 = scold[j].x;
-          if (sp < kStack && gl == 0) stk[sp] = make_uint4(r0.w, k0 & kCountMask, ((k0 >> 26) & 31u) + 1u, om0);
+          if (sp < kAll && gl == 0) sset(sp, make_uint4(r0.w, k0 & kCountMask, ((k0 >> 26) & 31u) + 1u, om0));
           ++sp;
         }
         if (om1) {
           const uint32_t k1 = scold[j + 1].x;
-          if (sp < kStack && gl == 0) stk[sp] = make_uint4(r1.w, k1 & kCountMask, ((k1 >> 26) & 31u) + 1u, om1);
+          if (sp < kAll && gl == 0) sset(sp, make_uint4(r1.w, k1 & kCountMask, ((k1 >> 26) & 31u) + 1u, om1));
           ++sp;
         }
-        if (sp > kStack) {
+        if (sp > kAll) {  // beyond the bound on the stack's depth: a malformed tree
           if (gl == 0) atomicOr(err, FL_ERR_STACK);
-          sp = kStack;
+          sp = kAll;
         }
         if (STATS && sp > maxsp) maxsp = sp;
       }
@@ -855,6 +877,18 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
       break;
     }
   }
+  if (live) {
+    const float2 ax2 = up2(AX), ay2 = up2(AY), az2 = up2(AZ);
+    float4 v = vel[myid];
+    v.x += ax2.x + ax2.y;
+    if (NDIM > 1) v.y += ay2.x + ay2.y;
+    if (NDIM > 2) v.z += az2.x + az2.y;
+    vel[myid] = v;
+  }
+  __syncwarp();
+  wi = lane == 0 ? (int)atomicAdd(work, 1u) : 0;
+  wi = __shfl_sync(FL_FULL, wi, 0);
+  }
   if (STATS) {
     if (gl == 0) {
       atomicAdd(stats, st_tests);
@@ -865,14 +899,6 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
     }
     if (lane == 0) atomicAdd(stats + 5, st_rare);
   }
-  if (!live) return;
-  const float2 ax2 = up2(AX), ay2 = up2(AY), az2 = up2(AZ);
-  const float ax = ax2.x + ax2.y, ay = ay2.x + ay2.y, az = az2.x + az2.y;
-  float4 v = vel[myid];
-  v.x += ax;
-  if (NDIM > 1) v.y += ay;
-  if (NDIM > 2) v.z += az;
-  vel[myid] = v;
 }
 
 // Exact all-pairs sum (theta ~ 0; src/gpu/passes/manyBody.js:5-16 semantics): each block
@@ -941,7 +967,19 @@ size_t fl_tree_bytes(int64_t n) {
   return align256(4 * m) * 3 + align256(4 * N) + align256(8 * m) + align256(m) +
          align256(4 * m) * 3 + align256(16 * m) + align256(16 * N) + align256(16 * (2 * N + 1)) +
          align256(8 * (2 * N + 1)) + align256(4 * blocks) + align256(32 * N) +
-         align256(32 * blocks) + align256(4 * m) + align256(4 * (2 * N)) + 256;
+         align256(32 * blocks) + align256(4 * m) + align256(4 * (2 * N)) +
+         align256((size_t)fl_walk_slots(n) * kWalkSpillPerWarp * 16) + align256(4) + 256;
+}
+
+int fl_walk_slots(int64_t n) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
+    sms = 1;
+  const int64_t warps = (n > 0 ? n : 1) + 31 >> 5;
+  const int64_t want = (warps + kWalkWarps - 1) / kWalkWarps * kWalkWarps;
+  const int64_t cap = (int64_t)sms * kWalkBlocksPerSm * kWalkWarps;
+  return (int)(want < cap ? want : cap);
 }
 
 void fl_tree_carve(FlTreeBufs* t, void* base, int64_t n, int ndim) {
@@ -974,6 +1012,13 @@ void fl_tree_carve(FlTreeBufs* t, void* base, int64_t n, int ndim) {
   t->wtiles = (double*)take(32 * blocks);  // per-block totals of the point records
   t->omask = (uint32_t*)take(4 * m);
   t->head_of = (uint32_t*)take(4 * (2 * N));
+  t->walk_slots = fl_walk_slots(n);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&t->sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || t->sms < 1)
+    t->sms = 1;
+  t->spill = (uint4*)take((size_t)t->walk_slots * kWalkSpillPerWarp * 16);
+  t->work = (uint32_t*)take(4);
 }
 
 void fl_launch_morton(const float4* pos, int n, int ndim, const FlReduce* red, uint64_t* keys,
@@ -1010,8 +1055,8 @@ void fl_launch_build(const FlTreeBufs* t, const uint64_t* skeys, const uint32_t*
 }
 
 void fl_launch_aggregate(const FlTreeBufs* t, const uint64_t* skeys, bool closed, float sign,
-                         const float* cube, int fx_exp, uint32_t* err, cudaStream_t st,
-                         int64_t* launches) {
+                         const float* cube, int fx_exp, int fp64_depth, uint32_t* err,
+                         cudaStream_t st, int64_t* launches) {
   const int n = t->n, m = n - 1;
   const int g = (m + kThreads - 1) / kThreads, g2 = (2 * n - 1 + kThreads - 1) / kThreads;
   uint32_t* ctot = static_cast<uint32_t*>(t->scan_scratch);
@@ -1032,7 +1077,7 @@ void fl_launch_aggregate(const FlTreeBufs* t, const uint64_t* skeys, bool closed
     cudaMemsetAsync(t->flag, 0, 4 * (size_t)m, st);
     k_cells_climb<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(
         n, t->ndim, t->left, t->right, t->parent, t->leaf_parent, t->range, t->depth, t->count,
-        t->flag, t->cell, t->leaf, err);
+        t->flag, t->cell, t->leaf, fp64_depth, err);
     ++*launches;
   }
   k_slots<<<g2, kThreads, 0, st>>>(n, t->ndim, t->head_of, t->omask, t->range, t->depth,
@@ -1041,28 +1086,45 @@ void fl_launch_aggregate(const FlTreeBufs* t, const uint64_t* skeys, bool closed
   ++*launches;
 }
 
+// Blocks of this walk variant resident on one SM (queried once), at most kWalkBlocksPerSm.
+template <int NDIM, int G, bool STATS, bool DMAX>
+int walk_blocks_per_sm() {
+  static int blocks = 0;
+  if (!blocks) {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_walk<NDIM, G, STATS, DMAX>, kWalkThreads, 0) !=
+            cudaSuccess || b < 1)
+      b = 1;
+    blocks = b < kWalkBlocksPerSm ? b : kWalkBlocksPerSm;
+  }
+  return blocks;
+}
+
 void fl_launch_walk(const FlTreeBufs* t, const uint32_t* perm, const float* cube, float4* vel,
                     float alpha, double theta2, double dmin2, double dmax2, uint32_t step,
                     uint32_t seed, uint32_t* err, unsigned long long* stats, int group,
                     cudaStream_t st) {
   const int n = t->n;
   const int warps = (n + 31) / 32;
-  const int g = (warps + kWalkWarps - 1) / kWalkWarps;
+  // a persistent grid of the blocks that fit on the device at once (and that the spill buffer
+  // has regions for), each warp walking every (grid)-th group of 32 points
+  const int cap = t->walk_slots / kWalkWarps;
+  cudaMemsetAsync(t->work, 0, 4, st);
   const float fmax2 = dmax2 > 3e38 ? INFINITY : (float)dmax2;
+#define FL_WALK_ONE(D, G, S, M)                                                                \
+  do {                                                                                         \
+    int g = t->sms * walk_blocks_per_sm<D, G, S, M>();                                         \
+    if (g > cap) g = cap;                                                                      \
+    if (g < 1) g = 1;                                                                          \
+    k_walk<D, G, S, M><<<g, kWalkThreads, 0, st>>>(                                            \
+        t->child_data, t->child_meta, t->leaf, perm, cube, vel, n, alpha, theta2,              \
+        (float)dmin2, fmax2, step, seed, err, stats, t->spill, warps, t->work);                \
+  } while (0)
 #define FL_WALK(D, G)                                                                          \
   do {                                                                                         \
-    if (stats)                                                                                 \
-      k_walk<D, G, true, true><<<g, kWalkThreads, 0, st>>>(                                    \
-          t->child_data, t->child_meta, t->leaf, perm, cube, vel, n, alpha, theta2,            \
-          (float)dmin2, fmax2, step, seed, err, stats);                                        \
-    else if (fmax2 < INFINITY)                                                                 \
-      k_walk<D, G, false, true><<<g, kWalkThreads, 0, st>>>(                                   \
-          t->child_data, t->child_meta, t->leaf, perm, cube, vel, n, alpha, theta2,            \
-          (float)dmin2, fmax2, step, seed, err, stats);                                        \
-    else                                                                                       \
-      k_walk<D, G, false, false><<<g, kWalkThreads, 0, st>>>(                                  \
-          t->child_data, t->child_meta, t->leaf, perm, cube, vel, n, alpha, theta2,            \
-          (float)dmin2, fmax2, step, seed, err, stats);                                        \
+    if (stats) FL_WALK_ONE(D, G, true, true);                                                  \
+    else if (fmax2 < INFINITY) FL_WALK_ONE(D, G, false, true);                                 \
+    else FL_WALK_ONE(D, G, false, false);                                                      \
   } while (0)
   if (group == 32) {
     if (t->ndim == 3) FL_WALK(3, 32);
@@ -1074,6 +1136,7 @@ void fl_launch_walk(const FlTreeBufs* t, const uint32_t* perm, const float* cube
     else FL_WALK(1, 16);
   }
 #undef FL_WALK
+#undef FL_WALK_ONE
 }
 
 void fl_launch_allpairs(const float4* pos, const float* strength, float4* vel, int n, int ndim,

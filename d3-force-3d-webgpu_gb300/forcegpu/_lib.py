@@ -27,7 +27,8 @@ EXPORTS = ["fl_create", "fl_destroy", "fl_last_error", "fl_fits", "fl_set_nodes"
            "fl_stream", "fl_query", "fl_profile", "fl_profile_read", "fl_radix_sort",
            "fl_debug_tree", "fl_set_tuning", "fl_radix_sort_noalloc"]
 SORT_NOALLOC_MAX_PAIRS = 262144  # FL_SORT_NOALLOC_MAX_PAIRS
-TUNE_WALK_GROUP = 1
+TUNE_WALK_GROUP, TUNE_CELL_SUMS = 1, 2
+CELLS_AUTO, CELLS_FP64_TOP, CELLS_FP32 = 0, 1, 2
 
 
 class FlError(RuntimeError):

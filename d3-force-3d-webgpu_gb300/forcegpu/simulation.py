@@ -323,8 +323,11 @@ class Simulation:
         self._engine.enqueue(alphas, self._velocityDecay)
 
     def tick(self, iterations=1):
-        """Queue `iterations` ticks; the nodes follow at the next sync()."""
+        """Queue `iterations` ticks; the nodes follow at the next sync(). A destroyed simulation
+        ignores it (src/gpu/simulation.js: destroy() leaves tick() callable)."""
         with self._lock:
+            if self._destroyed:
+                return self
             self._need_engine()
             self._advance(int(iterations))
         return self
@@ -488,6 +491,10 @@ class Simulation:
         if not args:
             return self._forces.get(name)
         f = args[0]
+        if f is not None and not callable(getattr(f, "gpu", None)):
+            # the reference runs such a simulation on the CPU (src/gpu/simulation.js:110-139);
+            # this engine has no CPU path, so the force is refused and the simulation unchanged
+            raise FlError(FL_E_UNSUPPORTED, "force %r has no gpu() description" % (name,))
         with self._lock:
             if f is None:
                 self._forces.pop(name, None)

@@ -138,8 +138,13 @@ int32_t fl_buffers(fl_sim* sim, fl_buffer_info* out);
 
 /* Tuning parameters (no reference counterpart; the reference's closest are its fixed
  * constants, e.g. src/gpu/passes/barnesHut.js:49-58): FL_TUNE_WALK_GROUP, points that share one
- * tree-walk traversal, 16 or 32 (default). */
-enum { FL_TUNE_WALK_GROUP = 1 };
+ * tree-walk traversal, 16 or 32 (default); FL_TUNE_CELL_SUMS, how the many-body cells' values
+ * and centroids are summed: FL_CELLS_AUTO (default: exact fixed-point prefix sums when the
+ * strengths share one sign, else the bottom-up recursion with FP64 sums near the root),
+ * FL_CELLS_FP64_TOP (always that recursion) or FL_CELLS_FP32 (the recursion all in FP32, for
+ * precision comparisons). */
+enum { FL_TUNE_WALK_GROUP = 1, FL_TUNE_CELL_SUMS = 2 };
+enum { FL_CELLS_AUTO = 0, FL_CELLS_FP64_TOP = 1, FL_CELLS_FP32 = 2 };
 int32_t fl_set_tuning(fl_sim* sim, int32_t key, int32_t value);
 
 /* The cudaStream_t every kernel of this simulation runs on. */

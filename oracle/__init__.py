@@ -31,7 +31,7 @@ def build(force: bool = False) -> str:
     if stale:
         tmp = LIB + ".tmp%d" % os.getpid()
         subprocess.check_call(["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared",
-                               "-ffp-contract=off", "-fno-fast-math", "-o", tmp, SRC, "-lm"])
+                               "-ffp-contract=off", "-fno-fast-math", "-pthread", "-o", tmp, SRC, "-lm"])
         os.replace(tmp, LIB)
     return LIB
 
@@ -77,6 +77,9 @@ def lib():
         L.ofl_tick.argtypes = [P, I32]
         L.ofl_apply_force.argtypes = [P, I32, ctypes.c_double]
         L.ofl_walk_stats.argtypes = [P, ctypes.c_void_p]
+        L.ofl_manybody_probe.restype = I32
+        L.ofl_manybody_probe.argtypes = [P, I32, ctypes.c_double, I32, I32, ctypes.c_void_p, I32,
+                                         ctypes.c_void_p]
         L.ofl_levels.restype = I32
         L.ofl_levels.argtypes = [I32]
         L.ofl_cube.restype = I32
@@ -230,6 +233,17 @@ class OracleSim:
 
     def apply_force(self, k, alpha):
         lib().ofl_apply_force(self._h, int(k), float(alpha))
+
+    def manybody_probe(self, k, alpha, targets, mode=MODE_D3, threads=1):
+        """Velocity change many-body force k would give the target nodes (count x 3), state
+        unchanged: MODE_D3 by d3's tree walk, MODE_EXACT by the FP64 sum over all pairs."""
+        t = np.ascontiguousarray(targets, dtype=np.int32)
+        out = np.zeros((len(t), 3), dtype=np.float64)
+        rc = lib().ofl_manybody_probe(self._h, int(k), float(alpha), int(mode), len(t), t.ctypes.data,
+                                      int(threads), out.ctypes.data)
+        if rc != 0:
+            raise ValueError("manybody_probe: bad force index or target")
+        return out
 
     def walk_stats(self):
         out = np.zeros(3, dtype=np.int64)

@@ -7,6 +7,7 @@
 #include "d3force_oracle.h"
 
 #include <math.h>
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -284,94 +285,158 @@ static void mb_accumulate(osim* s, int32_t qi) {
   q->value = strength;
 }
 
-static void manybody_tree(osim* s, oforce* f, double alpha) {
+/* apply() of src/manyBody.js:73-115 for one node: the d3 walk from the root of the tree the
+ * caller built (tree_build + visit_after(mb_accumulate)), adding the node's velocity change to
+ * acc[0..2]. */
+static void mb_walk_node(osim* s, oforce* f, int32_t ni, double alpha, double* acc) {
   int d = s->ndim;
-  int32_t n = s->n;
   double theta2 = f->p[2], dmin2 = f->p[0], dmax2 = f->p[1];
-  g_strengths = f->a;
-  tree_build(s, s->x);
-  visit_after(s, mb_accumulate);
   tree* t = &s->t;
-  if (t->root < 0) return;
-  for (int32_t ni = 0; ni < n; ++ni) {
-    double* np = &s->x[3 * (size_t)ni];
-    double* nv = &s->v[3 * (size_t)ni];
-    int32_t sp = 0;
-    stack_push(s, &sp, t->root, t->x0, t->x1);
-    while (sp > 0) {
-      quad q = s->stack[--sp];
-      tnode* tn = &t->a[q.node];
-      /* apply(treeNode, x0, ..., x1, ...) */
-      if (!(tn->value != 0)) continue; /* `!treeNode.value` (0 or NaN): skip the cell */
-      double x = tn->x[0] - np[0];
-      double y = d > 1 ? tn->x[1] - np[1] : 0;
-      double z = d > 2 ? tn->x[2] - np[2] : 0;
-      double w = q.x1[0] - q.x0[0];
-      double l = x * x + y * y + z * z;
-      int isint = internal(t, q.node);
-      if (w * w / theta2 < l) {
-        if (l < dmax2) {
-          if (x == 0) x = jiggle(s), l += x * x;
-          if (d > 1 && y == 0) y = jiggle(s), l += y * y;
-          if (d > 2 && z == 0) z = jiggle(s), l += z * z;
-          if (l < dmin2) l = sqrt(dmin2 * l);
-          nv[0] += x * tn->value * alpha / l;
-          if (d > 1) nv[1] += y * tn->value * alpha / l;
-          if (d > 2) nv[2] += z * tn->value * alpha / l;
-        }
-        if (isint) s->stats[0]++;
-        continue;
-      }
-      if (isint) {
-        s->stats[2]++;
-        push_children(s, &sp, &q, 1);
-        continue;
-      }
-      if (l >= dmax2) continue;
-      if (tn->data != ni || tn->next >= 0) {
+  const double* np = &s->x[3 * (size_t)ni];
+  double* nv = acc;
+  int32_t sp = 0;
+  stack_push(s, &sp, t->root, t->x0, t->x1);
+  while (sp > 0) {
+    quad q = s->stack[--sp];
+    tnode* tn = &t->a[q.node];
+    /* apply(treeNode, x0, ..., x1, ...) */
+    if (!(tn->value != 0)) continue; /* `!treeNode.value` (0 or NaN): skip the cell */
+    double x = tn->x[0] - np[0];
+    double y = d > 1 ? tn->x[1] - np[1] : 0;
+    double z = d > 2 ? tn->x[2] - np[2] : 0;
+    double w = q.x1[0] - q.x0[0];
+    double l = x * x + y * y + z * z;
+    int isint = internal(t, q.node);
+    if (w * w / theta2 < l) {
+      if (l < dmax2) {
         if (x == 0) x = jiggle(s), l += x * x;
         if (d > 1 && y == 0) y = jiggle(s), l += y * y;
         if (d > 2 && z == 0) z = jiggle(s), l += z * z;
         if (l < dmin2) l = sqrt(dmin2 * l);
+        nv[0] += x * tn->value * alpha / l;
+        if (d > 1) nv[1] += y * tn->value * alpha / l;
+        if (d > 2) nv[2] += z * tn->value * alpha / l;
       }
-      int32_t li = q.node;
-      do {
-        if (t->a[li].data != ni) {
-          w = g_strengths[t->a[li].data] * alpha / l;
-          nv[0] += x * w;
-          if (d > 1) nv[1] += y * w;
-          if (d > 2) nv[2] += z * w;
-          s->stats[1]++;
-        }
-      } while ((li = t->a[li].next) >= 0);
+      if (isint) s->stats[0]++;
+      continue;
     }
+    if (isint) {
+      s->stats[2]++;
+      push_children(s, &sp, &q, 1);
+      continue;
+    }
+    if (l >= dmax2) continue;
+    if (tn->data != ni || tn->next >= 0) {
+      if (x == 0) x = jiggle(s), l += x * x;
+      if (d > 1 && y == 0) y = jiggle(s), l += y * y;
+      if (d > 2 && z == 0) z = jiggle(s), l += z * z;
+      if (l < dmin2) l = sqrt(dmin2 * l);
+    }
+    int32_t li = q.node;
+    do {
+      if (t->a[li].data != ni) {
+        w = g_strengths[t->a[li].data] * alpha / l;
+        nv[0] += x * w;
+        if (d > 1) nv[1] += y * w;
+        if (d > 2) nv[2] += z * w;
+        s->stats[1]++;
+      }
+    } while ((li = t->a[li].next) >= 0);
   }
 }
 
-/* FP64 exact sum over all pairs, with the same distanceMin / distanceMax rule. */
-static void manybody_exact(osim* s, oforce* f, double alpha) {
+/* The tree of force f over the current positions, with d3's cell values and centroids. */
+static int mb_prepare(osim* s, oforce* f) {
+  g_strengths = f->a;
+  tree_build(s, s->x);
+  visit_after(s, mb_accumulate);
+  return s->t.root >= 0;
+}
+
+static void manybody_tree(osim* s, oforce* f, double alpha) {
+  if (!mb_prepare(s, f)) return;
+  for (int32_t ni = 0; ni < s->n; ++ni) mb_walk_node(s, f, ni, alpha, &s->v[3 * (size_t)ni]);
+}
+
+/* FP64 exact sum over all pairs for node i, with the same distanceMin / distanceMax rule. */
+static void mb_exact_node(const osim* s, const oforce* f, int32_t i, double alpha, double* out3) {
   int d = s->ndim;
   int32_t n = s->n;
   double dmin2 = f->p[0], dmax2 = f->p[1];
-  double* acc = (double*)calloc(3 * (size_t)n, sizeof(double));
-  for (int32_t i = 0; i < n; ++i) {
-    const double* pi = &s->x[3 * (size_t)i];
-    double ax = 0, ay = 0, az = 0;
-    for (int32_t j = 0; j < n; ++j) {
-      if (j == i || f->a[j] == 0) continue;
-      const double* pj = &s->x[3 * (size_t)j];
-      double x = pj[0] - pi[0], y = d > 1 ? pj[1] - pi[1] : 0, z = d > 2 ? pj[2] - pi[2] : 0;
-      double l = x * x + y * y + z * z;
-      if (l >= dmax2 || l == 0) continue;
-      if (l < dmin2) l = sqrt(dmin2 * l);
-      double w = f->a[j] * alpha / l;
-      ax += x * w, ay += y * w, az += z * w;
-    }
-    acc[3 * (size_t)i] = ax, acc[3 * (size_t)i + 1] = ay, acc[3 * (size_t)i + 2] = az;
+  const double* pi = &s->x[3 * (size_t)i];
+  double ax = 0, ay = 0, az = 0;
+  for (int32_t j = 0; j < n; ++j) {
+    if (j == i || f->a[j] == 0) continue;
+    const double* pj = &s->x[3 * (size_t)j];
+    double x = pj[0] - pi[0], y = d > 1 ? pj[1] - pi[1] : 0, z = d > 2 ? pj[2] - pi[2] : 0;
+    double l = x * x + y * y + z * z;
+    if (l >= dmax2 || l == 0) continue;
+    if (l < dmin2) l = sqrt(dmin2 * l);
+    double w = f->a[j] * alpha / l;
+    ax += x * w, ay += y * w, az += z * w;
   }
+  out3[0] = ax, out3[1] = d > 1 ? ay : 0, out3[2] = d > 2 ? az : 0;
+}
+
+static void manybody_exact(osim* s, oforce* f, double alpha) {
+  int d = s->ndim;
+  int32_t n = s->n;
+  double* acc = (double*)calloc(3 * (size_t)n, sizeof(double));
+  for (int32_t i = 0; i < n; ++i) mb_exact_node(s, f, i, alpha, &acc[3 * (size_t)i]);
   for (int32_t i = 0; i < n; ++i)
     for (int k = 0; k < d; ++k) s->v[3 * (size_t)i + k] += acc[3 * (size_t)i + k];
   free(acc);
+}
+
+typedef struct {
+  const osim* s;
+  const oforce* f;
+  double alpha;
+  const int32_t* targets;
+  int32_t lo, hi;
+  double* out3;
+} probe_job;
+
+static void* probe_exact_run(void* arg) {
+  probe_job* j = (probe_job*)arg;
+  for (int32_t k = j->lo; k < j->hi; ++k)
+    mb_exact_node(j->s, j->f, j->targets[k], j->alpha, &j->out3[3 * (size_t)k]);
+  return NULL;
+}
+
+int32_t ofl_manybody_probe(osim* s, int32_t k, double alpha, int32_t mode, int32_t count,
+                           const int32_t* targets, int32_t threads, double* out3) {
+  if (k < 0 || k >= s->nforces || s->forces[k].type != 1 || count < 0) return -1;
+  oforce* f = &s->forces[k];
+  for (int32_t i = 0; i < count; ++i)
+    if (targets[i] < 0 || targets[i] >= s->n) return -1;
+  memset(out3, 0, sizeof(double) * 3 * (size_t)count);
+  if (mode != OFL_MODE_EXACT) {
+    memset(s->stats, 0, sizeof(s->stats));
+    if (!mb_prepare(s, f)) return 0;
+    for (int32_t i = 0; i < count; ++i) mb_walk_node(s, f, targets[i], alpha, &out3[3 * (size_t)i]);
+    return 0;
+  }
+  if (threads < 1) threads = 1;
+  if (threads > 256) threads = 256;
+  if (threads > count) threads = count > 0 ? count : 1;
+  pthread_t tid[256];
+  probe_job jobs[256];
+  for (int32_t t = 0; t < threads; ++t) {
+    jobs[t].s = s, jobs[t].f = f, jobs[t].alpha = alpha, jobs[t].targets = targets;
+    jobs[t].lo = (int32_t)((int64_t)count * t / threads);
+    jobs[t].hi = (int32_t)((int64_t)count * (t + 1) / threads);
+    jobs[t].out3 = out3;
+  }
+  int32_t started = 0;
+  for (int32_t t = 1; t < threads; ++t) {
+    if (pthread_create(&tid[t], NULL, probe_exact_run, &jobs[t]) != 0) break;
+    started = t;
+  }
+  probe_exact_run(&jobs[0]);
+  for (int32_t t = 1; t <= started; ++t) pthread_join(tid[t], NULL);
+  for (int32_t t = started + 1; t < threads; ++t) probe_exact_run(&jobs[t]);  // not started
+  return 0;
 }
 
 /* ------------------------------------------------------------------ link (src/link.js) */

@@ -79,6 +79,13 @@ void ofl_tick(osim* s, int32_t iterations);
 /* Apply force k once at the given alpha (no alpha update, no integration). */
 void ofl_apply_force(osim* s, int32_t k, double alpha);
 
+/* The velocity change many-body force k would give each of `count` target nodes at the current
+ * state and `alpha`, without changing the state: OFL_MODE_D3 walks d3's tree (built over all
+ * nodes), OFL_MODE_EXACT sums every pair in FP64 on `threads` host threads. out3: 3 * count
+ * doubles. Returns 0, or -1 for a bad force index or target. */
+int32_t ofl_manybody_probe(osim* s, int32_t k, double alpha, int32_t mode, int32_t count,
+                           const int32_t* targets, int32_t threads, double* out3);
+
 /* Counters of the last many-body d3 tree walk: [0] approximated cells (internal cells that
  * passed the theta test, with a nonzero value), [1] point interactions (leaf data visited),
  * [2] cells opened (internal cells that failed the theta test). */

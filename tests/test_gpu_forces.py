@@ -8,6 +8,7 @@ import pytest
 
 from forcegpu import (forceCenter, forceCollide, forceLink, forceManyBody, forceRadial, forceX,
                       forceY, forceZ)
+from forcegpu._lib import CELLS_FP32, CELLS_FP64_TOP, TUNE_CELL_SUMS
 from gpu_helpers import assert_nodes_close, make_nodes, run_both, tree_outliers
 
 pytestmark = pytest.mark.gpu
@@ -127,6 +128,15 @@ def test_tree_theta(theta):
 def test_tree_strength_distance_min_max():
     r = run_both(3, 2000, 1, lambda: [("charge", forceManyBody().strength(lambda d, i, *a: -10 - i % 7)
                                        .distanceMin(3).distanceMax(60))])
+    assert_nodes_close(r["gpu"], r["cpu"], 3, rtol=1e-3, outliers=tree_outliers(2000))
+
+
+@pytest.mark.parametrize("cells", [CELLS_FP64_TOP, CELLS_FP32])
+def test_tree_cell_sum_variants(cells):
+    """The recursion's cell sums (FP64 near the root, or all FP32) in place of the exact
+    fixed-point closed form: the same tree, the same forces within the tolerance."""
+    r = run_both(3, 2000, 1, lambda: [("charge", forceManyBody())],
+                 setup=lambda sim, _: sim._engine.eng.set_tuning(TUNE_CELL_SUMS, cells))
     assert_nodes_close(r["gpu"], r["cpu"], 3, rtol=1e-3, outliers=tree_outliers(2000))
 
 
