@@ -69,6 +69,11 @@ def parse():
     p.add_argument("--precision", action="store_true",
                    help="print the many-body force accuracy report instead of the timing line")
     p.add_argument("--precision-ticks", type=int, default=100)
+    p.add_argument("--batched", action="store_true",
+                   help="print the batched-layout line (many graphs in one batch) instead")
+    p.add_argument("--graphs", type=int, default=2048)
+    p.add_argument("--serial-sample", type=int, default=48,
+                   help="graphs laid out one at a time on the plain engine, for the comparison")
     return p.parse_args()
 
 
@@ -275,6 +280,103 @@ def run_precision(args):
     print(json.dumps(out), flush=True)
 
 
+def batch_workload(graphs, seed=2024):
+    """The batched configuration: `graphs` independent 3D graphs, sizes log-uniform in
+    [100, 20000] (seeded), the reference benchmark's link generator at 1.5 links per node,
+    phyllotaxis starts; link + charge (theta 0.9) + center, d3's defaults."""
+    from forcegpu.batch import GraphSpec
+    from forcegpu.graphs import benchmark_links, phyllotaxis
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(100), np.log(20000), graphs)).astype(np.int64)
+    specs = []
+    for i, n in enumerate(sizes):
+        src, dst = benchmark_links(int(n), int(n) // 2, seed=1000 + i)
+        specs.append(GraphSpec(xyz=phyllotaxis(int(n), 3), source=src, target=dst))
+    return specs
+
+
+def run_batched(args):
+    """--batched: layouts per second of the batched engine on a batch of many graphs, 300 ticks
+    each (every graph's own d3 alpha schedule), against the plain engine laying out a sample of
+    the same graphs one at a time (the same work per graph; layouts/s of the sample)."""
+    import torch
+    from forcegpu import Engine
+    from forcegpu._lib import desc_from_gpu
+    from forcegpu.batch import Batch
+    from forcegpu.graphs import link_defaults
+    ticks = 300
+    specs = batch_workload(args.graphs)
+    nodes = int(sum(len(s.xyz) for s in specs))
+    b = Batch(0)
+    b.set_graphs(specs, ndim=3, seed=12345)
+    stream = torch.cuda.ExternalStream(b.stream(), device=0)
+    # warm-up on a copy of the schedule, then the timed full layout from the start
+    b.run(args.warmup)
+    b.sync()
+    b.set_graphs(specs, ndim=3, seed=12345)
+    sched = b.alpha_schedule(ticks)
+    clocks = Clocks()
+    clocks.start()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = b.launches()
+    t0 = time.perf_counter()
+    e0.record(stream)
+    b.enqueue(sched)
+    e1.record(stream)
+    pos, _ = b.sync()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    dev_ms = e0.elapsed_time(e1)
+    launches = b.launches() - launches0
+    assert np.isfinite(pos).all()
+    batched = len(specs) / (dev_ms / 1e3)
+    # the plain engine, one graph after another (a sample; each a full 300-tick layout)
+    rng = np.random.default_rng(99)
+    sample = rng.choice(len(specs), min(args.serial_sample, len(specs)), replace=False)
+    eng = Engine(0)
+    sample_nodes = 0
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for gi in sample:
+        s = specs[gi]
+        n = len(s.xyz)
+        sample_nodes += n
+        pos4 = np.zeros((n, 4), np.float32)
+        pos4[:, :3] = s.xyz
+        eng.set_nodes(pos4, 3)
+        bias, strength = link_defaults(n, s.source, s.target)
+        ld = desc_from_gpu({"type": "link", "version": 1, "source": s.source, "target": s.target,
+                            "iterations": 1, "strengths": strength,
+                            "distances": np.full(len(s.source), 30.0), "bias": bias}, 1, n)
+        cd = desc_from_gpu({"type": "manyBody", "version": 1, "strengths": np.full(n, -30.0),
+                            "distanceMin2": 1.0, "distanceMax2": math.inf, "theta2": 0.81}, 2, n)
+        xd = desc_from_gpu({"type": "center", "x": 0, "y": 0, "z": 0, "strength": 1.0}, 3, n)
+        eng.set_forces([ld, cd, xd])
+        al, _ = alphas(ticks)
+        eng.enqueue(al, 0.6)
+        eng.sync()
+    serial_s = time.perf_counter() - t1
+    eng.close()
+    serial = len(sample) / serial_s
+    line = {"metric": "layouts/s, 2048 graphs x 300 ticks (batched)", "value": batched,
+            "unit": "layouts/s", "n_gpus": 1, "steps": ticks, "warmup": args.warmup,
+            "ms_per_step": dev_ms / ticks, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "%d 3D graphs, sizes log-uniform in [100, 20000] (seed 2024), "
+                                   "1.5 links/node, link+charge(theta 0.9)+center, 300 ticks each"
+                                   % len(specs), "graphs": len(specs), "nodes": nodes},
+            "e2e": {"value": len(specs) / wall, "unit": "layouts/s",
+                    "h2d_bytes_per_step": 8 * len(specs), "d2h_bytes_per_step": 32 * nodes / ticks},
+            "serial_plain": {"value": serial, "unit": "layouts/s", "sample_graphs": len(sample),
+                             "sample_nodes": sample_nodes, "seconds": serial_s},
+            "speedup_vs_serial_plain": batched / serial,
+            "gpu_launches": int(launches), "clocks": clk,
+            "device_bytes": b.device_bytes()}
+    print(json.dumps(line), flush=True)
+    b.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -282,6 +384,9 @@ def main():
         return
     if args.precision:
         run_precision(args)
+        return
+    if args.batched:
+        run_batched(args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -1,0 +1,396 @@
+// fl_batch: many independent force layouts advanced together, one launch per kernel per tick.
+//
+// The graphs are concatenated (nodes, links) with per-graph offsets; every kernel of a tick runs
+// once over the whole batch and finds a node's graph from a graph-id array: bounding boxes and
+// centre sums are reduced per graph, each graph gets its own d3 cube and Morton keys, the tree's
+// sort orders the points by (graph, Morton code) so that each graph owns one contiguous range of
+// the sorted order and builds its own tree there, and the walk starts each point at its own
+// graph's root. Link, many-body and centre forces per graph, with per-graph alpha schedules
+// (fl_batch_enqueue takes one alpha per graph and tick), theta, distances and velocity decay.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/forcegpu.h"
+#include "kernels.h"
+
+namespace {
+
+struct Buf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  Buf() = default;
+  Buf(const Buf&) = delete;
+  Buf& operator=(const Buf&) = delete;
+  ~Buf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr, bytes = 0;
+  }
+  cudaError_t alloc(size_t b) {
+    release();
+    cudaError_t e = cudaMalloc(&p, b ? b : 256);
+    if (e != cudaSuccess) p = nullptr;
+    else bytes = b ? b : 256;
+    return e;
+  }
+  template <typename T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+constexpr int64_t kMaxBatchNodes = (int64_t(1) << 26) - 1;
+
+}  // namespace
+
+struct fl_batch {
+  int32_t device = 0;
+  cudaStream_t st = nullptr;
+  std::string err;
+  int32_t ndim = 3, graphs = 0, n = 0, m = 0;
+  Buf pos, vel[2], fix, mask, gid, off, prm, red, gr, alphas, charge, row, entry, code, errw;
+  Buf sort1, sort2, tree, gid_pos;
+  FlSortBufs sb{}, sb2{};
+  FlTreeBufs tb{};
+  int cur = 0;
+  size_t alpha_cap = 0;
+  uint32_t step = 0, seed = 0x9e3779b9u;
+  int fx_exp = 32;
+  bool closed = true;
+  float sign = -1.f;
+  double dmax_any = INFINITY;  // finite when some graph has a finite distanceMax
+  int64_t ticks = 0, launches = 0;
+};
+
+namespace {
+
+int32_t bfail(fl_batch* b, int32_t code, const std::string& msg) {
+  if (b) b->err = msg;
+  return code;
+}
+
+int32_t bcuda(fl_batch* b, cudaError_t e, const char* what) {
+  cudaGetLastError();
+  return bfail(b, e == cudaErrorMemoryAllocation ? FL_E_OOM : FL_E_DEVICE,
+               std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define FB_CK(b, call)                                      \
+  do {                                                      \
+    cudaError_t e_ = (call);                                \
+    if (e_ != cudaSuccess) return bcuda(b, e_, #call);      \
+  } while (0)
+
+int32_t bcheck(fl_batch* b) {
+  if (!b) return FL_E_ARG;
+  if (cudaSetDevice(b->device) != cudaSuccess) return bfail(b, FL_E_DEVICE, "cudaSetDevice failed");
+  return FL_OK;
+}
+
+float4* bvel(fl_batch* b) { return b->vel[b->cur].as<float4>(); }
+
+// One tick of the batch: alphas of this tick are at `alpha` (device, one per graph).
+void encode_batch_tick(fl_batch* b, const double* alpha) {
+  const int n = b->n, G = b->graphs;
+  cudaStream_t st = b->st;
+  uint32_t* err = b->errw.as<uint32_t>();
+  const uint32_t* gid = b->gid.as<uint32_t>();
+  FlGraph* gr = b->gr.as<FlGraph>();
+  // per-graph boxes and sums, then each graph's cube, threshold, alpha, decay and centre shift
+  cudaMemsetAsync(b->red.p, 0, sizeof(FlReduce) * (size_t)G, st);
+  fl_launch_breduce(b->pos.as<float4>(), n, b->ndim, gid, b->red.as<FlReduce>(), st);
+  fl_launch_bgraph(G, b->ndim, b->off.as<int32_t>(), b->red.as<FlReduce>(),
+                   b->prm.as<FlBatchParams>(), alpha, gr, st);
+  b->launches += 2;
+  // links (a snapshot: read v, write the other velocity buffer)
+  if (b->m > 0) {
+    FlLinkCsr csr{b->row.as<int32_t>(), b->entry.as<float4>(), b->code.as<uint32_t>()};
+    fl_launch_link(b->pos.as<float4>(), bvel(b), b->vel[1 - b->cur].as<float4>(), csr, n, b->ndim,
+                   0.f, b->step, b->seed, st, gr, gid);
+    b->cur = 1 - b->cur;
+    ++b->launches;
+  }
+  // many-body: sort by Morton code, then (stably) by graph; one tree per graph
+  if (n >= 2) {
+    const int bits = (b->ndim == 3 ? 21 : 24) * b->ndim, lo_bit = 64 - bits;
+    fl_sort_reset(&b->sb, n, (64 - lo_bit + 7) / 8, st);
+    fl_launch_bmorton(b->pos.as<float4>(), n, b->ndim, gid, gr, b->sb.keys[0], b->sb.vals[0],
+                      b->sb.hist, lo_bit, st);
+    const int r = fl_sort_passes(&b->sb, n, lo_bit, err, st, &b->launches);
+    fl_sort_reset(&b->sb2, n, 2, st);
+    fl_launch_bgidkey(n, b->sb.vals[r], gid, b->sb2.keys[0], b->sb2.vals[0], b->sb2.hist, st);
+    const int r2 = fl_sort_passes(&b->sb2, n, 48, err, st, &b->launches);
+    uint64_t* skeys = b->sb.keys[1 - r];
+    uint32_t* perm = b->sb.vals[1 - r];
+    uint32_t* gpos = b->gid_pos.as<uint32_t>();
+    fl_launch_bgather(n, b->sb2.vals[r2], b->sb.keys[r], b->sb.vals[r], gid, skeys, perm, gpos, st);
+    b->launches += 3;
+    FlSegs segs{G, b->off.as<int32_t>(), gid, gpos, gr};
+    fl_launch_build(&b->tb, skeys, perm, b->pos.as<float4>(), b->charge.as<float>(), b->closed,
+                    nullptr, b->fx_exp, st, &b->launches, segs);
+    fl_launch_aggregate(&b->tb, skeys, b->closed, b->sign, nullptr, b->fx_exp, 6, err, st,
+                        &b->launches, segs);
+    fl_launch_walk(&b->tb, perm, nullptr, bvel(b), 0.f, 1.0, 0.0, b->dmax_any, b->step, b->seed,
+                   err, nullptr, 32, st, segs);
+    ++b->launches;
+  }
+  // centre shift (per graph) and integration
+  fl_launch_integrate(b->pos.as<float4>(), bvel(b), b->fix.as<float4>(), b->mask.as<uint32_t>(),
+                      n, b->ndim, 1.f, nullptr, 0, 0, 0, 0, st, gr, gid);
+  ++b->launches;
+  ++b->step;
+  ++b->ticks;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t fl_batch_create(int32_t device, fl_batch** out) {
+  if (!out) return FL_E_ARG;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
+    cudaGetLastError();
+    return FL_E_DEVICE;
+  }
+  fl_batch* b = new fl_batch();
+  b->device = device;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess ||
+      b->errw.alloc(256) != cudaSuccess || cudaMemset(b->errw.p, 0, 256) != cudaSuccess) {
+    cudaGetLastError();
+    if (b->st) cudaStreamDestroy(b->st);
+    delete b;
+    return FL_E_DEVICE;
+  }
+  *out = b;
+  return FL_OK;
+}
+
+int32_t fl_batch_destroy(fl_batch* b) {
+  if (!b) return FL_OK;
+  cudaSetDevice(b->device);
+  cudaStreamSynchronize(b->st);
+  cudaStreamDestroy(b->st);
+  delete b;
+  return FL_OK;
+}
+
+const char* fl_batch_last_error(const fl_batch* b) { return b ? b->err.c_str() : "no batch"; }
+
+int32_t fl_batch_set_graphs(fl_batch* b, int32_t ndim, int32_t graphs, const fl_graph_desc* d) {
+  int32_t rc = bcheck(b);
+  if (rc) return rc;
+  if (ndim < 1 || ndim > 3) return bfail(b, FL_E_ARG, "ndim must be 1, 2 or 3");
+  if (graphs < 1 || graphs > 65535 || !d) return bfail(b, FL_E_ARG, "graphs must be 1..65535");
+  FB_CK(b, cudaStreamSynchronize(b->st));
+  int64_t n = 0, m = 0;
+  for (int32_t g = 0; g < graphs; ++g) {
+    if (d[g].n < 0 || d[g].m < 0 || (d[g].n && !d[g].pos4) || (d[g].m && (!d[g].source || !d[g].target)))
+      return bfail(b, FL_E_ARG, "graph " + std::to_string(g) + ": bad sizes or arrays");
+    if (!(d[g].theta2 >= 0) || !(d[g].distance_min2 >= 0) || !(d[g].distance_max2 > 0))
+      return bfail(b, FL_E_ARG, "graph " + std::to_string(g) + ": bad many-body parameters");
+    n += d[g].n, m += d[g].m;
+  }
+  if (n > kMaxBatchNodes) return bfail(b, FL_E_ARG, "too many nodes in one batch");
+  if (m > (int64_t(1) << 30)) return bfail(b, FL_E_ARG, "too many links in one batch");
+  b->ndim = ndim, b->graphs = graphs, b->n = (int32_t)n, b->m = (int32_t)m;
+  // nodes: state, graph ids, charges; graphs: offsets and fixed parameters
+  std::vector<float> pos(4 * (size_t)std::max<int64_t>(n, 1), 0.f), vel(pos.size(), 0.f);
+  std::vector<uint32_t> gid((size_t)std::max<int64_t>(n, 1), 0);
+  std::vector<float> charge((size_t)std::max<int64_t>(n, 1), -30.f);
+  std::vector<int32_t> off(graphs + 1, 0);
+  std::vector<FlBatchParams> prm(graphs);
+  bool neg = false, posv = false;
+  double smax = 0, dmax_any = INFINITY;
+  for (int32_t g = 0, at = 0; g < graphs; ++g) {
+    off[g] = at;
+    const fl_graph_desc& x = d[g];
+    for (int32_t i = 0; i < x.n; ++i) {
+      for (int k = 0; k < 4; ++k) {
+        const float p = k < ndim ? x.pos4[4 * (size_t)i + k] : 0.f;
+        pos[4 * (size_t)(at + i) + k] = std::isfinite(p) ? p : 0.f;
+        if (x.vel4 && k < ndim) vel[4 * (size_t)(at + i) + k] = x.vel4[4 * (size_t)i + k];
+      }
+      gid[at + i] = (uint32_t)g;
+      const float c = x.charge ? x.charge[i] : -30.f;
+      charge[at + i] = std::isfinite(c) ? c : 0.f;
+      neg = neg || charge[at + i] < 0.f, posv = posv || charge[at + i] > 0.f;
+      smax = std::max(smax, (double)std::fabs(charge[at + i]));
+    }
+    prm[g] = FlBatchParams{x.theta2, x.distance_min2, x.distance_max2, x.center_x, x.center_y,
+                           x.center_z, x.center_strength, 1.0 - x.velocity_decay};
+    if (x.distance_max2 < 3e38) dmax_any = 1.0;  // some graph has a finite distanceMax
+    at += x.n;
+    off[g + 1] = at;
+  }
+  b->closed = !(neg && posv);
+  b->sign = neg ? -1.f : 1.f;
+  b->fx_exp = fl_fixed_exponent(n, smax * (ndim == 1 ? 8192.0 : 1.0));
+  b->dmax_any = dmax_any;
+  // links: one CSR over the batch, node indices made global; d3's default strength and bias
+  std::vector<int32_t> row((size_t)n + 1, 0);
+  std::vector<int32_t> src((size_t)std::max<int64_t>(m, 1)), dst(src.size());
+  std::vector<float> dist(src.size()), str(src.size()), bias(src.size());
+  {
+    int64_t k = 0;
+    for (int32_t g = 0; g < graphs; ++g) {
+      const fl_graph_desc& x = d[g];
+      std::vector<int32_t> cnt((size_t)std::max(x.n, 1), 0);
+      for (int32_t j = 0; j < x.m; ++j) {
+        const int32_t a = x.source[j], c = x.target[j];
+        if (a < 0 || a >= x.n || c < 0 || c >= x.n)
+          return bfail(b, FL_E_ARG, "graph " + std::to_string(g) + " link " + std::to_string(j) + ": node not found");
+        ++cnt[a], ++cnt[c];
+      }
+      for (int32_t j = 0; j < x.m; ++j, ++k) {
+        const int32_t a = x.source[j], c = x.target[j];
+        src[k] = off[g] + a, dst[k] = off[g] + c;
+        dist[k] = x.link_distance ? x.link_distance[j] : 30.f;
+        // src/link.js:73-75, :36-38: bias = count(source) / (count(source) + count(target)),
+        // strength = 1 / min(count(source), count(target))
+        bias[k] = x.link_bias ? x.link_bias[j] : (float)((double)cnt[a] / (cnt[a] + cnt[c]));
+        str[k] = x.link_strength ? x.link_strength[j] : (float)(1.0 / std::min(cnt[a], cnt[c]));
+      }
+    }
+  }
+  for (int64_t k = 0; k < m; ++k) ++row[src[k] + 1], ++row[dst[k] + 1];
+  for (int64_t i = 0; i < n; ++i) row[i + 1] += row[i];
+  std::vector<int32_t> cur(row.begin(), row.end() - 1);
+  std::vector<float> entry(4 * (size_t)std::max<int64_t>(2 * m, 1));
+  std::vector<uint32_t> code((size_t)std::max<int64_t>(2 * m, 1));
+  for (int64_t k = 0; k < m; ++k) {
+    const int32_t a = src[k], c = dst[k];
+    int32_t e = cur[a]++;
+    std::memcpy(&entry[4 * (size_t)e], &c, 4);
+    entry[4 * (size_t)e + 1] = dist[k], entry[4 * (size_t)e + 2] = str[k];
+    entry[4 * (size_t)e + 3] = (float)(1.0 - (double)bias[k]);
+    code[e] = 2u * (uint32_t)k;
+    e = cur[c]++;
+    std::memcpy(&entry[4 * (size_t)e], &a, 4);
+    entry[4 * (size_t)e + 1] = dist[k], entry[4 * (size_t)e + 2] = str[k];
+    entry[4 * (size_t)e + 3] = bias[k];
+    code[e] = 2u * (uint32_t)k + 1u;
+  }
+  // device buffers
+  const size_t N = (size_t)std::max<int64_t>(n, 1);
+  FB_CK(b, b->pos.alloc(16 * N));
+  FB_CK(b, b->vel[0].alloc(16 * N));
+  FB_CK(b, b->vel[1].alloc(16 * N));
+  FB_CK(b, b->fix.alloc(16 * N));
+  FB_CK(b, b->mask.alloc(4 * N));
+  FB_CK(b, b->gid.alloc(4 * N));
+  FB_CK(b, b->gid_pos.alloc(4 * N));
+  FB_CK(b, b->charge.alloc(4 * N));
+  FB_CK(b, b->off.alloc(4 * (size_t)(graphs + 1)));
+  FB_CK(b, b->prm.alloc(sizeof(FlBatchParams) * (size_t)graphs));
+  FB_CK(b, b->red.alloc(sizeof(FlReduce) * (size_t)graphs));
+  FB_CK(b, b->gr.alloc(sizeof(FlGraph) * (size_t)graphs));
+  FB_CK(b, b->row.alloc(4 * ((size_t)n + 1)));
+  FB_CK(b, b->entry.alloc(16 * (size_t)std::max<int64_t>(2 * m, 1)));
+  FB_CK(b, b->code.alloc(4 * (size_t)std::max<int64_t>(2 * m, 1)));
+  FB_CK(b, b->sort1.alloc(fl_sort_bytes(n)));
+  FB_CK(b, b->sort2.alloc(fl_sort_bytes(n)));
+  FB_CK(b, b->tree.alloc(fl_tree_bytes(n)));
+  fl_sort_carve(&b->sb, b->sort1.p, n);
+  fl_sort_carve(&b->sb2, b->sort2.p, n);
+  fl_tree_carve(&b->tb, b->tree.p, n, ndim);
+  FB_CK(b, cudaMemcpy(b->pos.p, pos.data(), 16 * N, cudaMemcpyHostToDevice));
+  FB_CK(b, cudaMemcpy(b->vel[0].p, vel.data(), 16 * N, cudaMemcpyHostToDevice));
+  FB_CK(b, cudaMemset(b->vel[1].p, 0, 16 * N));
+  FB_CK(b, cudaMemset(b->fix.p, 0, 16 * N));
+  FB_CK(b, cudaMemset(b->mask.p, 0, 4 * N));
+  FB_CK(b, cudaMemcpy(b->gid.p, gid.data(), 4 * N, cudaMemcpyHostToDevice));
+  FB_CK(b, cudaMemcpy(b->charge.p, charge.data(), 4 * N, cudaMemcpyHostToDevice));
+  FB_CK(b, cudaMemcpy(b->off.p, off.data(), 4 * (size_t)(graphs + 1), cudaMemcpyHostToDevice));
+  FB_CK(b, cudaMemcpy(b->prm.p, prm.data(), sizeof(FlBatchParams) * (size_t)graphs, cudaMemcpyHostToDevice));
+  FB_CK(b, cudaMemcpy(b->row.p, row.data(), 4 * ((size_t)n + 1), cudaMemcpyHostToDevice));
+  if (m) {
+    FB_CK(b, cudaMemcpy(b->entry.p, entry.data(), 32 * (size_t)m, cudaMemcpyHostToDevice));
+    FB_CK(b, cudaMemcpy(b->code.p, code.data(), 8 * (size_t)m, cudaMemcpyHostToDevice));
+  }
+  b->cur = 0;
+  b->step = 0;
+  return FL_OK;
+}
+
+int32_t fl_batch_set_seed(fl_batch* b, uint32_t seed) {
+  int32_t rc = bcheck(b);
+  if (rc) return rc;
+  b->seed = seed;
+  return FL_OK;
+}
+
+int32_t fl_batch_enqueue(fl_batch* b, const double* alphas, int32_t ticks) {
+  int32_t rc = bcheck(b);
+  if (rc) return rc;
+  if (!b->graphs) return bfail(b, FL_E_STATE, "no graphs set");
+  if (ticks < 0 || (ticks && !alphas)) return bfail(b, FL_E_ARG, "bad alphas");
+  if (!ticks) return FL_OK;
+  const size_t need = (size_t)ticks * (size_t)b->graphs;
+  if (need > b->alpha_cap) {
+    FB_CK(b, cudaStreamSynchronize(b->st));
+    FB_CK(b, b->alphas.alloc(8 * need));
+    b->alpha_cap = need;
+  }
+  // copied on the stream, so after every tick already queued has read the previous alphas
+  FB_CK(b, cudaMemcpyAsync(b->alphas.p, alphas, 8 * need, cudaMemcpyHostToDevice, b->st));
+  for (int32_t k = 0; k < ticks; ++k)
+    encode_batch_tick(b, b->alphas.as<double>() + (size_t)k * b->graphs);
+  FB_CK(b, cudaGetLastError());
+  return FL_OK;
+}
+
+int32_t fl_batch_sync(fl_batch* b, float* pos4_out, float* vel4_out) {
+  int32_t rc = bcheck(b);
+  if (rc) return rc;
+  if (b->n && pos4_out)
+    FB_CK(b, cudaMemcpyAsync(pos4_out, b->pos.p, 16 * (size_t)b->n, cudaMemcpyDeviceToHost, b->st));
+  if (b->n && vel4_out)
+    FB_CK(b, cudaMemcpyAsync(vel4_out, bvel(b), 16 * (size_t)b->n, cudaMemcpyDeviceToHost, b->st));
+  uint32_t w = 0;
+  FB_CK(b, cudaMemcpyAsync(&w, b->errw.p, 4, cudaMemcpyDeviceToHost, b->st));
+  FB_CK(b, cudaStreamSynchronize(b->st));
+  if (w) {
+    cudaMemsetAsync(b->errw.p, 0, 4, b->st);
+    if (w & FL_ERR_LOOKBACK) return bfail(b, FL_E_TIMEOUT, "a device-side look-back wait gave up");
+    return bfail(b, FL_E_OVERFLOW, "a tree was malformed or a walk overflowed");
+  }
+  return FL_OK;
+}
+
+int32_t fl_batch_query(fl_batch* b, int32_t what, int64_t* out) {
+  int32_t rc = bcheck(b);
+  if (rc) return rc;
+  if (!out) return bfail(b, FL_E_ARG, "null output");
+  switch (what) {
+    case FL_Q_LAUNCHES: *out = b->launches; break;
+    case FL_Q_TICKS: *out = b->ticks; break;
+    case FL_Q_NODES: *out = b->n; break;
+    case FL_Q_DEVICE_BYTES: {
+      const Buf* all[] = {&b->pos, &b->vel[0], &b->vel[1], &b->fix, &b->mask, &b->gid, &b->off,
+                          &b->prm, &b->red, &b->gr, &b->alphas, &b->charge, &b->row, &b->entry,
+                          &b->code, &b->sort1, &b->sort2, &b->tree, &b->gid_pos};
+      size_t s = 0;
+      for (const Buf* x : all) s += x->bytes;
+      *out = (int64_t)s;
+      break;
+    }
+    default: return bfail(b, FL_E_ARG, "unknown query");
+  }
+  return FL_OK;
+}
+
+int32_t fl_batch_stream(fl_batch* b, void** stream) {
+  if (!b || !stream) return FL_E_ARG;
+  *stream = (void*)b->st;
+  return FL_OK;
+}
+
+}  // extern "C"

@@ -6,6 +6,48 @@
 
 #include "common.cuh"
 
+// ---------------------------------------------------------------- batches of graphs
+// One graph's values for a tick of a batch (device). The first five floats have the layout of a
+// single simulation's cube record (origin x, y, z, size, log2 size).
+struct FlGraph {
+  float origin[3], size, lg;
+  float T0;               // size^2 / theta^2: the walk's threshold at depth 0
+  float dmin2, dmax2;     // many-body distanceMin^2, distanceMax^2
+  float alpha, decay;     // this tick's alpha; velocity multiplier
+  float2 shift[3];        // the centre force's shift per axis (hi + lo), 0 without one
+  int32_t first, count;   // nodes [first, first + count)
+  float pad[2];
+};
+// A batch of independent graphs, concatenated: graph g owns nodes [off[g], off[g+1]) and, after
+// the tree's sort (by graph, then Morton code), the same range of sorted positions. Kernels
+// take it by value; graphs == 0 means a single simulation.
+struct FlSegs {
+  int graphs;
+  const int32_t* off;        // [graphs + 1]
+  const uint32_t* gid_node;  // [n] graph of each node
+  const uint32_t* gid_pos;   // [n] graph of each sorted position
+  const FlGraph* g;          // [graphs]
+};
+
+// A graph's fixed parameters in a batch: many-body theta^2, distanceMin^2, distanceMax^2; the
+// centre force's point and strength (0: none); the velocity multiplier (1 - velocityDecay).
+struct FlBatchParams {
+  double theta2, dmin2, dmax2;
+  double cx, cy, cz, cstrength;
+  double decay;
+};
+void fl_launch_breduce(const float4* pos, int n, int ndim, const uint32_t* gid, FlReduce* red,
+                       cudaStream_t st);
+void fl_launch_bgraph(int graphs, int ndim, const int32_t* off, const FlReduce* red,
+                      const FlBatchParams* prm, const double* alpha, FlGraph* gr, cudaStream_t st);
+void fl_launch_bmorton(const float4* pos, int n, int ndim, const uint32_t* gid, const FlGraph* gr,
+                       uint64_t* keys, uint32_t* vals, uint32_t* hist, int lo_bit, cudaStream_t st);
+void fl_launch_bgidkey(int n, const uint32_t* mperm, const uint32_t* gid, uint64_t* keys,
+                       uint32_t* vals, uint32_t* hist, cudaStream_t st);
+void fl_launch_bgather(int n, const uint32_t* order2, const uint64_t* mkeys, const uint32_t* mperm,
+                       const uint32_t* gid, uint64_t* skeys, uint32_t* perm, uint32_t* gid_pos,
+                       cudaStream_t st);
+
 // ---------------------------------------------------------------- radix sort (sort.cu)
 // Stable LSD sort of (uint64 key, uint32 value) pairs on the key bits [lo_bit, 64), 8 bits per
 // pass: one histogram pass fused into the key producer (or run on its own), then one onesweep
@@ -40,9 +82,11 @@ void fl_launch_center_apply(float4* pos, int n, int ndim, const FlReduce* red, d
                             double cy, double cz, double strength, cudaStream_t st);
 // v *= decay; p += v; pinned axes: p = fix, v = 0. When red != NULL, first shifts p by the
 // centre force of (cx, cy, cz, strength) computed from red->sum (the centre force fused).
+// In a batch (gr, gid non-null) each node takes its graph's decay and centre shift.
 void fl_launch_integrate(float4* pos, float4* vel, const float4* fix, const uint32_t* mask, int n,
                          int ndim, float decay, const FlReduce* red, double cx, double cy,
-                         double cz, double strength, cudaStream_t st);
+                         double cz, double strength, cudaStream_t st, const FlGraph* gr = nullptr,
+                         const uint32_t* gid = nullptr);
 void fl_launch_radial(const float4* pos, float4* vel, const float* radius, const float* strength,
                       int n, int ndim, float cx, float cy, float cz, float alpha, cudaStream_t st);
 void fl_launch_position(const float4* pos, float4* vel, const float* target, const float* strength,
@@ -54,8 +98,10 @@ struct FlLinkCsr {
   const float4* entry;     // [2m] (other node as int bits, distance, strength, bias share)
   const uint32_t* code;    // [2m] link * 2 + (this node is the target)
 };
+// In a batch (gr, gid non-null) each node's links use its graph's alpha.
 void fl_launch_link(const float4* pos, const float4* vel_in, float4* vel_out, FlLinkCsr csr, int n,
-                    int ndim, float alpha, uint32_t step, uint32_t seed, cudaStream_t st);
+                    int ndim, float alpha, uint32_t step, uint32_t seed, cudaStream_t st,
+                    const FlGraph* gr = nullptr, const uint32_t* gid = nullptr);
 
 // ---------------------------------------------------------------- many-body (tree.cu)
 struct FlTreeBufs {
@@ -103,22 +149,24 @@ void fl_launch_morton(const float4* pos, int n, int ndim, const FlReduce* red, u
 // records of the closed-form cell sums.
 void fl_launch_build(const FlTreeBufs* t, const uint64_t* skeys, const uint32_t* perm,
                      const float4* pos, const float* strength, bool closed, const float* cube,
-                     int fx_exp, cudaStream_t st, int64_t* launches);
+                     int fx_exp, cudaStream_t st, int64_t* launches, FlSegs segs = FlSegs{});
 // Heads, child counts and slots; cell values and centroids in closed form (strengths of one
 // sign, fixed-point sums at scale 2^fx_exp) or by the bottom-up recursion (both signs; FP64 sums
 // for the cells above depth fp64_depth, FP32 below).
 void fl_launch_aggregate(const FlTreeBufs* t, const uint64_t* skeys, bool closed, float sign,
                          const float* cube, int fx_exp, int fp64_depth, uint32_t* err,
-                         cudaStream_t st, int64_t* launches);
+                         cudaStream_t st, int64_t* launches, FlSegs segs = FlSegs{});
 // Scale exponent of the fixed-point cell sums: no sum over n points of weight <= wmax overflows.
 int fl_fixed_exponent(int64_t n, double wmax);
 // stats (optional): [0] child tests made by the warps (32 per child), [1] of those, tests by a
 // lane whose point needed them (the d3 traversal's own work)
 // group: points per traversal (16 or 32)
+// A batch (segs.graphs > 0): cube, alpha, theta2 and dmin2 are per graph (segs.g); dmax2 is
+// only tested when finite (pass the largest of the graphs').
 void fl_launch_walk(const FlTreeBufs* t, const uint32_t* perm, const float* cube, float4* vel,
                     float alpha, double theta2, double dmin2, double dmax2, uint32_t step,
                     uint32_t seed, uint32_t* err, unsigned long long* stats, int group,
-                    cudaStream_t st);
+                    cudaStream_t st, FlSegs segs = FlSegs{});
 // Exact all-pairs sum (theta ~ 0): O(n^2), tiled through shared memory.
 void fl_launch_allpairs(const float4* pos, const float* strength, float4* vel, int n, int ndim,
                         float alpha, float dmin2, float dmax2, uint32_t step, uint32_t seed,

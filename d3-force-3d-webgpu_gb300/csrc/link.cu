@@ -54,10 +54,12 @@ __global__ void __launch_bounds__(kThreads) k_link(const float4* __restrict__ po
                                                    const float4* __restrict__ entry,
                                                    const uint32_t* __restrict__ code, int n,
                                                    int ndim, float alpha, uint32_t step,
-                                                   uint32_t seed) {
+                                                   uint32_t seed, const FlGraph* __restrict__ gr,
+                                                   const uint32_t* __restrict__ gid) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const bool live = i < n;
+  if (gr && live) alpha = gr[gid[i]].alpha;  // a batch: the node's graph's alpha
   int r0 = 0, r1 = 0;
   float4 p = make_float4(0, 0, 0, 0), v = p;
   if (live) {
@@ -77,9 +79,10 @@ __global__ void __launch_bounds__(kThreads) k_link(const float4* __restrict__ po
     const int a = __shfl_sync(FL_FULL, r0, src), b = __shfl_sync(FL_FULL, r1, src);
     const float3 m = make_float3(__shfl_sync(FL_FULL, me.x, src), __shfl_sync(FL_FULL, me.y, src),
                                  __shfl_sync(FL_FULL, me.z, src));
+    const float am = __shfl_sync(FL_FULL, alpha, src);
     float3 part = make_float3(0.f, 0.f, 0.f);
     for (int e = a + lane; e < b; e += 32)
-      link_term(pos, vel_in, m, __ldg(entry + e), __ldg(code + e), ndim, alpha, step, seed, part);
+      link_term(pos, vel_in, m, __ldg(entry + e), __ldg(code + e), ndim, am, step, seed, part);
     part.x = fl::warp_sum(part.x), part.y = fl::warp_sum(part.y), part.z = fl::warp_sum(part.z);
     if (lane == src) acc = part;
   }
@@ -93,9 +96,10 @@ __global__ void __launch_bounds__(kThreads) k_link(const float4* __restrict__ po
 }  // namespace
 
 void fl_launch_link(const float4* pos, const float4* vel_in, float4* vel_out, FlLinkCsr csr, int n,
-                    int ndim, float alpha, uint32_t step, uint32_t seed, cudaStream_t st) {
+                    int ndim, float alpha, uint32_t step, uint32_t seed, cudaStream_t st,
+                    const FlGraph* gr, const uint32_t* gid) {
   int g = (n + kThreads - 1) / kThreads;
   if (g < 1) g = 1;
   k_link<<<g, kThreads, 0, st>>>(pos, vel_in, vel_out, csr.row, csr.entry, csr.code, n, ndim, alpha,
-                                 step, seed);
+                                 step, seed, gr, gid);
 }

@@ -78,6 +78,40 @@ __global__ void __launch_bounds__(kThreads) k_reduce(const float4* __restrict__ 
   }
 }
 
+// Per-graph bounding boxes and position sums of a batch, one node per thread. Nodes are grouped
+// by graph, so a warp's graph ids do not decrease along its lanes: each run of equal ids is
+// reduced toward its first lane (shuffles that stop at the run's end), which adds the run to
+// its graph's record.
+__global__ void __launch_bounds__(kThreads) k_breduce(const float4* __restrict__ pos, int n,
+                                                      int ndim, const uint32_t* __restrict__ gid,
+                                                      FlReduce* red) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const bool ok = i < n;
+  const uint32_t g = ok ? gid[i] : 0xffffffffu;
+  float4 p = ok ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+  float lo[3] = {p.x, p.y, p.z}, hi[3] = {p.x, p.y, p.z}, sm[3] = {p.x, p.y, p.z};
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t go = __shfl_down_sync(FL_FULL, g, o);
+    const bool same = lane + o < 32 && go == g;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float a = __shfl_down_sync(FL_FULL, lo[k], o), b = __shfl_down_sync(FL_FULL, hi[k], o),
+                  c = __shfl_down_sync(FL_FULL, sm[k], o);
+      if (same) lo[k] = fminf(lo[k], a), hi[k] = fmaxf(hi[k], b), sm[k] += c;
+    }
+  }
+  const uint32_t gp = __shfl_up_sync(FL_FULL, g, 1);
+  if (!ok || (lane > 0 && gp == g)) return;  // not the first lane of its run
+  FlReduce* r = red + g;
+  for (int k = 0; k < ndim; ++k) {
+    atomicMax(&r->lo[k], ~fl::ordered(lo[k]));
+    atomicMax(&r->hi[k], fl::ordered(hi[k]));
+    atomicAdd(&r->sum[k], (double)sm[k]);
+  }
+}
+
 // The centre force's shift, (mean - c) * strength per active axis, computed in FP64 once per
 // block and shared as a pair of floats (hi + lo), which the threads subtract in FP32.
 __device__ __forceinline__ void center_shift(const FlReduce* red, int n, int ndim, double cx,
@@ -124,13 +158,19 @@ __global__ void __launch_bounds__(kThreads) k_integrate(float4* __restrict__ pos
                                                         const uint32_t* __restrict__ mask, int n,
                                                         int ndim, float decay, const FlReduce* red,
                                                         double cx, double cy, double cz,
-                                                        double strength) {
+                                                        double strength, const FlGraph* gr,
+                                                        const uint32_t* __restrict__ gid) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   float2 sh[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
   if (red) center_shift(red, n, ndim, cx, cy, cz, strength, sh);  // block-uniform branch
   if (i >= n) return;
   float4 p = pos[i], v = vel[i];
-  if (red) {
+  if (gr) {  // a batch: the node's graph's decay and centre shift
+    const FlGraph& g = gr[gid[i]];
+    decay = g.decay;
+    sh[0] = g.shift[0], sh[1] = g.shift[1], sh[2] = g.shift[2];
+  }
+  if (red || gr) {
     p.x = sub_shift(p.x, sh[0]);
     p.y = sub_shift(p.y, sh[1]);
     p.z = sub_shift(p.z, sh[2]);
@@ -208,11 +248,17 @@ void fl_launch_center_apply(float4* pos, int n, int ndim, const FlReduce* red, d
   k_center_apply<<<grid_for(n, kThreads), kThreads, 0, st>>>(pos, n, ndim, red, cx, cy, cz, strength);
 }
 
+void fl_launch_breduce(const float4* pos, int n, int ndim, const uint32_t* gid, FlReduce* red,
+                       cudaStream_t st) {
+  k_breduce<<<grid_for(n, kThreads), kThreads, 0, st>>>(pos, n, ndim, gid, red);
+}
+
 void fl_launch_integrate(float4* pos, float4* vel, const float4* fix, const uint32_t* mask, int n,
                          int ndim, float decay, const FlReduce* red, double cx, double cy,
-                         double cz, double strength, cudaStream_t st) {
+                         double cz, double strength, cudaStream_t st, const FlGraph* gr,
+                         const uint32_t* gid) {
   k_integrate<<<grid_for(n, kThreads), kThreads, 0, st>>>(pos, vel, fix, mask, n, ndim, decay, red,
-                                                          cx, cy, cz, strength);
+                                                          cx, cy, cz, strength, gr, gid);
 }
 
 void fl_launch_radial(const float4* pos, float4* vel, const float* radius, const float* strength,

@@ -46,6 +46,8 @@ constexpr uint32_t kLeaf = 0x80000000u;
 constexpr uint32_t kIndex = 0x7fffffffu;
 constexpr uint32_t kLeafMark = 0x7fffffffu;  // meta word of a point (a cell's is count | depth << 26)
 constexpr uint32_t kCountMask = (1u << 26) - 1;
+constexpr uint32_t kNoParent = 0xffffffffu;  // a point alone in its graph (batches)
+constexpr uint8_t kGapDepth = 0xff;          // an internal index between two graphs (batches)
 constexpr int kThreads = 256;
 
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -127,6 +129,37 @@ __device__ __forceinline__ uint64_t cell_of(float x, float origin, int e, uint32
   return (uint64_t)c;
 }
 
+// d3 cover() of a bounding box (d3-octree): origin = floor(min); a power-of-two size doubled
+// until max < origin + size (FP64, one thread). cube5 = origin x, y, z, size, log2 size.
+__device__ void d3_cover(const FlReduce* red, int ndim, float* cube5) {
+  double lo0 = 0, lo1 = 0, lo2 = 0, hi0 = 0, hi1 = 0, hi2 = 0;
+  lo0 = floor((double)fl::unordered(~red->lo[0])), hi0 = (double)fl::unordered(red->hi[0]);
+  if (ndim > 1) lo1 = floor((double)fl::unordered(~red->lo[1])), hi1 = (double)fl::unordered(red->hi[1]);
+  if (ndim > 2) lo2 = floor((double)fl::unordered(~red->lo[2])), hi2 = (double)fl::unordered(red->hi[2]);
+  double size = 1;
+  int lg = 0;
+  while (lg < 1100 && !(hi0 < lo0 + size && (ndim < 2 || hi1 < lo1 + size) && (ndim < 3 || hi2 < lo2 + size)))
+    size *= 2, ++lg;
+  cube5[0] = (float)lo0, cube5[1] = (float)lo1, cube5[2] = (float)lo2;
+  cube5[3] = (float)size, cube5[4] = (float)lg;
+}
+
+// The left-aligned Morton key of p in the cube with the given origin, e = LEVELS - log2(size).
+__device__ __forceinline__ uint64_t morton_key(float4 p, const float* origin, int e, int ndim) {
+  const int L = levels_of(ndim), bits = L * ndim;
+  const uint32_t top = (1u << L) - 1;
+  const uint64_t qx = cell_of(p.x, origin[0], e, top);
+  uint64_t key;
+  if (ndim == 3)
+    key = spread3(qx) | spread3(cell_of(p.y, origin[1], e, top)) << 1 |
+          spread3(cell_of(p.z, origin[2], e, top)) << 2;
+  else if (ndim == 2)
+    key = spread2(qx) | spread2(cell_of(p.y, origin[1], e, top)) << 1;
+  else
+    key = qx;
+  return key << (64 - bits);
+}
+
 // Bounding box -> d3 cube -> keys; digit histograms of the sort passes in the same read.
 __global__ void __launch_bounds__(kThreads) k_morton(const float4* __restrict__ pos, int n,
                                                      int ndim, const FlReduce* red,
@@ -134,54 +167,24 @@ __global__ void __launch_bounds__(kThreads) k_morton(const float4* __restrict__ 
                                                      uint32_t* __restrict__ vals,
                                                      uint32_t* __restrict__ hist, int lo_bit,
                                                      float* cube_out) {
-  __shared__ float s_origin[3];
-  __shared__ int s_lg;
+  __shared__ float s_cube[5];
   __shared__ uint32_t sh[8 * 256];
-  const int L = levels_of(ndim), bits = L * ndim, passes = (64 - lo_bit + 7) / 8;
+  const int passes = (64 - lo_bit + 7) / 8;
   if (threadIdx.x == 0) {
-    // d3 cover(): x0 = floor(min); double a power-of-two size until max < x0 + size (FP64)
-    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-    for (int k = 0; k < ndim; ++k) {
-      lo[k] = floor((double)fl::unordered(~red->lo[k]));
-      hi[k] = (double)fl::unordered(red->hi[k]);
-    }
-    double size = 1;
-    int lg = 0;
-    for (;;) {
-      bool inside = true;
-      for (int k = 0; k < ndim; ++k)
-        if (!(hi[k] < lo[k] + size)) inside = false;
-      if (inside || lg >= 1100) break;
-      size *= 2, ++lg;
-    }
-    for (int k = 0; k < 3; ++k) s_origin[k] = (float)lo[k];
-    s_lg = lg;
-    if (blockIdx.x == 0) {
-      cube_out[0] = (float)lo[0], cube_out[1] = (float)lo[1], cube_out[2] = (float)lo[2];
-      cube_out[3] = (float)size;
-      cube_out[4] = (float)lg;
-    }
+    d3_cover(red, ndim, s_cube);
+    if (blockIdx.x == 0)
+      for (int k = 0; k < 5; ++k) cube_out[k] = s_cube[k];
   }
   for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) sh[i] = 0;
   __syncthreads();
-  const int e = L - s_lg;
-  const uint32_t top = (1u << L) - 1;
+  const int e = levels_of(ndim) - (int)s_cube[4];
   const int stride = gridDim.x * blockDim.x;
   for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
     const int i = base + threadIdx.x;
     const bool ok = i < n;
     uint64_t key = 0;
     if (ok) {
-      float4 p = pos[i];
-      uint64_t qx = cell_of(p.x, s_origin[0], e, top);
-      if (ndim == 3)
-        key = spread3(qx) | spread3(cell_of(p.y, s_origin[1], e, top)) << 1 |
-              spread3(cell_of(p.z, s_origin[2], e, top)) << 2;
-      else if (ndim == 2)
-        key = spread2(qx) | spread2(cell_of(p.y, s_origin[1], e, top)) << 1;
-      else
-        key = qx;
-      key <<= (64 - bits);
+      key = morton_key(pos[i], s_cube, e, ndim);
       keys[i] = key;
       vals[i] = (uint32_t)i;
     }
@@ -193,9 +196,120 @@ __global__ void __launch_bounds__(kThreads) k_morton(const float4* __restrict__ 
     if (sh[i]) atomicAdd(&hist[i], sh[i]);
 }
 
-__device__ __forceinline__ int kdelta(const uint64_t* __restrict__ k, int n, uint64_t ki, int i,
-                                      int j) {
-  if (j < 0 || j >= n) return -1;
+// ---- batches of graphs: the per-graph tick values, the keys, and the sort by graph
+
+// One thread per graph: the graph's d3 cube from its bounding box, the walk's threshold, its
+// distances, this tick's alpha, its velocity multiplier and its centre force's shift.
+__global__ void __launch_bounds__(kThreads) k_bgraph(int graphs, int ndim, const int32_t* __restrict__ off,
+                                                     const FlReduce* __restrict__ red,
+                                                     const FlBatchParams* __restrict__ prm,
+                                                     const double* __restrict__ alpha,
+                                                     FlGraph* __restrict__ gr) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= graphs) return;
+  FlGraph o;
+  const int first = off[g], count = off[g + 1] - off[g];
+  if (count > 0) {
+    d3_cover(red + g, ndim, o.origin);
+  } else {
+    o.origin[0] = o.origin[1] = o.origin[2] = 0.f, o.size = 1.f, o.lg = 0.f;
+  }
+  const FlBatchParams p = prm[g];
+  o.T0 = (float)((double)o.size * (double)o.size / p.theta2);
+  o.dmin2 = (float)p.dmin2;
+  o.dmax2 = p.dmax2 > 3e38 ? INFINITY : (float)p.dmax2;
+  o.alpha = (float)alpha[g];
+  o.decay = (float)p.decay;
+  const double c[3] = {p.cx, p.cy, p.cz};
+  for (int k = 0; k < 3; ++k) {
+    const double d = k < ndim && count > 0 && p.cstrength != 0 ? (red[g].sum[k] / count - c[k]) * p.cstrength : 0.0;
+    const float h = (float)d;
+    o.shift[k] = make_float2(h, (float)(d - (double)h));
+  }
+  o.first = first, o.count = count;
+  o.pad[0] = o.pad[1] = 0.f;
+  gr[g] = o;
+}
+
+// Morton keys of a batch, each point in its own graph's cube; histograms as k_morton.
+__global__ void __launch_bounds__(kThreads) k_bmorton(const float4* __restrict__ pos, int n,
+                                                      int ndim, const uint32_t* __restrict__ gid,
+                                                      const FlGraph* __restrict__ gr,
+                                                      uint64_t* __restrict__ keys,
+                                                      uint32_t* __restrict__ vals,
+                                                      uint32_t* __restrict__ hist, int lo_bit) {
+  __shared__ uint32_t sh[8 * 256];
+  const int passes = (64 - lo_bit + 7) / 8;
+  for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) sh[i] = 0;
+  __syncthreads();
+  const int stride = gridDim.x * blockDim.x;
+  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const int i = base + threadIdx.x;
+    const bool ok = i < n;
+    uint64_t key = 0;
+    if (ok) {
+      const FlGraph& g = gr[gid[i]];
+      key = morton_key(pos[i], g.origin, levels_of(ndim) - (int)g.lg, ndim);
+      keys[i] = key;
+      vals[i] = (uint32_t)i;
+    }
+    for (int p = 0; p < passes; ++p)
+      fl::hist_add(sh + p * 256, (uint32_t)(key >> (lo_bit + 8 * p)) & 255u, ok);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < passes * 256; i += blockDim.x)
+    if (sh[i]) atomicAdd(&hist[i], sh[i]);
+}
+
+// The second sort's input: the graph of each point in Morton order, in key bits [48, 64), and
+// the point's Morton-order position; with the histograms of those two digits.
+__global__ void __launch_bounds__(kThreads) k_bgidkey(int n, const uint32_t* __restrict__ mperm,
+                                                      const uint32_t* __restrict__ gid,
+                                                      uint64_t* __restrict__ keys,
+                                                      uint32_t* __restrict__ vals,
+                                                      uint32_t* __restrict__ hist) {
+  __shared__ uint32_t sh[2 * 256];
+  for (int i = threadIdx.x; i < 2 * 256; i += blockDim.x) sh[i] = 0;
+  __syncthreads();
+  const int stride = gridDim.x * blockDim.x;
+  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const int i = base + threadIdx.x;
+    const bool ok = i < n;
+    uint64_t key = 0;
+    if (ok) {
+      key = (uint64_t)gid[mperm[i]] << 48;
+      keys[i] = key;
+      vals[i] = (uint32_t)i;
+    }
+    fl::hist_add(sh, (uint32_t)(key >> 48) & 255u, ok);
+    fl::hist_add(sh + 256, (uint32_t)(key >> 56) & 255u, ok);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 2 * 256; i += blockDim.x)
+    if (sh[i]) atomicAdd(&hist[i], sh[i]);
+}
+
+// The order by (graph, Morton code): position j takes the Morton-order point at order2[j].
+__global__ void __launch_bounds__(kThreads) k_bgather(int n, const uint32_t* __restrict__ order2,
+                                                      const uint64_t* __restrict__ mkeys,
+                                                      const uint32_t* __restrict__ mperm,
+                                                      const uint32_t* __restrict__ gid,
+                                                      uint64_t* __restrict__ skeys,
+                                                      uint32_t* __restrict__ perm,
+                                                      uint32_t* __restrict__ gid_pos) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const uint32_t v = order2[j];
+  const uint32_t node = mperm[v];
+  skeys[j] = mkeys[v];
+  perm[j] = node;
+  gid_pos[j] = gid[node];
+}
+
+// Common prefix of sorted keys i and j (index tie-break), -1 outside [lo, hi] (one graph's range)
+__device__ __forceinline__ int kdelta(const uint64_t* __restrict__ k, int lo, int hi, uint64_t ki,
+                                      int i, int j) {
+  if (j < lo || j > hi) return -1;
   uint64_t kj = k[j];
   return ki != kj ? __clzll(ki ^ kj) : 64 + __clz(i ^ j);
 }
@@ -240,11 +354,21 @@ __global__ void __launch_bounds__(kThreads) k_build(
     uint32_t* __restrict__ left, uint32_t* __restrict__ right, uint32_t* __restrict__ parent,
     uint32_t* __restrict__ leaf_parent, uint32_t* __restrict__ range, uint8_t* __restrict__ depth,
     float4* __restrict__ leaf, D4* __restrict__ wsum, D4* __restrict__ wtot,
-    const float* __restrict__ cube, int fx_exp) {
+    const float* __restrict__ cube, int fx_exp, FlSegs seg) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int L = levels_of(ndim), bits = L * ndim;
+  // the sorted range of this point's graph (a batch), and that graph's cube
+  int lo = 0, hi = n - 1;
+  const float* cb = cube;
+  if (seg.graphs && i < n) {
+    const uint32_t g = seg.gid_pos[i];
+    lo = seg.off[g], hi = seg.off[g + 1] - 1;
+    cb = seg.g[g].origin;
+  }
   const uint64_t ki = i < n ? k[i] : 0;
-  const int up = i < n ? kdelta(k, n, ki, i, i + 1) : -1, dn = i < n ? kdelta(k, n, ki, i, i - 1) : -1;
+  const int up = i < n ? kdelta(k, lo, hi, ki, i, i + 1) : -1;
+  const int dn = i < n ? kdelta(k, lo, hi, ki, i, i - 1) : -1;
+  if (i < n && lo == hi) leaf_parent[i] = kNoParent;  // alone in its graph: no tree
   D4 wrec = mk4(0, 0, 0, 0);
   if (i < n) {
     const uint32_t node = perm[i];
@@ -254,30 +378,37 @@ __global__ void __launch_bounds__(kThreads) k_build(
     if (wsum) {
       const int dmx = up > dn ? up : dn;
       const int lD = (dmx >= bits ? L : dmx / ndim) + 1;  // the point's d3 leaf depth
-      const float sF = offset_scale(cube);
+      const float sF = offset_scale(cb);
       const long long W =
           __float2ll_rn(fabsf(p.w * damp(ndim, lD)) * __int_as_float((fx_exp + 127) << 23));
-      wrec = mk4(W, mulhi62(W, fx_offset(p.x, cube[0], sF)),
-                 ndim > 1 ? mulhi62(W, fx_offset(p.y, cube[1], sF)) : 0,
-                 ndim > 2 ? mulhi62(W, fx_offset(p.z, cube[2], sF)) : 0);
+      wrec = mk4(W, mulhi62(W, fx_offset(p.x, cb[0], sF)),
+                 ndim > 1 ? mulhi62(W, fx_offset(p.y, cb[1], sF)) : 0,
+                 ndim > 2 ? mulhi62(W, fx_offset(p.z, cb[2], sF)) : 0);
     }
   }
   if (wsum)  // block-uniform
     block_prefix4(wrec, wsum, wtot, i < n ? i : -1);
   if (i >= n - 1) return;
+  if (i == hi) {  // the last point of a graph: this internal index belongs to no tree
+    left[i] = right[i] = kNoParent;
+    range[2 * i] = range[2 * i + 1] = (uint32_t)i;
+    depth[i] = kGapDepth;
+    return;
+  }
+  if (i == lo) parent[i] = (uint32_t)i;  // a graph's root is its own parent
   const int d = up > dn ? 1 : -1;
   const int dmin = up > dn ? dn : up;
   int64_t lmax = 2;
-  while (kdelta(k, n, ki, i, (int)(i + lmax * d)) > dmin) lmax *= 2;
+  while (kdelta(k, lo, hi, ki, i, (int)(i + lmax * d)) > dmin) lmax *= 2;
   int64_t len = 0;
   for (int64_t t = lmax >> 1; t >= 1; t >>= 1)
-    if (kdelta(k, n, ki, i, (int)(i + (len + t) * d)) > dmin) len += t;
+    if (kdelta(k, lo, hi, ki, i, (int)(i + (len + t) * d)) > dmin) len += t;
   const int j = (int)(i + len * d);
-  const int dnode = kdelta(k, n, ki, i, j);
+  const int dnode = kdelta(k, lo, hi, ki, i, j);
   int64_t s = 0, t = len;
   do {
     t = (t + 1) >> 1;
-    if (kdelta(k, n, ki, i, (int)(i + (s + t) * d)) > dnode) s += t;
+    if (kdelta(k, lo, hi, ki, i, (int)(i + (s + t) * d)) > dnode) s += t;
   } while (t > 1);
   const int split = (int)(i + s * d + (d < 0 ? -1 : 0));
   const int first = i < j ? i : j, last = i < j ? j : i;
@@ -337,14 +468,18 @@ __global__ void __launch_bounds__(kThreads) k_frontier(
   const bool pt = t >= n - 1;
   const uint32_t x = pt ? (uint32_t)(t - (n - 1)) : (uint32_t)t;
   uint32_t rec = 0;
-  if (pt || x != 0) {
-    const uint32_t p = pt ? leaf_parent[x] : parent[x];
+  // the parent cell's binary node: none for a graph's root, an index between two graphs, or a
+  // point alone in its graph
+  uint32_t p = kNoParent;
+  if (pt) p = leaf_parent[x];
+  else if (depth[x] != kGapDepth && parent[x] != x) p = parent[x];
+  if (p != kNoParent) {
     const int Dp = depth[p];
     if (pt || depth[x] > Dp) {
       uint32_t h = p;
-      for (int guard = 0; h != 0; ++guard) {  // equal depths: splits inside one cell
+      for (int guard = 0;; ++guard) {  // equal depths: splits inside one cell
         const uint32_t up = parent[h];
-        if (depth[up] < Dp) break;
+        if (up == h || depth[up] < Dp) break;
         h = up;
         if (guard > 64) {
           atomicOr(err, FL_ERR_TREE);
@@ -379,8 +514,11 @@ __global__ void __launch_bounds__(kThreads) k_heads(int n, int ndim,
   uint32_t c = 0;
   if (i < n - 1) {
     const int D = depth[i];
-    const bool head = i == 0 || depth[parent[i]] < D;
-    if (head) c = D >= levels_of(ndim) ? range[2 * i + 1] - range[2 * i] + 1 : __popc(omask[i]);
+    if (D != kGapDepth) {
+      const uint32_t pa = parent[i];
+      const bool head = pa == (uint32_t)i || depth[pa] < D;  // a graph's root, or a deeper cell
+      if (head) c = D >= levels_of(ndim) ? range[2 * i + 1] - range[2 * i] + 1 : __popc(omask[i]);
+    }
     count[i] = c;
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -452,10 +590,11 @@ __global__ void __launch_bounds__(kTopThreads) k_top4(D4* tot, int nb) {
   top_scan<D4>(tot, nb, mk4(0, 0, 0, 0));
 }
 
-// first child slot of head x: slot 0 is the root's own; children follow in head order
+// first child slot of head x: slots [0, roots) hold the roots (one per graph), children follow
+// in head order
 __device__ __forceinline__ uint32_t first_slot(const uint32_t* first, const uint32_t* ctot,
-                                               uint32_t x) {
-  return 1u + first[x] + ctot[x >> 8];
+                                               uint32_t x, uint32_t roots) {
+  return roots + first[x] + ctot[x >> 8];
 }
 
 // Cells from the prefix sums (strengths of one sign, `sign`): value and centroid of every head.
@@ -466,12 +605,14 @@ __global__ void __launch_bounds__(kThreads) k_cells_closed(int n, int ndim, floa
                                                            const D4* __restrict__ P,
                                                            const D4* __restrict__ Ptot,
                                                            const float4* __restrict__ leaf,
-                                                           const float* __restrict__ cube,
+                                                           const float* __restrict__ cube1,
                                                            int fx_exp,
-                                                           float4* __restrict__ cell) {
+                                                           float4* __restrict__ cell,
+                                                           FlSegs seg) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n - 1 || !count[i]) return;
   const uint32_t a = range[2 * i], b = range[2 * i + 1];
+  const float* cube = seg.graphs ? seg.g[seg.gid_pos[a]].origin : cube1;
   // prefix sums: within the 256-point block, plus the blocks before it; exact in fixed point
   const D4 hi = add4(P[b], Ptot[b >> 8]);
   const D4 lo = a ? add4(P[a - 1], Ptot[(a - 1) >> 8]) : mk4(0, 0, 0, 0);
@@ -507,6 +648,7 @@ __global__ void __launch_bounds__(kThreads) k_cells_climb(
   const int L = levels_of(ndim);
   const double c1 = sqrt(4.0 / (double)(1 << ndim));
   uint32_t node = leaf_parent[s];
+  if (node == kNoParent) return;  // a point alone in its graph
   for (int guard = 0;; ++guard) {
     if (guard > 256) {
       atomicOr(err, FL_ERR_TREE);
@@ -550,7 +692,7 @@ __global__ void __launch_bounds__(kThreads) k_cells_climb(
       out.w = fabs(tv) <= ta * 0x1p-20 ? 0.f : (float)(tv * c1);
       cell[node] = out;
     }
-    if (node == 0) return;
+    if (parent[node] == node) return;  // a graph's root
     node = parent[node];
   }
 }
@@ -560,18 +702,21 @@ __global__ void __launch_bounds__(kThreads) k_cells_climb(
 // the root also fills slot 0. Threads as in k_frontier.
 __global__ void __launch_bounds__(kThreads) k_slots(
     int n, int ndim, const uint32_t* __restrict__ head_of, const uint32_t* __restrict__ omask,
+    const uint32_t* __restrict__ parent,
     const uint32_t* __restrict__ range, const uint8_t* __restrict__ depth,
     const uint32_t* __restrict__ count, const uint32_t* __restrict__ first,
     const uint32_t* __restrict__ ctot, const float4* __restrict__ cell,
     const float4* __restrict__ leaf, float4* __restrict__ cdata, uint2* __restrict__ cmeta,
-    uint32_t* err) {
+    uint32_t* err, FlSegs seg) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= 2 * n - 1) return;
   const bool pt = t >= n - 1;
   const uint32_t x = pt ? (uint32_t)(t - (n - 1)) : (uint32_t)t;
-  if (!pt && x == 0) {
-    cdata[0] = cell[0];
-    cmeta[0] = make_uint2(first_slot(first, ctot, 0u), count[0] | ((uint32_t)depth[0] << 26));
+  const uint32_t roots = seg.graphs ? (uint32_t)seg.graphs : 1u;
+  if (!pt && depth[x] != kGapDepth && parent[x] == x) {  // a graph's root: its own slot
+    const uint32_t rs = seg.graphs ? seg.gid_pos[x] : 0u;
+    cdata[rs] = cell[x];
+    cmeta[rs] = make_uint2(first_slot(first, ctot, x, roots), count[x] | ((uint32_t)depth[x] << 26));
   }
   const uint32_t rec = head_of[t];
   if (!(rec & 0x80000000u)) return;
@@ -579,7 +724,7 @@ __global__ void __launch_bounds__(kThreads) k_slots(
   const uint32_t rank = depth[h] >= levels_of(ndim)
                             ? (pt ? x : range[2 * x]) - range[2 * h]
                             : (uint32_t)__popc(omask[h] & ((1u << oct) - 1u));
-  const uint32_t slot = first_slot(first, ctot, h) + rank;
+  const uint32_t slot = first_slot(first, ctot, h, roots) + rank;
   if (rank >= count[h] || slot >= 2u * (uint32_t)n + 1u) {  // a malformed tree
     atomicOr(err, FL_ERR_TREE);
     return;
@@ -589,7 +734,7 @@ __global__ void __launch_bounds__(kThreads) k_slots(
     cmeta[slot] = make_uint2(x, kLeafMark);
   } else {
     cdata[slot] = cell[x];
-    cmeta[slot] = make_uint2(first_slot(first, ctot, x), count[x] | ((uint32_t)depth[x] << 26));
+    cmeta[slot] = make_uint2(first_slot(first, ctot, x, roots), count[x] | ((uint32_t)depth[x] << 26));
   }
 }
 
@@ -685,13 +830,20 @@ __device__ __forceinline__ void rare_case(uint32_t meta, uint32_t top, uint32_t 
 // stats (STATS): [0] child tests (G per child), [1] tests a lane's own traversal needed,
 // [2] deepest stack, [3] lanes that opened a cell, [4] lanes that applied a cell or point,
 // [5] pair rounds that took the uncommon-case branch.
-template <int NDIM, int G, bool STATS, bool DMAX>
+__device__ __forceinline__ float below(float d2) {  // l < d2 <=> l <= below(d2), for l >= 0
+  return d2 > 0.f ? __uint_as_float(__float_as_uint(d2) - 1u) : -1.f;
+}
+
+// BATCH: the points belong to a batch of graphs (segs): each graph has its own tree (root slot =
+// its index), cube, theta, distances and alpha; a group's points may span graphs.
+template <int NDIM, int G, bool STATS, bool DMAX, bool BATCH>
 __global__ void __launch_bounds__(kWalkThreads) k_walk(
     const float4* __restrict__ cdata, const uint2* __restrict__ cmeta,
     const float4* __restrict__ leaf, const uint32_t* __restrict__ perm,
     const float* __restrict__ cube, float4* __restrict__ vel, int n, float alpha,
     double theta2, float dmin2, float dmax2, uint32_t step, uint32_t seed, uint32_t* err,
-    unsigned long long* stats, uint4* __restrict__ spill, int nwarps, uint32_t* work) {
+    unsigned long long* stats, uint4* __restrict__ spill, int nwarps, uint32_t* work,
+    FlSegs segs) {
   constexpr int NG = 32 / G;
   // the stack of a group: kStack entries in shared memory, then up to kWalkStack(NDIM, G) in
   // all, the rest in this warp slot's region of the spill buffer
@@ -703,9 +855,9 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
   const uint32_t gmask = G == 32 ? FL_FULL : (((1u << G) - 1u) << gbase);
   const uint32_t lanebit = 1u << lane;
   // (size / 2^k)^2 / theta^2 = T0 * 4^-k, exactly (a power-of-two scaling)
-  const float T0 = (float)((double)cube[3] * (double)cube[3] / theta2);
+  const float T0 = BATCH ? 0.f : (float)((double)cube[3] * (double)cube[3] / theta2);
   // l < dmin2  <=>  l <= the largest float below dmin2 (l >= 0)
-  const float dmin_le = dmin2 > 0.f ? __uint_as_float(__float_as_uint(dmin2) - 1u) : -1.f;
+  const float dmin_le = below(dmin2);
   const uint32_t slot_cap = 2u * (uint32_t)n + 1u;
   unsigned long long st_tests = 0, st_useful = 0, st_open = 0, st_apply = 0, st_rare = 0;
   int maxsp = 0;
@@ -733,8 +885,28 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
   const uint32_t myid = live ? perm[t] : 0;
   uint64_t AX = 0, AY = 0, AZ = 0;  // force sums, one per child of a round's pair
   const uint64_t MX = pk2(me.x, me.x), MY = pk2(me.y, me.y), MZ = pk2(me.z, me.z);
-  if (gl == 0 && act) sset(0, make_uint4(0u, 1u, 0u, act));  // the root: slot 0, top depth 0
-  int sp = act ? 1 : 0;
+  // the lane's own graph: what its uncommon cases and distanceMax use
+  float myT0 = T0, mydmin2 = dmin2, mydmax2 = dmax2;
+  int sp;
+  if (!BATCH) {
+    if (gl == 0 && act) sset(0, make_uint4(0u, 1u, 0u, act));  // the root: slot 0, top depth 0
+    sp = act ? 1 : 0;
+  } else {
+    // one root entry per graph among the group's points (a graph of one point has no tree);
+    // a stack entry's third word is its top depth | graph << 8
+    const uint32_t g = live ? segs.gid_pos[t] : 0xffffffffu;
+    bool tree = false;
+    if (live) {
+      const FlGraph& gr = segs.g[g];
+      myT0 = gr.T0, mydmin2 = gr.dmin2, mydmax2 = gr.dmax2;
+      tree = gr.count > 1;
+    }
+    const uint32_t peers = __match_any_sync(FL_FULL, tree ? g : 0xffffffffu) & gmask;
+    const bool leader = tree && (peers & (lanebit - 1u)) == 0;
+    const uint32_t leaders = __ballot_sync(FL_FULL, leader) & gmask;
+    if (leader) sset(__popc(leaders & (lanebit - 1u)), make_uint4(g, 1u, g << 8, peers));
+    sp = __popc(leaders);
+  }
   if (sp > maxsp) maxsp = sp;
   __syncwarp();
   uint32_t guard = 0;
@@ -778,7 +950,8 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
     const uint32_t own_first = __shfl_sync(FL_FULL, e.x, (int)own, G);
     const uint32_t own_exc = __shfl_sync(FL_FULL, exc, (int)own, G);
     const uint32_t my_mask = __shfl_sync(FL_FULL, e.w, (int)own, G);
-    const uint32_t my_top = __shfl_sync(FL_FULL, e.z, (int)own, G);
+    const uint32_t my_z = __shfl_sync(FL_FULL, e.z, (int)own, G);
+    const uint32_t my_top = my_z & 0xffu, my_g = my_z >> 8;
     const uint32_t my_slot = own_first + ((uint32_t)gl - own_exc);
     __syncwarp();
     const int jmax = G == 32 ? total : (int)__reduce_max_sync(FL_FULL, (unsigned)total);
@@ -791,15 +964,20 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
       uint32_t mask = q.w != 0.f ? my_mask : 0u;  // d3 skips a zero value and all it holds
       if (lf && m.x - (uint32_t)base < 32u) mask &= ~(1u << (m.x - (uint32_t)base));  // itself
       const bool chain = !lf && my_top < D;
+      float T0c = T0, alc = alpha, dminc = dmin_le;
+      if (BATCH) {  // the child's graph: that of the lanes that test it
+        const FlGraph& gr = segs.g[my_g];
+        T0c = gr.T0, alc = gr.alpha, dminc = below(gr.dmin2);
+      }
       // a point is never approximated (its sum is the same either way); a cell is opened when
       // even its deepest depth fails the theta test
-      const float topen = lf ? -INFINITY : T0 * pow4neg(D);
-      const float ttop = chain ? T0 * pow4neg(my_top) : topen;
-      const float va = chain ? q.w * alpha * damp(NDIM, (int)(D - my_top)) : q.w * alpha;
+      const float topen = lf ? -INFINITY : T0c * pow4neg(D);
+      const float ttop = chain ? T0c * pow4neg(my_top) : topen;
+      const float va = chain ? q.w * alc * damp(NDIM, (int)(D - my_top)) : q.w * alc;
       float* pa = reinterpret_cast<float*>(spair + (gl & ~1));
       pa[gl & 1] = q.x, pa[2 + (gl & 1)] = q.y, pa[4 + (gl & 1)] = q.z, pa[6 + (gl & 1)] = va;
-      stest[gl] = make_uint4(__float_as_uint(topen), __float_as_uint(fmaxf(ttop, dmin_le)), mask, m.x);
-      scold[gl] = make_uint2(m.y, my_top);
+      stest[gl] = make_uint4(__float_as_uint(topen), __float_as_uint(fmaxf(ttop, dminc)), mask, m.x);
+      scold[gl] = make_uint2(m.y, my_top | my_g << 8);
     } else if (gl < ((jmax + 1) & ~1)) {  // pad the group's batch: a child no lane tests
       float* pa = reinterpret_cast<float*>(spair + (gl & ~1));
       pa[gl & 1] = 0.f, pa[2 + (gl & 1)] = 0.f, pa[4 + (gl & 1)] = 0.f, pa[6 + (gl & 1)] = 0.f;
@@ -819,7 +997,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
       float2 l = up2(L);
       const bool m0 = r0.z & lanebit, m1 = r1.z & lanebit;
       const bool o0 = m0 && __uint_as_float(r0.x) >= l.x, o1 = m1 && __uint_as_float(r1.x) >= l.y;
-      const bool a0 = m0 && !o0 && (!DMAX || l.x < dmax2), a1 = m1 && !o1 && (!DMAX || l.y < dmax2);
+      const bool a0 = m0 && !o0 && (!DMAX || l.x < mydmax2), a1 = m1 && !o1 && (!DMAX || l.y < mydmax2);
       float v0 = pb.z, v1 = pb.w;
       const bool c0 = a0 && (l.x <= __uint_as_float(r0.y) || zp.x == 0.f);
       const bool c1 = a1 && (l.y <= __uint_as_float(r1.y) || zp.y == 0.f);
@@ -829,11 +1007,11 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
         float2 dx = up2(DX), dy = up2(DY), dz = up2(DZ);
         if (c0) {
           const uint2 k0 = scold[j];
-          rare_case<NDIM>(k0.x, k0.y, r0.w, T0, dmin2, myid, perm, n, step, seed, v0, dx.x, dy.x, dz.x, l.x);
+          rare_case<NDIM>(k0.x, k0.y & 0xffu, r0.w, myT0, mydmin2, myid, perm, n, step, seed, v0, dx.x, dy.x, dz.x, l.x);
         }
         if (c1) {
           const uint2 k1 = scold[j + 1];
-          rare_case<NDIM>(k1.x, k1.y, r1.w, T0, dmin2, myid, perm, n, step, seed, v1, dx.y, dy.y, dz.y, l.y);
+          rare_case<NDIM>(k1.x, k1.y & 0xffu, r1.w, myT0, mydmin2, myid, perm, n, step, seed, v1, dx.y, dy.y, dz.y, l.y);
         }
         DX = pk2(dx.x, dx.y), DY = pk2(dy.x, dy.y), DZ = pk2(dz.x, dz.y);
       }
@@ -846,13 +1024,15 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
       const uint32_t om1 = __ballot_sync(FL_FULL, o1) & gmask;
       if (om0 | om1) {  // push the children some lanes must open (rare next to the tests)
         if (om0) {
-          const uint32_t k0 = scold[j].x;
-          if (sp < kAll && gl == 0) sset(sp, make_uint4(r0.w, k0 & kCountMask, ((k0 >> 26) & 31u) + 1u, om0));
+          const uint2 k0 = scold[j];
+          if (sp < kAll && gl == 0)
+            sset(sp, make_uint4(r0.w, k0.x & kCountMask, (((k0.x >> 26) & 31u) + 1u) | (k0.y & ~0xffu), om0));
           ++sp;
         }
         if (om1) {
-          const uint32_t k1 = scold[j + 1].x;
-          if (sp < kAll && gl == 0) sset(sp, make_uint4(r1.w, k1 & kCountMask, ((k1 >> 26) & 31u) + 1u, om1));
+          const uint2 k1 = scold[j + 1];
+          if (sp < kAll && gl == 0)
+            sset(sp, make_uint4(r1.w, k1.x & kCountMask, (((k1.x >> 26) & 31u) + 1u) | (k1.y & ~0xffu), om1));
           ++sp;
         }
         if (sp > kAll) {  // beyond the bound on the stack's depth: a malformed tree
@@ -1040,13 +1220,13 @@ int fl_fixed_exponent(int64_t n, double wmax) {
 
 void fl_launch_build(const FlTreeBufs* t, const uint64_t* skeys, const uint32_t* perm,
                      const float4* pos, const float* strength, bool closed, const float* cube,
-                     int fx_exp, cudaStream_t st, int64_t* launches) {
+                     int fx_exp, cudaStream_t st, int64_t* launches, FlSegs segs) {
   const int n = t->n;
   const int nb = (n + kThreads - 1) / kThreads;
   k_build<<<nb, kThreads, 0, st>>>(skeys, perm, pos, strength, n, t->ndim, t->left, t->right,
                                    t->parent, t->leaf_parent, t->range, t->depth, t->leaf,
                                    closed ? reinterpret_cast<D4*>(t->wsum) : nullptr,
-                                   reinterpret_cast<D4*>(t->wtiles), cube, fx_exp);
+                                   reinterpret_cast<D4*>(t->wtiles), cube, fx_exp, segs);
   ++*launches;
   if (closed) {
     k_top4<<<1, kTopThreads, 0, st>>>(reinterpret_cast<D4*>(t->wtiles), nb);
@@ -1056,7 +1236,7 @@ void fl_launch_build(const FlTreeBufs* t, const uint64_t* skeys, const uint32_t*
 
 void fl_launch_aggregate(const FlTreeBufs* t, const uint64_t* skeys, bool closed, float sign,
                          const float* cube, int fx_exp, int fp64_depth, uint32_t* err,
-                         cudaStream_t st, int64_t* launches) {
+                         cudaStream_t st, int64_t* launches, FlSegs segs) {
   const int n = t->n, m = n - 1;
   const int g = (m + kThreads - 1) / kThreads, g2 = (2 * n - 1 + kThreads - 1) / kThreads;
   uint32_t* ctot = static_cast<uint32_t*>(t->scan_scratch);
@@ -1071,7 +1251,7 @@ void fl_launch_aggregate(const FlTreeBufs* t, const uint64_t* skeys, bool closed
     k_cells_closed<<<g, kThreads, 0, st>>>(n, t->ndim, sign, t->range, t->depth, t->count,
                                            reinterpret_cast<const D4*>(t->wsum),
                                            reinterpret_cast<const D4*>(t->wtiles), t->leaf, cube,
-                                           fx_exp, t->cell);
+                                           fx_exp, t->cell, segs);
     ++*launches;
   } else {
     cudaMemsetAsync(t->flag, 0, 4 * (size_t)m, st);
@@ -1080,20 +1260,20 @@ void fl_launch_aggregate(const FlTreeBufs* t, const uint64_t* skeys, bool closed
         t->flag, t->cell, t->leaf, fp64_depth, err);
     ++*launches;
   }
-  k_slots<<<g2, kThreads, 0, st>>>(n, t->ndim, t->head_of, t->omask, t->range, t->depth,
-                                   t->count, t->first, ctot, t->cell, t->leaf, t->child_data,
-                                   t->child_meta, err);
+  k_slots<<<g2, kThreads, 0, st>>>(n, t->ndim, t->head_of, t->omask, t->parent, t->range,
+                                   t->depth, t->count, t->first, ctot, t->cell, t->leaf,
+                                   t->child_data, t->child_meta, err, segs);
   ++*launches;
 }
 
 // Blocks of this walk variant resident on one SM (queried once), at most kWalkBlocksPerSm.
-template <int NDIM, int G, bool STATS, bool DMAX>
+template <int NDIM, int G, bool STATS, bool DMAX, bool BATCH>
 int walk_blocks_per_sm() {
   static int blocks = 0;
   if (!blocks) {
     int b = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_walk<NDIM, G, STATS, DMAX>, kWalkThreads, 0) !=
-            cudaSuccess || b < 1)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_walk<NDIM, G, STATS, DMAX, BATCH>,
+                                                      kWalkThreads, 0) != cudaSuccess || b < 1)
       b = 1;
     blocks = b < kWalkBlocksPerSm ? b : kWalkBlocksPerSm;
   }
@@ -1103,7 +1283,7 @@ int walk_blocks_per_sm() {
 void fl_launch_walk(const FlTreeBufs* t, const uint32_t* perm, const float* cube, float4* vel,
                     float alpha, double theta2, double dmin2, double dmax2, uint32_t step,
                     uint32_t seed, uint32_t* err, unsigned long long* stats, int group,
-                    cudaStream_t st) {
+                    cudaStream_t st, FlSegs segs) {
   const int n = t->n;
   const int warps = (n + 31) / 32;
   // a persistent grid of the blocks that fit on the device at once (and that the spill buffer
@@ -1111,22 +1291,32 @@ void fl_launch_walk(const FlTreeBufs* t, const uint32_t* perm, const float* cube
   const int cap = t->walk_slots / kWalkWarps;
   cudaMemsetAsync(t->work, 0, 4, st);
   const float fmax2 = dmax2 > 3e38 ? INFINITY : (float)dmax2;
-#define FL_WALK_ONE(D, G, S, M)                                                                \
+#define FL_WALK_ONE(D, G, S, M, B)                                                             \
   do {                                                                                         \
-    int g = t->sms * walk_blocks_per_sm<D, G, S, M>();                                         \
+    int g = t->sms * walk_blocks_per_sm<D, G, S, M, B>();                                      \
     if (g > cap) g = cap;                                                                      \
     if (g < 1) g = 1;                                                                          \
-    k_walk<D, G, S, M><<<g, kWalkThreads, 0, st>>>(                                            \
+    k_walk<D, G, S, M, B><<<g, kWalkThreads, 0, st>>>(                                         \
         t->child_data, t->child_meta, t->leaf, perm, cube, vel, n, alpha, theta2,              \
-        (float)dmin2, fmax2, step, seed, err, stats, t->spill, warps, t->work);                \
+        (float)dmin2, fmax2, step, seed, err, stats, t->spill, warps, t->work, segs);          \
   } while (0)
 #define FL_WALK(D, G)                                                                          \
   do {                                                                                         \
-    if (stats) FL_WALK_ONE(D, G, true, true);                                                  \
-    else if (fmax2 < INFINITY) FL_WALK_ONE(D, G, false, true);                                 \
-    else FL_WALK_ONE(D, G, false, false);                                                      \
+    if (stats) FL_WALK_ONE(D, G, true, true, false);                                           \
+    else if (fmax2 < INFINITY) FL_WALK_ONE(D, G, false, true, false);                          \
+    else FL_WALK_ONE(D, G, false, false, false);                                               \
   } while (0)
-  if (group == 32) {
+  // a batch: distanceMax per graph (the walk tests it when any graph has a finite one)
+#define FL_WALK_BATCH(D)                                                                       \
+  do {                                                                                         \
+    if (fmax2 < INFINITY) FL_WALK_ONE(D, 32, false, true, true);                               \
+    else FL_WALK_ONE(D, 32, false, false, true);                                               \
+  } while (0)
+  if (segs.graphs) {
+    if (t->ndim == 3) FL_WALK_BATCH(3);
+    else if (t->ndim == 2) FL_WALK_BATCH(2);
+    else FL_WALK_BATCH(1);
+  } else if (group == 32) {
     if (t->ndim == 3) FL_WALK(3, 32);
     else if (t->ndim == 2) FL_WALK(2, 32);
     else FL_WALK(1, 32);
@@ -1136,6 +1326,7 @@ void fl_launch_walk(const FlTreeBufs* t, const uint32_t* perm, const float* cube
     else FL_WALK(1, 16);
   }
 #undef FL_WALK
+#undef FL_WALK_BATCH
 #undef FL_WALK_ONE
 }
 
@@ -1149,4 +1340,33 @@ void fl_launch_allpairs(const float4* pos, const float* strength, float4* vel, i
   const int g = (n + per - 1) / per;
   k_allpairs<<<g < 1 ? 1 : g, kPairThreads, 0, st>>>(pos, strength, vel, n, ndim, alpha, dmin2,
                                                      dmax2, step, seed, split);
+}
+
+void fl_launch_bgraph(int graphs, int ndim, const int32_t* off, const FlReduce* red,
+                      const FlBatchParams* prm, const double* alpha, FlGraph* gr, cudaStream_t st) {
+  k_bgraph<<<(graphs + kThreads - 1) / kThreads, kThreads, 0, st>>>(graphs, ndim, off, red, prm,
+                                                                    alpha, gr);
+}
+
+void fl_launch_bmorton(const float4* pos, int n, int ndim, const uint32_t* gid, const FlGraph* gr,
+                       uint64_t* keys, uint32_t* vals, uint32_t* hist, int lo_bit, cudaStream_t st) {
+  int g = (n + kThreads - 1) / kThreads;
+  if (g > 2 * 152) g = 2 * 152;
+  if (g < 1) g = 1;
+  k_bmorton<<<g, kThreads, 0, st>>>(pos, n, ndim, gid, gr, keys, vals, hist, lo_bit);
+}
+
+void fl_launch_bgidkey(int n, const uint32_t* mperm, const uint32_t* gid, uint64_t* keys,
+                       uint32_t* vals, uint32_t* hist, cudaStream_t st) {
+  int g = (n + kThreads - 1) / kThreads;
+  if (g > 2 * 152) g = 2 * 152;
+  if (g < 1) g = 1;
+  k_bgidkey<<<g, kThreads, 0, st>>>(n, mperm, gid, keys, vals, hist);
+}
+
+void fl_launch_bgather(int n, const uint32_t* order2, const uint64_t* mkeys, const uint32_t* mperm,
+                       const uint32_t* gid, uint64_t* skeys, uint32_t* perm, uint32_t* gid_pos,
+                       cudaStream_t st) {
+  k_bgather<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(n, order2, mkeys, mperm, gid,
+                                                                 skeys, perm, gid_pos);
 }

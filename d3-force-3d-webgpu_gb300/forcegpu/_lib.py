@@ -25,7 +25,9 @@ EXPORTS = ["fl_create", "fl_destroy", "fl_last_error", "fl_fits", "fl_set_nodes"
            "fl_update_positions", "fl_update_pins", "fl_update_velocities", "fl_set_forces",
            "fl_set_seed", "fl_enqueue", "fl_sync", "fl_idle", "fl_busy", "fl_buffers",
            "fl_stream", "fl_query", "fl_profile", "fl_profile_read", "fl_radix_sort",
-           "fl_debug_tree", "fl_set_tuning", "fl_radix_sort_noalloc"]
+           "fl_debug_tree", "fl_set_tuning", "fl_radix_sort_noalloc", "fl_batch_create",
+           "fl_batch_destroy", "fl_batch_last_error", "fl_batch_set_graphs", "fl_batch_set_seed",
+           "fl_batch_enqueue", "fl_batch_sync", "fl_batch_query", "fl_batch_stream"]
 SORT_NOALLOC_MAX_PAIRS = 262144  # FL_SORT_NOALLOC_MAX_PAIRS
 TUNE_WALK_GROUP, TUNE_CELL_SUMS = 1, 2
 CELLS_AUTO, CELLS_FP64_TOP, CELLS_FP32 = 0, 1, 2
@@ -51,6 +53,21 @@ class ForceDesc(ctypes.Structure):
         ("distance_min2", ctypes.c_double), ("distance_max2", ctypes.c_double),
         ("theta2", ctypes.c_double), ("strength", ctypes.c_double),
         ("x", ctypes.c_double), ("y", ctypes.c_double), ("z", ctypes.c_double),
+    ]
+
+
+class GraphDesc(ctypes.Structure):
+    """fl_graph_desc: one graph of a batch."""
+    _fields_ = [
+        ("n", ctypes.c_int32), ("m", ctypes.c_int32),
+        ("pos4", ctypes.c_void_p), ("vel4", ctypes.c_void_p),
+        ("source", ctypes.c_void_p), ("target", ctypes.c_void_p),
+        ("link_distance", ctypes.c_void_p), ("link_strength", ctypes.c_void_p),
+        ("link_bias", ctypes.c_void_p), ("charge", ctypes.c_void_p),
+        ("theta2", ctypes.c_double), ("distance_min2", ctypes.c_double),
+        ("distance_max2", ctypes.c_double),
+        ("center_x", ctypes.c_double), ("center_y", ctypes.c_double), ("center_z", ctypes.c_double),
+        ("center_strength", ctypes.c_double), ("velocity_decay", ctypes.c_double),
     ]
 
 
@@ -95,6 +112,15 @@ def load():
         "fl_debug_tree": (I32, [P, I32, P, P, P, P, P, P]),
         "fl_set_tuning": (I32, [P, I32, I32]),
         "fl_radix_sort_noalloc": (I32, [P, P, I64, I32, P, P, P]),
+        "fl_batch_create": (I32, [I32, ctypes.POINTER(P)]),
+        "fl_batch_destroy": (I32, [P]),
+        "fl_batch_last_error": (ctypes.c_char_p, [P]),
+        "fl_batch_set_graphs": (I32, [P, I32, I32, ctypes.POINTER(GraphDesc)]),
+        "fl_batch_set_seed": (I32, [P, U32]),
+        "fl_batch_enqueue": (I32, [P, P, I32]),
+        "fl_batch_sync": (I32, [P, P, P]),
+        "fl_batch_query": (I32, [P, I32, ctypes.POINTER(I64)]),
+        "fl_batch_stream": (I32, [P, ctypes.POINTER(P)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -168,6 +168,45 @@ int32_t fl_profile(fl_sim* sim, int32_t enable);
 int32_t fl_profile_read(fl_sim* sim, int32_t cap, const char** names, double* ms,
                         int64_t* launches, int32_t* count);
 
+/* ---- batches: many independent layouts advanced together ----
+ * No counterpart in the reference, which runs one simulation per engine (src/gpu/engine.js:73);
+ * its closest relatives are the per-device engine sharing of src/gpu/device.js:4 and the
+ * step batching of src/gpu/engine.js:7-9, :362-389. A batch holds G graphs, each with a link
+ * force, a many-body force and an optional centre force (the forces of the reference's
+ * benchmark), all in one dimensionality; every kernel of a tick runs once for the whole batch.
+ * Each graph has its own alpha schedule, theta, distances, centre and velocity decay. */
+typedef struct fl_graph_desc {
+  int32_t n;                 /* nodes */
+  int32_t m;                 /* links */
+  const float* pos4;         /* [4n] start positions (x, y, z, -) */
+  const float* vel4;         /* [4n] start velocities, or NULL (0) */
+  const int32_t* source;     /* [m] link ends, node indices within this graph */
+  const int32_t* target;     /* [m] */
+  const float* link_distance; /* [m] or NULL: 30 (src/link.js:19) */
+  const float* link_strength; /* [m] or NULL: 1 / min(count(source), count(target)) (src/link.js:36-38) */
+  const float* link_bias;     /* [m] or NULL: count(source) / (count(source) + count(target)) (src/link.js:73-75) */
+  const float* charge;       /* [n] many-body strengths, or NULL (-30) */
+  double theta2, distance_min2, distance_max2;  /* many-body (d3 defaults 0.81, 1, inf) */
+  double center_x, center_y, center_z, center_strength; /* centre force; strength 0: none */
+  double velocity_decay;     /* d3's velocityDecay (0.4 default) */
+} fl_graph_desc;
+
+typedef struct fl_batch fl_batch;
+int32_t fl_batch_create(int32_t device, fl_batch** out);
+int32_t fl_batch_destroy(fl_batch* b);
+const char* fl_batch_last_error(const fl_batch* b);
+/* Replace the batch's graphs (copied; the state starts from pos4 / vel4). */
+int32_t fl_batch_set_graphs(fl_batch* b, int32_t ndim, int32_t graphs, const fl_graph_desc* descs);
+int32_t fl_batch_set_seed(fl_batch* b, uint32_t seed);
+/* Queue `ticks` ticks without waiting; alphas[k * graphs + g] is graph g's alpha at tick k. */
+int32_t fl_batch_enqueue(fl_batch* b, const double* alphas, int32_t ticks);
+/* Wait, then copy the concatenated positions / velocities (4 floats per node; either may be
+ * NULL). Reports a device-side error raised since the previous sync. */
+int32_t fl_batch_sync(fl_batch* b, float* pos4_out, float* vel4_out);
+/* FL_Q_LAUNCHES, FL_Q_TICKS, FL_Q_NODES, FL_Q_DEVICE_BYTES */
+int32_t fl_batch_query(fl_batch* b, int32_t what, int64_t* out);
+int32_t fl_batch_stream(fl_batch* b, void** stream);
+
 /* ---- integer stages, exposed for bit-exact checks against a CPU rebuild ---- */
 
 /* Stable LSD radix sort of n (key, value) pairs on key bits [lo_bit, 64), the engine's sort on

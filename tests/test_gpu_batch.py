@@ -1,0 +1,111 @@
+"""Batches of graphs (fl_batch_*): every graph of a batch against the oracle run on that graph
+alone, and a graph alone against the same graph in a mix.
+
+The batch's forces are link (applied as the reference's GPU does: all links against one
+snapshot, the oracle's Jacobi mode), many-body by d3's tree and centre, with d3's defaults."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from forcegpu import FlError
+from forcegpu.batch import Batch, GraphSpec
+from forcegpu.graphs import benchmark_links, make_nodes
+from gpu_helpers import tree_outliers
+
+pytestmark = pytest.mark.gpu
+
+
+def spec(n, dims, seed, **kw):
+    xyz = make_nodes(n, dims, 200.0 + n, seed)[:, :dims]
+    src, dst = benchmark_links(n, n // 3, seed=seed)
+    return GraphSpec(xyz=xyz, source=src, target=dst, **kw)
+
+
+def oracle_run(s, dims, ticks):
+    """The reference's CPU simulation of one graph (Jacobi links, as the GPU)."""
+    n = len(s.xyz)
+    xyz = np.zeros((n, 3))
+    xyz[:, :dims] = s.xyz
+    o = oracle.OracleSim(n, dims, xyz=xyz)
+    o.set_params(alphaDecay=s.alpha_decay, velocityDecay=s.velocity_decay)
+    if len(s.source):
+        o.link(s.source, s.target, mode=oracle.MODE_JACOBI)
+    o.manybody(theta=s.theta, distanceMin=s.distance_min, distanceMax=s.distance_max)
+    if s.center_strength:
+        o.center(*s.center, strength=s.center_strength)
+    o.tick(ticks)
+    return o.state()[0][:, :dims]
+
+
+def assert_close(got, want, rtol, outliers):
+    tol = 1e-3 + rtol * np.maximum(1.0, np.maximum(np.abs(got), np.abs(want)))
+    bad = np.any(np.abs(got - want) > tol, axis=1)
+    assert np.isfinite(got).all()
+    assert bad.sum() <= outliers, "%d nodes off (%d allowed), worst %g" % (
+        bad.sum(), outliers, (np.abs(got - want) / tol).max())
+
+
+@pytest.mark.parametrize("dims", [2, 3])
+def test_every_graph_of_a_batch_matches_the_oracle(dims):
+    sizes = [1, 2, 3, 40, 257, 1500, 31, 700]
+    specs = [spec(n, dims, 100 + i) for i, n in enumerate(sizes)]
+    specs[3].alpha_decay = 0.05                     # a graph with its own schedule
+    specs[4].theta, specs[4].distance_max = 0.6, 150.0
+    specs[5].center, specs[5].center_strength = (10.0, -5.0, 3.0), 0.5
+    specs[6].velocity_decay = 0.2
+    b = Batch()
+    b.set_graphs(specs, ndim=dims, seed=7)
+    ticks = 3
+    b.run(ticks)
+    got = b.positions()
+    for s, p in zip(specs, got):
+        want = oracle_run(s, dims, ticks)
+        assert_close(p, want, 1e-3, tree_outliers(len(p)))
+
+
+def test_a_graph_alone_and_in_a_mix_agree():
+    """The same graph laid out alone and among others: its result does not depend on the rest
+    of the batch (the continuous-batching property a server relies on)."""
+    me = spec(900, 3, 5)
+    others = [spec(n, 3, 20 + i) for i, n in enumerate([300, 2, 1200, 77])]
+    alone = Batch()
+    alone.set_graphs([me], ndim=3, seed=3)
+    alone.run(20)
+    a = alone.positions()[0]
+    mix = Batch()
+    mix.set_graphs(others[:2] + [me] + others[2:], ndim=3, seed=3)
+    mix.run(20)
+    m = mix.positions()[2]
+    # the same tree, interactions and forces; only the order of some float sums may differ
+    assert_close(m, a, 1e-4, tree_outliers(900))
+
+
+def test_graphs_with_finished_schedules_and_many_ticks_stay_finite():
+    specs = [spec(n, 3, 50 + n) for n in (5, 60, 600)]
+    b = Batch()
+    b.set_graphs(specs, ndim=3)
+    b.run(300)
+    for p in b.positions():
+        assert np.isfinite(p).all()
+        assert np.abs(p).max() < 1e5
+
+
+def test_a_bad_link_is_refused():
+    s = spec(10, 3, 1)
+    s.target = s.target.copy()
+    s.target[0] = 10
+    b = Batch()
+    with pytest.raises(FlError):
+        b.set_graphs([s], ndim=3)
+
+
+def test_the_batch_counts_its_launches_per_tick_independent_of_graphs():
+    one, many = Batch(), Batch()
+    one.set_graphs([spec(500, 3, 9)], ndim=3)
+    many.set_graphs([spec(500, 3, 9 + i) for i in range(64)], ndim=3)
+    one.run(2)
+    many.run(2)
+    one.sync(), many.sync()
+    assert one.launches() == many.launches(), "one launch per kernel per tick, whatever the batch"
