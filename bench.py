@@ -74,6 +74,10 @@ def parse():
     p.add_argument("--graphs", type=int, default=2048)
     p.add_argument("--serial-sample", type=int, default=48,
                    help="graphs laid out one at a time on the plain engine, for the comparison")
+    p.add_argument("--served", action="store_true",
+                   help="print the served-layout line (Poisson arrivals, continuous batching)")
+    p.add_argument("--jobs", type=int, default=100)
+    p.add_argument("--rate", type=float, default=50.0, help="job arrivals per second")
     return p.parse_args()
 
 
@@ -377,8 +381,88 @@ def run_batched(args):
     b.close()
 
 
+def served_jobs(count, rate, seed=77):
+    """The served configuration: Poisson arrivals at `rate` jobs/s; each job a 2D or 3D graph
+    (50/50), size log-uniform in [500, 200000], the reference benchmark's link generator at 1 to
+    3 links per node (uniform), link + charge + center, and in 30 % of jobs also collide with
+    radii uniform in [1, 5]; tick count uniform in [100, 500]."""
+    from forcegpu.graphs import benchmark_links, phyllotaxis
+    from forcegpu.serve import Job
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, count))
+    jobs = []
+    for i in range(count):
+        n = int(np.exp(rng.uniform(np.log(500), np.log(200_000))))
+        dims = 2 if rng.random() < 0.5 else 3
+        per = rng.uniform(1.0, 3.0)
+        src, dst = benchmark_links(n, max(0, int(n * per) - (n - 1)), seed=5000 + i)
+        radii = rng.uniform(1.0, 5.0, n) if rng.random() < 0.3 else None
+        jobs.append(Job(xyz=phyllotaxis(n, dims)[:, :dims], source=src, target=dst,
+                        ticks=int(rng.integers(100, 501)), radii=radii, arrival=float(t[i])))
+    return jobs
+
+
+def run_served(args):
+    """--served: the layout server under Poisson arrivals (continuous batching), and the same
+    jobs solved one at a time on the plain engine, first come first served."""
+    import copy
+    from forcegpu.serve import LayoutServer, latency_summary
+    jobs = served_jobs(args.jobs, args.rate)
+    work = copy.deepcopy(jobs)
+    # the server, in real time: arrivals are offsets from the start
+    srv = LayoutServer(hbm_budget=96 << 30, block=50)
+    clocks = Clocks()
+    clocks.start()
+    t0 = time.perf_counter()
+    for j in work:
+        j.arrival = t0 + j.arrival
+        srv.submit(j)
+    srv.run_until_idle()
+    makespan = time.perf_counter() - t0
+    clk = clocks.stop()
+    srv.close()
+    assert all(j.result is not None and np.isfinite(j.result).all() for j in work)
+    served = latency_summary(work)
+    # serial plain solves, FIFO under the same arrivals: each job's service time measured alone
+    serial = copy.deepcopy(jobs)
+    one = LayoutServer(hbm_budget=96 << 30, block=50, batching=False)
+    service = []
+    for j in serial:
+        j.arrival = None
+        one.submit(j)
+        s0 = time.perf_counter()
+        one.run_until_idle()
+        service.append(time.perf_counter() - s0)
+    one.close()
+    finish, lat = 0.0, []
+    for j, sv in zip(jobs, service):
+        finish = max(finish, j.arrival) + sv
+        lat.append(finish - j.arrival)
+    lat = np.array(lat)
+    node_ticks = sum(j.n * j.ticks for j in jobs)
+    line = {"metric": "served layouts/s and p99 latency (continuous batching)",
+            "value": len(jobs) / makespan, "unit": "layouts/s", "n_gpus": 1, "steps": len(jobs),
+            "warmup": 0, "ms_per_step": 1e3 * makespan / len(jobs), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "%d jobs, Poisson arrivals at %g/s, 2D/3D 50/50, sizes "
+                                   "log-uniform [500, 200000], 1-3 links/node, 30%% collide, "
+                                   "ticks uniform [100, 500]" % (len(jobs), args.rate),
+                       "node_ticks": int(node_ticks)},
+            "latency": served,
+            "serial_plain": {"layouts_per_s": len(jobs) / max(finish - jobs[0].arrival, 1e-9),
+                             "p50_s": float(np.percentile(lat, 50)),
+                             "p99_s": float(np.percentile(lat, 99)),
+                             "busy_seconds": float(sum(service))},
+            "clocks": clk}
+    line["speedup_vs_serial_plain"] = line["value"] / line["serial_plain"]["layouts_per_s"]
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.served:
+        run_served(args)
+        return
     if args.impl == "reference":
         run_reference(args)
         return

@@ -16,7 +16,8 @@ struct FlGraph {
   float alpha, decay;     // this tick's alpha; velocity multiplier
   float2 shift[3];        // the centre force's shift per axis (hi + lo), 0 without one
   int32_t first, count;   // nodes [first, first + count)
-  float pad[2];
+  int32_t frozen;         // 1: the graph sits this tick out (its alpha was given as negative)
+  float pad;
 };
 // A batch of independent graphs, concatenated: graph g owns nodes [off[g], off[g+1]) and, after
 // the tree's sort (by graph, then Morton code), the same range of sorted positions. Kernels

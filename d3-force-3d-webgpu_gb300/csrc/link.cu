@@ -59,7 +59,11 @@ __global__ void __launch_bounds__(kThreads) k_link(const float4* __restrict__ po
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const bool live = i < n;
-  if (gr && live) alpha = gr[gid[i]].alpha;  // a batch: the node's graph's alpha
+  bool frozen = false;
+  if (gr && live) {  // a batch: the node's graph's alpha; a graph sitting the tick out keeps v
+    const FlGraph& g = gr[gid[i]];
+    alpha = g.alpha, frozen = g.frozen != 0;
+  }
   int r0 = 0, r1 = 0;
   float4 p = make_float4(0, 0, 0, 0), v = p;
   if (live) {
@@ -68,8 +72,8 @@ __global__ void __launch_bounds__(kThreads) k_link(const float4* __restrict__ po
   }
   const float3 me = make_float3(p.x + v.x, p.y + v.y, p.z + v.z);
   float3 acc = make_float3(0.f, 0.f, 0.f);
-  const bool longrow = (r1 - r0) > kLong;
-  if (!longrow)
+  const bool longrow = !frozen && (r1 - r0) > kLong;
+  if (!longrow && !frozen)
     for (int e = r0; e < r1; ++e) link_term(pos, vel_in, me, __ldg(entry + e), __ldg(code + e), ndim, alpha, step, seed, acc);
   // long rows: the warp takes them one at a time
   uint32_t longs = __ballot_sync(FL_FULL, longrow);

@@ -167,6 +167,7 @@ __global__ void __launch_bounds__(kThreads) k_integrate(float4* __restrict__ pos
   float4 p = pos[i], v = vel[i];
   if (gr) {  // a batch: the node's graph's decay and centre shift
     const FlGraph& g = gr[gid[i]];
+    if (g.frozen) return;  // sitting this tick out: state unchanged
     decay = g.decay;
     sh[0] = g.shift[0], sh[1] = g.shift[1], sh[2] = g.shift[2];
   }

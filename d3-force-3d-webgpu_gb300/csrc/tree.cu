@@ -227,7 +227,8 @@ __global__ void __launch_bounds__(kThreads) k_bgraph(int graphs, int ndim, const
     o.shift[k] = make_float2(h, (float)(d - (double)h));
   }
   o.first = first, o.count = count;
-  o.pad[0] = o.pad[1] = 0.f;
+  o.frozen = alpha[g] < 0.0 ? 1 : 0;
+  o.pad = 0.f;
   gr[g] = o;
 }
 
@@ -899,7 +900,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
     if (live) {
       const FlGraph& gr = segs.g[g];
       myT0 = gr.T0, mydmin2 = gr.dmin2, mydmax2 = gr.dmax2;
-      tree = gr.count > 1;
+      tree = gr.count > 1 && !gr.frozen;
     }
     const uint32_t peers = __match_any_sync(FL_FULL, tree ? g : 0xffffffffu) & gmask;
     const bool leader = tree && (peers & (lanebit - 1u)) == 0;

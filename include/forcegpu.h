@@ -198,7 +198,9 @@ const char* fl_batch_last_error(const fl_batch* b);
 /* Replace the batch's graphs (copied; the state starts from pos4 / vel4). */
 int32_t fl_batch_set_graphs(fl_batch* b, int32_t ndim, int32_t graphs, const fl_graph_desc* descs);
 int32_t fl_batch_set_seed(fl_batch* b, uint32_t seed);
-/* Queue `ticks` ticks without waiting; alphas[k * graphs + g] is graph g's alpha at tick k. */
+/* Queue `ticks` ticks without waiting; alphas[k * graphs + g] is graph g's alpha at tick k. A
+ * negative alpha makes graph g sit tick k out: its positions and velocities do not change (a
+ * graph whose layout is finished while others in the batch go on). */
 int32_t fl_batch_enqueue(fl_batch* b, const double* alphas, int32_t ticks);
 /* Wait, then copy the concatenated positions / velocities (4 floats per node; either may be
  * NULL). Reports a device-side error raised since the previous sync. */

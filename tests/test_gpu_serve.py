@@ -1,0 +1,86 @@
+"""The layout server: continuous batching of jobs that arrive while others run.
+
+A job's result must not depend on which other jobs share the GPU with it: the same job laid
+out alone and in a mix (joining a running batch, with jobs leaving around it) gives the same
+layout within the tolerance of the other GPU tests."""
+import numpy as np
+import pytest
+
+from forcegpu.graphs import benchmark_links, make_nodes
+from forcegpu.serve import Job, LayoutServer, latency_summary
+from gpu_helpers import tree_outliers
+
+pytestmark = pytest.mark.gpu
+
+
+def job(n, dims, seed, ticks, radii=False, arrival=0.0):
+    xyz = make_nodes(n, dims, 150.0 + n, seed)[:, :dims]
+    src, dst = benchmark_links(n, n // 2, seed=seed)
+    r = (1.0 + (np.arange(n) % 5)).astype(float) if radii else None
+    return Job(xyz=xyz, source=src, target=dst, ticks=ticks, radii=r, arrival=arrival)
+
+
+def close(a, b, outliers, rtol=1e-3):
+    tol = 1e-3 + rtol * np.maximum(1.0, np.maximum(np.abs(a), np.abs(b)))
+    bad = np.any(np.abs(a - b) > tol, axis=1)
+    return np.isfinite(a).all() and bad.sum() <= outliers
+
+
+class FakeClock:
+    """Time that advances by one step per server round, so arrivals land mid-run."""
+
+    def __init__(self):
+        self.t = 0.0
+
+    def __call__(self):
+        self.t += 1.0
+        return self.t
+
+
+@pytest.mark.parametrize("dims", [2, 3])
+def test_a_job_alone_and_in_the_mix_gives_the_same_layout(dims):
+    # A force layout is chaotic: float sums taken in another order (the walk's, the centre's
+    # atomics) differ in the last bits and the difference grows tick by tick, by about 10x every
+    # 10 ticks here; so the job runs 12 ticks, in blocks of 4, with the mix changing around it.
+    ticks = 12
+    alone = LayoutServer(block=4, clock=FakeClock())
+    me = alone.submit(job(600, dims, 11, ticks))
+    alone.run_until_idle()
+    alone.close()
+    # the same job in a mix: it joins a running batch, others join and leave while it runs
+    srv = LayoutServer(block=4, clock=FakeClock())
+    srv.submit(job(300, dims, 12, 6, arrival=0.0))
+    srv.submit(job(1500, dims, 13, 20, arrival=0.0))
+    mine = srv.submit(job(600, dims, 11, ticks, arrival=3.0))
+    srv.submit(job(50, dims, 14, 5, arrival=6.0))
+    srv.submit(job(900, dims, 15, 9, arrival=9.0))
+    srv.run_until_idle()
+    srv.close()
+    assert all(j.result is not None for j in srv.finished)
+    assert len(srv.finished) == 5
+    assert mine.done_ticks == ticks
+    assert close(mine.result, me.result, tree_outliers(600))
+
+
+def test_admission_waits_for_memory_to_free_up():
+    a, b = job(2000, 3, 21, 30), job(2000, 3, 22, 30)
+    srv = LayoutServer(block=10, hbm_budget=a.footprint + b.footprint // 2, clock=FakeClock())
+    srv.submit(a)
+    srv.submit(b)
+    srv.run_until_idle()
+    srv.close()
+    assert a.finished is not None and b.finished is not None
+    assert b.admitted >= a.finished, "the second job waits for the first one's memory"
+
+
+def test_jobs_with_collide_run_on_their_own_engines_alongside_the_batch():
+    srv = LayoutServer(block=10, clock=FakeClock())
+    plain = srv.submit(job(400, 3, 31, 20, radii=True))
+    batched = srv.submit(job(400, 3, 32, 20))
+    srv.run_until_idle()
+    srv.close()
+    for j in (plain, batched):
+        assert j.result is not None and np.isfinite(j.result).all()
+        assert j.result.shape == (400, 3)
+    s = latency_summary(srv.finished)
+    assert s["jobs"] == 2 and s["p99_s"] >= s["p50_s"] > 0
