@@ -77,6 +77,9 @@ def parse():
     p.add_argument("--served", action="store_true",
                    help="print the served-layout line (Poisson arrivals, continuous batching)")
     p.add_argument("--jobs", type=int, default=100)
+    p.add_argument("--config2", action="store_true",
+                   help="print the 100k-node line (link+charge+center+collide+radial, pins) with "
+                        "per-force errors against the oracle")
     p.add_argument("--rate", type=float, default=50.0, help="job arrivals per second")
     return p.parse_args()
 
@@ -458,8 +461,111 @@ def run_served(args):
     print(json.dumps(line), flush=True)
 
 
+def run_config2(args):
+    """--config2: 100,000 nodes in 3D, the benchmark's link generator, link + charge (theta 0.9)
+    + center + collide (radius uniform in [1, 5], 1 iteration, grid path) + radial (r 200,
+    strength 0.05), every 10th node pinned at its start; 300 ticks timed. Then, from the state
+    after those ticks, each force's velocity change on 4,096 random nodes against the oracle
+    (link and collide in their Jacobi form, as the GPU applies them) and, for the many-body
+    force, against the FP64 exact sum."""
+    import torch
+    import oracle
+    from forcegpu import Engine
+    from forcegpu._lib import desc_from_gpu
+    n, ticks = 100_000, 300
+    xyz, src, dst, bias, strength = workload(n)
+    rng = np.random.default_rng(4)
+    radii = rng.uniform(1.0, 5.0, n).astype(np.float32).astype(np.float64)
+    pos4 = np.zeros((n, 4), np.float32)
+    pos4[:, :3] = xyz
+    fix4 = pos4.copy()
+    mask = np.where(np.arange(n) % 10 == 0, 7, 0).astype(np.uint32)
+    g = {
+        "link": {"type": "link", "version": 1, "source": src, "target": dst, "iterations": 1,
+                 "strengths": strength, "distances": np.full(len(src), 30.0), "bias": bias},
+        "charge": {"type": "manyBody", "version": 1, "strengths": np.full(n, -30.0),
+                   "distanceMin2": 1.0, "distanceMax2": math.inf, "theta2": 0.81},
+        "center": {"type": "center", "x": 0, "y": 0, "z": 0, "strength": 1.0},
+        "collide": {"type": "collide", "version": 1, "radii": radii, "strength": 1.0, "iterations": 1},
+        "radial": {"type": "radial", "version": 1, "radiuses": np.full(n, 200.0),
+                   "strengths": np.full(n, 0.05), "x": 0, "y": 0, "z": 0},
+    }
+    names = ["link", "charge", "center", "collide", "radial"]
+    eng = Engine(0)
+    eng.set_nodes(pos4, 3, None, fix4, mask)
+    eng.set_forces([desc_from_gpu(g[k], i + 1, n) for i, k in enumerate(names)])
+    eng.set_seed(12345)
+    al, _ = alphas(ticks + args.warmup + 1)
+    eng.enqueue(al[:args.warmup], 0.6)
+    eng.idle()
+    stream = torch.cuda.ExternalStream(eng.stream(), device=0)
+    eng.profile(True)
+    clocks = Clocks()
+    clocks.start()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    eng.enqueue(al[args.warmup:args.warmup + ticks], 0.6)
+    e1.record(stream)
+    pos, vel = eng.sync()
+    clk = clocks.stop()
+    prof = eng.profile_read()
+    eng.profile(False)
+    eng.close()
+    ms = e0.elapsed_time(e1) / ticks
+    alpha = float(al[args.warmup + ticks])
+    targets = np.sort(rng.choice(n, 4096, replace=False)).astype(np.int32)
+    p64, v64 = pos[:, :3].astype(np.float64), vel[:, :3].astype(np.float64)
+
+    def gpu_dv(name):
+        e = Engine(0)
+        e.set_nodes(pos, 3, vel)
+        e.set_forces([desc_from_gpu(g[name], 1, n)])
+        e.set_seed(777)
+        e.enqueue(np.array([alpha]), 1.0)
+        _, v2 = e.sync()
+        e.close()
+        return (v2[:, :3].astype(np.float64) - v64)[targets]
+
+    def cpu_dv(add, probe_mode=None):
+        o = oracle.OracleSim(n, 3, xyz=p64, vxyz=v64)
+        add(o)
+        if probe_mode is not None:
+            return o.manybody_probe(0, alpha, targets, probe_mode, threads=os.cpu_count() or 1)
+        o.apply_force(0, alpha)
+        return (o.state()[1] - v64)[targets]
+
+    errors = {}
+    errors["link_vs_cpu_jacobi"] = rel_errors(
+        gpu_dv("link"), cpu_dv(lambda o: o.link(src, dst, 30.0, strength, 1, oracle.MODE_JACOBI)))
+    charge_gpu = gpu_dv("charge")
+    errors["charge_vs_cpu_barnes_hut"] = rel_errors(
+        charge_gpu, cpu_dv(lambda o: o.manybody(theta=0.9), oracle.MODE_D3))
+    errors["charge_vs_fp64_exact"] = rel_errors(
+        charge_gpu, cpu_dv(lambda o: o.manybody(theta=0.9), oracle.MODE_EXACT))
+    errors["cpu_barnes_hut_vs_fp64_exact"] = rel_errors(
+        cpu_dv(lambda o: o.manybody(theta=0.9), oracle.MODE_D3),
+        cpu_dv(lambda o: o.manybody(theta=0.9), oracle.MODE_EXACT))
+    errors["collide_vs_cpu_jacobi"] = rel_errors(
+        gpu_dv("collide"), cpu_dv(lambda o: o.collide(radii, 1.0, 1, oracle.MODE_JACOBI)))
+    errors["radial_vs_cpu"] = rel_errors(
+        gpu_dv("radial"), cpu_dv(lambda o: o.radial(np.full(n, 200.0), 0.05)))
+    line = {"metric": "ms/tick at 100k nodes (3D link+charge+center+collide+radial, pins)",
+            "value": ms, "unit": "ms/tick", "n_gpus": 1, "steps": ticks, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "100,000 nodes, 149,999 links, collide r U[1,5] (grid), radial "
+                                   "r 200 s 0.05, every 10th node pinned, 300 ticks", "nodes": n},
+            "kernels": {k: {"ms_per_tick": v[0] / ticks, "launches": v[1]} for k, v in prof.items()},
+            "force_errors_4096_targets": errors, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.config2:
+        run_config2(args)
+        return
     if args.served:
         run_served(args)
         return

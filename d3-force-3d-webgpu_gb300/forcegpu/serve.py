@@ -207,25 +207,32 @@ class LayoutServer:
                                            "iterations": 1}, 3, n))
         eng.set_forces(descs)
         eng.set_seed(self.seed)
-        eng.enqueue(j.next_alphas(j.ticks), 1 - j.velocity_decay)
         self.plain.append((j, eng, descs))
 
     def step(self):
-        """One round: admit, launch a block on every batch, land finished plain jobs, land the
-        batches' blocks. Returns the jobs finished in this round."""
+        """One round: admit; launch a block on every batch and queue the next block of ticks of
+        every plain job (a block at a time, so that no queue of thousands of launches holds the
+        host while the batches wait); land the finished plain jobs and the batches' blocks.
+        Returns the jobs finished in this round."""
         self._admit()
         for lane in self.lanes.values():
             lane.launch(self.block, self.seed)
+        for j, eng, _ in self.plain:
+            k = min(self.block, j.ticks - j.done_ticks)
+            if k > 0:
+                al = j.next_alphas(k)
+                eng.enqueue(al, 1 - j.velocity_decay)
+                j.alpha = float(al[-1])
+                j.done_ticks += k
         done = []
         still = []
         for j, eng, descs in self.plain:
-            if eng.busy():
+            if j.done_ticks < j.ticks or eng.busy():
                 still.append((j, eng, descs))
                 continue
             pos, _ = eng.sync()
             eng.close()
             j.result = pos[:, :j.ndim].copy()
-            j.done_ticks = j.ticks
             j.finished = self.now()
             done.append(j)
         self.plain = still
@@ -239,8 +246,9 @@ class LayoutServer:
             wait = self.queue[0].arrival - self.now()
             if wait > 0:
                 time.sleep(min(wait, 0.05))
-        elif not any(l.jobs for l in self.lanes.values()) and self.plain:
-            time.sleep(0.0005)  # only plain engines running: poll gently
+        elif not any(l.jobs for l in self.lanes.values()) and self.plain and \
+                all(j.done_ticks >= j.ticks for j, _, _ in self.plain):
+            time.sleep(0.0005)  # only queued plain work left: poll gently
         return done
 
     def run_until_idle(self):
