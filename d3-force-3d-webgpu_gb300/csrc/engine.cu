@@ -97,6 +97,10 @@ enum {
 struct fl_sim {
   int32_t device = 0;
   cudaStream_t st = nullptr;
+  // a second stream for the many-body tree's construction, which depends on the positions only
+  // and so overlaps with the forces before it; joined before the walk
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_tree = nullptr;
   std::string err;
   int32_t n = 0, ndim = 2;
   DevMem pos, vel[2], fix, mask, red, errw;
@@ -152,17 +156,18 @@ cudaEvent_t take_event(fl_sim* s) {
 struct Scope {
   fl_sim* s;
   int group;
+  cudaStream_t st;
   cudaEvent_t a = nullptr;
-  Scope(fl_sim* s_, int g) : s(s_), group(g) {
+  Scope(fl_sim* s_, int g, cudaStream_t st_ = nullptr) : s(s_), group(g), st(st_ ? st_ : s_->st) {
     if (s->profiling) {
       a = take_event(s);
-      cudaEventRecord(a, s->st);
+      cudaEventRecord(a, st);
     }
   }
   ~Scope() {
     if (a) {
       cudaEvent_t b = take_event(s);
-      cudaEventRecord(b, s->st);
+      cudaEventRecord(b, st);
       s->prof_pending.push_back({group, a, b});
     }
   }
@@ -326,7 +331,51 @@ bool is_tree(const Pass* p) {
 
 // ---------------------------------------------------------------- the tick
 
-void encode_manybody(fl_sim* s, Pass* p, float alpha, const FlReduce* box) {
+// The many-body tree of pass p from the current positions (box: their bounding box, or null to
+// reduce it here), on stream st.
+void encode_tree(fl_sim* s, Pass* p, const FlReduce* box, cudaStream_t st) {
+  const int n = s->n;
+  FlTreeBufs* t = &p->tb;
+  const float* strength = p->a.as<float>();
+  const int lo_bit = 64 - t->bits;
+  if (!box) {
+    Scope sc(s, G_REDUCE, st);
+    cudaMemsetAsync(p->red.p, 0, sizeof(FlReduce), st);
+    fl_launch_reduce(s->pos.as<float4>(), n, s->ndim, 1, 0, p->red.as<FlReduce>(), st);
+    ++s->launches;
+    box = p->red.as<FlReduce>();
+  }
+  {
+    Scope sc(s, G_MORTON, st);
+    fl_sort_reset(&p->sb, n, (64 - lo_bit + 7) / 8, st);
+    fl_launch_morton(s->pos.as<float4>(), n, s->ndim, box, p->sb.keys[0], p->sb.vals[0],
+                     p->sb.hist, lo_bit, p->cube.as<float>(), st);
+    ++s->launches;
+  }
+  int r;
+  {
+    Scope sc(s, G_SORT, st);
+    r = fl_sort_passes(&p->sb, n, lo_bit, s->errw.as<uint32_t>(), st, &s->launches);
+    p->sorted_in = r;
+  }
+  // the closed form (exact fixed-point sums) when the strengths share one sign, unless a
+  // recursion was asked for
+  const bool closed = !p->mixed && s->cell_sums == FL_CELLS_AUTO;
+  {
+    Scope sc(s, G_BUILD, st);
+    fl_launch_build(t, p->sb.keys[r], p->sb.vals[r], s->pos.as<float4>(), strength, closed,
+                    p->cube.as<float>(), p->fx_exp, st, &s->launches);
+  }
+  {
+    Scope sc(s, G_AGGREGATE, st);
+    fl_launch_aggregate(t, p->sb.keys[r], closed, p->sign, p->cube.as<float>(), p->fx_exp,
+                        s->cell_sums == FL_CELLS_FP32 ? 0 : kRecursionFp64Depth,
+                        s->errw.as<uint32_t>(), st, &s->launches);
+  }
+}
+
+// The many-body force of pass p: its tree (unless built already, on the side stream) and walk.
+void encode_manybody(fl_sim* s, Pass* p, float alpha, const FlReduce* box, bool built) {
   const int n = s->n;
   if (n < 2) return;  // a lone node feels nothing
   const float* strength = p->a.as<float>();
@@ -338,46 +387,12 @@ void encode_manybody(fl_sim* s, Pass* p, float alpha, const FlReduce* box) {
     ++s->launches;
     return;
   }
-  FlTreeBufs* t = &p->tb;
-  const int lo_bit = 64 - t->bits;
-  if (!box) {
-    Scope sc(s, G_REDUCE);
-    cudaMemsetAsync(p->red.p, 0, sizeof(FlReduce), s->st);
-    fl_launch_reduce(s->pos.as<float4>(), n, s->ndim, 1, 0, p->red.as<FlReduce>(), s->st);
-    ++s->launches;
-    box = p->red.as<FlReduce>();
-  }
-  {
-    Scope sc(s, G_MORTON);
-    fl_sort_reset(&p->sb, n, (64 - lo_bit + 7) / 8, s->st);
-    fl_launch_morton(s->pos.as<float4>(), n, s->ndim, box, p->sb.keys[0], p->sb.vals[0],
-                     p->sb.hist, lo_bit, p->cube.as<float>(), s->st);
-    ++s->launches;
-  }
-  int r;
-  {
-    Scope sc(s, G_SORT);
-    r = fl_sort_passes(&p->sb, n, lo_bit, s->errw.as<uint32_t>(), s->st, &s->launches);
-    p->sorted_in = r;
-  }
-  // the closed form (exact fixed-point sums) when the strengths share one sign, unless a
-  // recursion was asked for
-  const bool closed = !p->mixed && s->cell_sums == FL_CELLS_AUTO;
-  {
-    Scope sc(s, G_BUILD);
-    fl_launch_build(t, p->sb.keys[r], p->sb.vals[r], s->pos.as<float4>(), strength, closed,
-                    p->cube.as<float>(), p->fx_exp, s->st, &s->launches);
-  }
-  {
-    Scope sc(s, G_AGGREGATE);
-    fl_launch_aggregate(t, p->sb.keys[r], closed, p->sign, p->cube.as<float>(), p->fx_exp,
-                        s->cell_sums == FL_CELLS_FP32 ? 0 : kRecursionFp64Depth,
-                        s->errw.as<uint32_t>(), s->st, &s->launches);
-  }
+  if (built) cudaStreamWaitEvent(s->st, s->ev_tree, 0);
+  else encode_tree(s, p, box, s->st);
   {
     Scope sc(s, G_WALK);
-    fl_launch_walk(t, p->sb.vals[r], p->cube.as<float>(), vel_cur(s), alpha, p->d.theta2,
-                   p->d.distance_min2, p->d.distance_max2, s->step, s->seed,
+    fl_launch_walk(&p->tb, p->sb.vals[p->sorted_in], p->cube.as<float>(), vel_cur(s), alpha,
+                   p->d.theta2, p->d.distance_min2, p->d.distance_max2, s->step, s->seed,
                    s->errw.as<uint32_t>(),
                    s->prof_level >= 2 ? s->wstats.as<unsigned long long>() : nullptr,
                    s->walk_group, s->st);
@@ -445,12 +460,30 @@ void encode_tick(fl_sim* s, float alpha, float decay) {
                      s->red.as<FlReduce>(), s->st);
     ++s->launches;
   }
+  // the first tree before any centre force is built from the tick's starting positions, which
+  // nothing changes until then: on the side stream, overlapping with the forces before it
+  int early = -1;
+  if (tree_at_start && s->aux)
+    for (int k = 0; k < np; ++k) {
+      if (plan[k]->type == FL_FORCE_CENTER) break;
+      if (is_tree(plan[k].get())) {
+        early = k;
+        break;
+      }
+    }
+  if (early >= 0) {
+    cudaEventRecord(s->ev_fork, s->st);
+    cudaStreamWaitEvent(s->aux, s->ev_fork, 0);
+    encode_tree(s, plan[early].get(), s->red.as<FlReduce>(), s->aux);
+    cudaEventRecord(s->ev_tree, s->aux);
+  }
   bool before_center = true;
   for (int k = 0; k < np; ++k) {
     Pass* p = plan[k].get();
     switch (p->type) {
       case FL_FORCE_MANYBODY:
-        encode_manybody(s, p, alpha, before_center && tree_at_start ? s->red.as<FlReduce>() : nullptr);
+        encode_manybody(s, p, alpha, before_center && tree_at_start ? s->red.as<FlReduce>() : nullptr,
+                        k == early);
         break;
       case FL_FORCE_LINK:
         if (p->m == 0) break;
@@ -552,6 +585,13 @@ int32_t fl_create(int32_t device, fl_sim** out) {
   if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaSetDevice");
   e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
   if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaStreamCreate");
+  if (cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&s->ev_tree, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();  // no side stream: every pass runs on the main one
+    if (s->aux) cudaStreamDestroy(s->aux);
+    s->aux = nullptr;
+  }
   if ((e = s->red.alloc(sizeof(FlReduce))) != cudaSuccess) return cuda_fail(nullptr, e, "cudaMalloc");
   if ((e = s->errw.alloc(256)) != cudaSuccess) return cuda_fail(nullptr, e, "cudaMalloc");
   if ((e = cudaMemset(s->errw.p, 0, 256)) != cudaSuccess) return cuda_fail(nullptr, e, "cudaMemset");
@@ -565,10 +605,14 @@ int32_t fl_destroy(fl_sim* s) {
   cudaStreamSynchronize(s->st);
   for (auto& r : s->prof_pending) cudaEventDestroy(r.a), cudaEventDestroy(r.b);
   for (auto e : s->ev_pool) cudaEventDestroy(e);
+  if (s->aux) cudaStreamSynchronize(s->aux);
   s->plan.clear();
-  cudaStream_t st = s->st;
+  cudaStream_t st = s->st, aux = s->aux;
+  if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+  if (s->ev_tree) cudaEventDestroy(s->ev_tree);
   delete s;  // frees the device buffers
   if (st) cudaStreamDestroy(st);
+  if (aux) cudaStreamDestroy(aux);
   return FL_OK;
 }
 
