@@ -65,6 +65,19 @@ struct fl_batch {
   float sign = -1.f;
   double dmax_any = INFINITY;  // finite when some graph has a finite distanceMax
   int64_t ticks = 0, launches = 0;
+  // per-tick steps in device memory and the CUDA graphs of tick blocks, as fl_sim's
+  Buf tickbuf;
+  int32_t tick_cap = 0;
+  std::vector<FlTick> htick;
+  struct Block {
+    int32_t count;
+    int cur_in, cur_out;
+    int64_t launches;
+    bool captured;
+    cudaGraphExec_t exec;
+  };
+  std::vector<Block> blocks;
+  bool use_graphs = true;
 };
 
 namespace {
@@ -94,8 +107,15 @@ int32_t bcheck(fl_batch* b) {
 
 float4* bvel(fl_batch* b) { return b->vel[b->cur].as<float4>(); }
 
-// One tick of the batch: alphas of this tick are at `alpha` (device, one per graph).
-void encode_batch_tick(fl_batch* b, const double* alpha) {
+void clear_blocks(fl_batch* b) {
+  for (auto& x : b->blocks)
+    if (x.captured) cudaGraphExecDestroy(x.exec);
+  b->blocks.clear();
+}
+
+// One tick of the batch: alphas of this tick are at `alpha` (device, one per graph), its step
+// and seed at tk (device).
+void encode_batch_tick(fl_batch* b, const double* alpha, const FlTick* tk) {
   const int n = b->n, G = b->graphs;
   cudaStream_t st = b->st;
   uint32_t* err = b->errw.as<uint32_t>();
@@ -111,17 +131,19 @@ void encode_batch_tick(fl_batch* b, const double* alpha) {
   if (b->m > 0) {
     FlLinkCsr csr{b->row.as<int32_t>(), b->entry.as<float4>(), b->code.as<uint32_t>()};
     fl_launch_link(b->pos.as<float4>(), bvel(b), b->vel[1 - b->cur].as<float4>(), csr, n, b->ndim,
-                   0.f, b->step, b->seed, st, gr, gid);
+                   0.f, b->step, b->seed, st, gr, gid, tk);
     b->cur = 1 - b->cur;
     ++b->launches;
   }
   // many-body: sort by Morton code, then (stably) by graph; one tree per graph
   if (n >= 2) {
     const int bits = (b->ndim == 3 ? 21 : 24) * b->ndim, lo_bit = 64 - bits;
-    fl_sort_reset(&b->sb, n, (64 - lo_bit + 7) / 8, st);
+    const int lo_sort = fl_sort_split(lo_bit);
+    fl_sort_reset(&b->sb, n, (64 - lo_sort + 7) / 8, st);
     fl_launch_bmorton(b->pos.as<float4>(), n, b->ndim, gid, gr, b->sb.keys[0], b->sb.vals[0],
-                      b->sb.hist, lo_bit, st);
-    const int r = fl_sort_passes(&b->sb, n, lo_bit, err, st, &b->launches);
+                      b->sb.hist, lo_sort, st);
+    int r = fl_sort_passes(&b->sb, n, lo_sort, err, st, &b->launches);
+    r = fl_sort_runfix(&b->sb, n, lo_bit, lo_sort, r, st, &b->launches);
     fl_sort_reset(&b->sb2, n, 2, st);
     fl_launch_bgidkey(n, b->sb.vals[r], gid, b->sb2.keys[0], b->sb2.vals[0], b->sb2.hist, st);
     const int r2 = fl_sort_passes(&b->sb2, n, 48, err, st, &b->launches);
@@ -136,15 +158,13 @@ void encode_batch_tick(fl_batch* b, const double* alpha) {
     fl_launch_aggregate(&b->tb, skeys, b->closed, b->sign, nullptr, b->fx_exp, 6, err, st,
                         &b->launches, segs);
     fl_launch_walk(&b->tb, perm, nullptr, bvel(b), 0.f, 1.0, 0.0, b->dmax_any, b->step, b->seed,
-                   err, nullptr, 32, st, segs);
+                   err, nullptr, 32, st, segs, tk);
     ++b->launches;
   }
   // centre shift (per graph) and integration
   fl_launch_integrate(b->pos.as<float4>(), bvel(b), b->fix.as<float4>(), b->mask.as<uint32_t>(),
                       n, b->ndim, 1.f, nullptr, 0, 0, 0, 0, st, gr, gid);
   ++b->launches;
-  ++b->step;
-  ++b->ticks;
 }
 
 }  // namespace
@@ -177,6 +197,7 @@ int32_t fl_batch_destroy(fl_batch* b) {
   if (!b) return FL_OK;
   cudaSetDevice(b->device);
   cudaStreamSynchronize(b->st);
+  clear_blocks(b);
   cudaStreamDestroy(b->st);
   delete b;
   return FL_OK;
@@ -190,6 +211,7 @@ int32_t fl_batch_set_graphs(fl_batch* b, int32_t ndim, int32_t graphs, const fl_
   if (ndim < 1 || ndim > 3) return bfail(b, FL_E_ARG, "ndim must be 1, 2 or 3");
   if (graphs < 1 || graphs > 65535 || !d) return bfail(b, FL_E_ARG, "graphs must be 1..65535");
   FB_CK(b, cudaStreamSynchronize(b->st));
+  clear_blocks(b);
   int64_t n = 0, m = 0;
   for (int32_t g = 0; g < graphs; ++g) {
     if (d[g].n < 0 || d[g].m < 0 || (d[g].n && !d[g].pos4) || (d[g].m && (!d[g].source || !d[g].target)))
@@ -334,15 +356,75 @@ int32_t fl_batch_enqueue(fl_batch* b, const double* alphas, int32_t ticks) {
   if (ticks < 0 || (ticks && !alphas)) return bfail(b, FL_E_ARG, "bad alphas");
   if (!ticks) return FL_OK;
   const size_t need = (size_t)ticks * (size_t)b->graphs;
-  if (need > b->alpha_cap) {
+  if (need > b->alpha_cap || ticks > b->tick_cap) {
     FB_CK(b, cudaStreamSynchronize(b->st));
-    FB_CK(b, b->alphas.alloc(8 * need));
-    b->alpha_cap = need;
+    clear_blocks(b);  // captured blocks point into the old buffers
+    if (need > b->alpha_cap) {
+      FB_CK(b, b->alphas.alloc(8 * need));
+      b->alpha_cap = need;
+    }
+    if (ticks > b->tick_cap) {
+      FB_CK(b, b->tickbuf.alloc(sizeof(FlTick) * (size_t)ticks));
+      b->tick_cap = ticks;
+    }
   }
-  // copied on the stream, so after every tick already queued has read the previous alphas
+  // copied on the stream, so after every tick already queued has read the previous values
   FB_CK(b, cudaMemcpyAsync(b->alphas.p, alphas, 8 * need, cudaMemcpyHostToDevice, b->st));
-  for (int32_t k = 0; k < ticks; ++k)
-    encode_batch_tick(b, b->alphas.as<double>() + (size_t)k * b->graphs);
+  b->htick.resize(ticks);
+  for (int32_t k = 0; k < ticks; ++k) b->htick[k] = FlTick{0.f, 1.f, b->step + (uint32_t)k, b->seed};
+  FB_CK(b, cudaMemcpyAsync(b->tickbuf.p, b->htick.data(), sizeof(FlTick) * (size_t)ticks,
+                           cudaMemcpyHostToDevice, b->st));
+  auto encode = [&]() {
+    for (int32_t k = 0; k < ticks; ++k)
+      encode_batch_tick(b, b->alphas.as<double>() + (size_t)k * b->graphs, b->tickbuf.as<FlTick>() + k);
+  };
+  // a block of ticks seen before runs as one CUDA graph (captured the second time)
+  fl_batch::Block* x = nullptr;
+  if (b->use_graphs)
+    for (auto& y : b->blocks)
+      if (y.count == ticks && y.cur_in == b->cur) x = &y;
+  if (x && x->captured) {
+    FB_CK(b, cudaGraphLaunch(x->exec, b->st));
+    b->cur = x->cur_out;
+    b->launches += x->launches;
+  } else if (x) {
+    const int cur0 = b->cur;
+    const int64_t l0 = b->launches;
+    cudaGraph_t g = nullptr;
+    bool ok = cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+      encode();
+      ok = cudaStreamEndCapture(b->st, &g) == cudaSuccess && g;
+    }
+    if (ok) {
+      ok = cudaGraphInstantiate(&x->exec, g, 0) == cudaSuccess;
+      cudaGraphDestroy(g);
+    }
+    if (ok) {
+      x->captured = true;
+      FB_CK(b, cudaGraphLaunch(x->exec, b->st));
+    } else {
+      cudaGetLastError();
+      if (g) cudaGraphDestroy(g);
+      b->use_graphs = false;
+      b->cur = cur0;
+      b->launches = l0;
+      encode();
+    }
+  } else {
+    const int cur0 = b->cur;
+    const int64_t l0 = b->launches;
+    encode();
+    if (b->use_graphs) {
+      if (b->blocks.size() >= 8) {
+        if (b->blocks.front().captured) cudaGraphExecDestroy(b->blocks.front().exec);
+        b->blocks.erase(b->blocks.begin());
+      }
+      b->blocks.push_back(fl_batch::Block{ticks, cur0, b->cur, b->launches - l0, false, nullptr});
+    }
+  }
+  b->step += (uint32_t)ticks;
+  b->ticks += ticks;
   FB_CK(b, cudaGetLastError());
   return FL_OK;
 }

@@ -43,7 +43,8 @@ __device__ __forceinline__ void pair_push(float3 me, float ri2, float ri, float4
 __global__ void __launch_bounds__(kThreads) k_collide_allpairs(
     const float4* __restrict__ pos, const float4* __restrict__ vel_in, float4* __restrict__ vel_out,
     const float* __restrict__ radius, int n, int ndim, float strength, uint32_t step,
-    uint32_t seed, int split) {
+    uint32_t seed, int split, const FlTick* __restrict__ tk) {
+  if (tk) step = tk->step, seed = tk->seed;
   __shared__ float4 tile[kThreads];
   __shared__ float3 part[kThreads];
   const int per = kThreads / split;
@@ -166,7 +167,8 @@ __global__ void __launch_bounds__(kThreads) k_grid_query(
     const uint64_t* __restrict__ skeys, const uint32_t* __restrict__ perm,
     const uint32_t* __restrict__ starts, const float4* __restrict__ sorted,
     const float4* __restrict__ vel_in, float4* __restrict__ vel_out, int n, int ndim, int bits,
-    float inv, float strength, uint32_t step, uint32_t seed) {
+    float inv, float strength, uint32_t step, uint32_t seed, const FlTick* __restrict__ tk) {
+  if (tk) step = tk->step, seed = tk->seed;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   const float4 me4 = sorted[s];
@@ -206,13 +208,13 @@ __global__ void __launch_bounds__(kThreads) k_grid_query(
 
 void fl_launch_collide_allpairs(const float4* pos, const float4* vel_in, float4* vel_out,
                                 const float* radius, int n, int ndim, float strength,
-                                uint32_t step, uint32_t seed, cudaStream_t st) {
+                                uint32_t step, uint32_t seed, cudaStream_t st, const FlTick* tk) {
   int split = 1;
   while (split < 16 && (int64_t)n * split < (1 << 18)) split *= 2;
   const int per = kThreads / split;
   const int g = (n + per - 1) / per;
   k_collide_allpairs<<<g < 1 ? 1 : g, kThreads, 0, st>>>(pos, vel_in, vel_out, radius, n, ndim,
-                                                         strength, step, seed, split);
+                                                         strength, step, seed, split, tk);
 }
 
 size_t fl_grid_bytes(int64_t n) {
@@ -242,11 +244,12 @@ void fl_launch_grid_keys(const float4* pos, const float4* vel, int n, int ndim, 
 void fl_launch_grid_query(const FlGridBufs* g, const uint64_t* skeys, const uint32_t* perm,
                           const float4* pos, const float4* vel_in, float4* vel_out,
                           const float* radius, int ndim, float inv_cell, float strength,
-                          uint32_t step, uint32_t seed, cudaStream_t st, int64_t* launches) {
+                          uint32_t step, uint32_t seed, cudaStream_t st, int64_t* launches,
+                          const FlTick* tk) {
   const int n = g->n, blocks = (n + kThreads - 1) / kThreads;
   k_grid_begin<<<blocks, kThreads, 0, st>>>(skeys, perm, pos, vel_in, radius, n, g->bits, g->starts,
                                             g->sorted);
   k_grid_query<<<blocks, kThreads, 0, st>>>(skeys, perm, g->starts, g->sorted, vel_in, vel_out, n,
-                                            ndim, g->bits, inv_cell, strength, step, seed);
+                                            ndim, g->bits, inv_cell, strength, step, seed, tk);
   *launches += 2;
 }

@@ -109,6 +109,21 @@ struct fl_sim {
   uint32_t seed = 0, step = 0;
   int64_t ticks = 0, launches = 0;
   int walk_group = 32;  // points per tree-walk traversal (tuning: 16 or 32)
+  // per-tick values in device memory and the CUDA graphs of tick blocks (fl_enqueue)
+  const FlTick* tkp = nullptr;  // the tick being encoded (null: parameters)
+  DevMem tickbuf;
+  int32_t tick_cap = 0;
+  std::vector<FlTick> htick;
+  struct Block {
+    int32_t count;
+    int cur_in, cur_out;
+    int64_t launches;
+    bool captured;
+    cudaGraphExec_t exec;
+  };
+  std::vector<Block> blocks;
+  std::vector<double> plan_sig;
+  bool use_graphs = true;
   int cell_sums = 0;    // tuning FL_TUNE_CELL_SUMS
   bool profiling = false;
   int prof_level = 0;
@@ -337,7 +352,7 @@ void encode_tree(fl_sim* s, Pass* p, const FlReduce* box, cudaStream_t st) {
   const int n = s->n;
   FlTreeBufs* t = &p->tb;
   const float* strength = p->a.as<float>();
-  const int lo_bit = 64 - t->bits;
+  const int lo_bit = 64 - t->bits, lo_sort = fl_sort_split(lo_bit);
   if (!box) {
     Scope sc(s, G_REDUCE, st);
     cudaMemsetAsync(p->red.p, 0, sizeof(FlReduce), st);
@@ -347,15 +362,16 @@ void encode_tree(fl_sim* s, Pass* p, const FlReduce* box, cudaStream_t st) {
   }
   {
     Scope sc(s, G_MORTON, st);
-    fl_sort_reset(&p->sb, n, (64 - lo_bit + 7) / 8, st);
+    fl_sort_reset(&p->sb, n, (64 - lo_sort + 7) / 8, st);
     fl_launch_morton(s->pos.as<float4>(), n, s->ndim, box, p->sb.keys[0], p->sb.vals[0],
-                     p->sb.hist, lo_bit, p->cube.as<float>(), st);
+                     p->sb.hist, lo_sort, p->cube.as<float>(), st);
     ++s->launches;
   }
   int r;
   {
     Scope sc(s, G_SORT, st);
-    r = fl_sort_passes(&p->sb, n, lo_bit, s->errw.as<uint32_t>(), st, &s->launches);
+    r = fl_sort_passes(&p->sb, n, lo_sort, s->errw.as<uint32_t>(), st, &s->launches);
+    r = fl_sort_runfix(&p->sb, n, lo_bit, lo_sort, r, st, &s->launches);
     p->sorted_in = r;
   }
   // the closed form (exact fixed-point sums) when the strengths share one sign, unless a
@@ -383,7 +399,7 @@ void encode_manybody(fl_sim* s, Pass* p, float alpha, const FlReduce* box, bool 
     Scope sc(s, G_ALLPAIRS);
     const float dmax2 = p->d.distance_max2 > 3e38 ? INFINITY : (float)p->d.distance_max2;
     fl_launch_allpairs(s->pos.as<float4>(), strength, vel_cur(s), n, s->ndim, alpha,
-                       (float)p->d.distance_min2, dmax2, s->step, s->seed, s->st);
+                       (float)p->d.distance_min2, dmax2, s->step, s->seed, s->st, s->tkp);
     ++s->launches;
     return;
   }
@@ -395,7 +411,7 @@ void encode_manybody(fl_sim* s, Pass* p, float alpha, const FlReduce* box, bool 
                    p->d.theta2, p->d.distance_min2, p->d.distance_max2, s->step, s->seed,
                    s->errw.as<uint32_t>(),
                    s->prof_level >= 2 ? s->wstats.as<unsigned long long>() : nullptr,
-                   s->walk_group, s->st);
+                   s->walk_group, s->st, FlSegs{}, s->tkp);
     ++s->launches;
   }
 }
@@ -408,7 +424,7 @@ void encode_collide(fl_sim* s, Pass* p) {
     if (n < kGridMin) {
       Scope sc(s, G_CALLPAIRS);
       fl_launch_collide_allpairs(s->pos.as<float4>(), vel_cur(s), vel_next(s), p->a.as<float>(),
-                                 n, s->ndim, strength, s->step, s->seed, s->st);
+                                 n, s->ndim, strength, s->step, s->seed, s->st, s->tkp);
       ++s->launches;
     } else {
       FlGridBufs* g = &p->gb;
@@ -430,7 +446,7 @@ void encode_collide(fl_sim* s, Pass* p) {
         Scope sc(s, G_CQUERY);
         fl_launch_grid_query(g, p->sb.keys[r], p->sb.vals[r], s->pos.as<float4>(), vel_cur(s),
                              vel_next(s), p->a.as<float>(), s->ndim, inv, strength, s->step,
-                             s->seed, s->st, &s->launches);
+                             s->seed, s->st, &s->launches, s->tkp);
       }
     }
     s->cur = 1 - s->cur;
@@ -491,7 +507,7 @@ void encode_tick(fl_sim* s, float alpha, float decay) {
           Scope sc(s, G_LINK);
           FlLinkCsr csr{p->row.as<int32_t>(), p->entry.as<float4>(), p->code.as<uint32_t>()};
           fl_launch_link(s->pos.as<float4>(), vel_cur(s), vel_next(s), csr, n, s->ndim, alpha,
-                         s->step, s->seed, s->st);
+                         s->step, s->seed, s->st, nullptr, nullptr, s->tkp);
           ++s->launches;
           s->cur = 1 - s->cur;
         }
@@ -514,7 +530,7 @@ void encode_tick(fl_sim* s, float alpha, float decay) {
       case FL_FORCE_RADIAL: {
         Scope sc(s, G_RADIAL);
         fl_launch_radial(s->pos.as<float4>(), vel_cur(s), p->a.as<float>(), p->b.as<float>(), n,
-                         s->ndim, (float)p->d.x, (float)p->d.y, (float)p->d.z, alpha, s->st);
+                         s->ndim, (float)p->d.x, (float)p->d.y, (float)p->d.z, alpha, s->st, s->tkp);
         ++s->launches;
         break;
       }
@@ -523,7 +539,7 @@ void encode_tick(fl_sim* s, float alpha, float decay) {
         {
           Scope sc(s, G_POSITION);
           fl_launch_position(s->pos.as<float4>(), vel_cur(s), p->a.as<float>(), p->b.as<float>(),
-                             n, p->d.axis, alpha, s->st);
+                             n, p->d.axis, alpha, s->st, s->tkp);
           ++s->launches;
         }
         break;
@@ -535,11 +551,31 @@ void encode_tick(fl_sim* s, float alpha, float decay) {
     fl_launch_integrate(s->pos.as<float4>(), vel_cur(s), s->fix.as<float4>(),
                         s->mask.as<uint32_t>(), n, s->ndim, decay,
                         c ? s->red.as<FlReduce>() : nullptr, c ? c->d.x : 0, c ? c->d.y : 0,
-                        c ? c->d.z : 0, c ? c->d.strength : 0, s->st);
+                        c ? c->d.z : 0, c ? c->d.strength : 0, s->st, nullptr, nullptr, s->tkp);
     ++s->launches;
   }
-  ++s->step;
-  ++s->ticks;
+}
+
+// Captured tick blocks depend on the passes' buffers and scalars: forget them on any change.
+void clear_blocks(fl_sim* s) {
+  for (auto& b : s->blocks)
+    if (b.captured) cudaGraphExecDestroy(b.exec);
+  s->blocks.clear();
+}
+
+// What a captured block bakes in: every pass's identity, version, scalars and buffers.
+std::vector<double> plan_signature(const fl_sim* s) {
+  std::vector<double> v;
+  for (auto& p : s->plan) {
+    const fl_force_desc& d = p->d;
+    const double f[] = {(double)p->type, (double)p->key, (double)p->version, (double)d.iterations,
+                        (double)d.axis, d.distance_min2, d.distance_max2, d.theta2, d.strength,
+                        d.x, d.y, d.z, (double)p->m, (double)p->rmax, (double)p->alloc_n,
+                        (double)(uintptr_t)p->a.p, (double)(uintptr_t)p->b.p,
+                        (double)(uintptr_t)p->row.p, (double)(uintptr_t)p->scratch.p};
+    v.insert(v.end(), f, f + sizeof f / sizeof f[0]);
+  }
+  return v;
 }
 
 int32_t check_sim(fl_sim* s) {
@@ -606,6 +642,7 @@ int32_t fl_destroy(fl_sim* s) {
   for (auto& r : s->prof_pending) cudaEventDestroy(r.a), cudaEventDestroy(r.b);
   for (auto e : s->ev_pool) cudaEventDestroy(e);
   if (s->aux) cudaStreamSynchronize(s->aux);
+  clear_blocks(s);
   s->plan.clear();
   cudaStream_t st = s->st, aux = s->aux;
   if (s->ev_fork) cudaEventDestroy(s->ev_fork);
@@ -635,6 +672,7 @@ int32_t fl_set_nodes(fl_sim* s, int32_t n, int32_t ndim, const float* pos4, cons
   int32_t rc = check_sim(s);
   if (rc) return rc;
   if (n < 0 || n > kMaxNodes) return fail(s, FL_E_ARG, "node count out of range");
+  clear_blocks(s);
   if (n > 0 && !pos4) return fail(s, FL_E_ARG, "positions are NULL");
   FL_CK(s, cudaStreamSynchronize(s->st));
   s->plan.clear();
@@ -707,7 +745,15 @@ int32_t fl_set_forces(fl_sim* s, int32_t count, const fl_force_desc* descs) {
     if (descs[i].type < FL_FORCE_MANYBODY || descs[i].type > FL_FORCE_POSITION)
       return fail(s, FL_E_UNSUPPORTED, "force " + std::to_string(i) + " (type " +
                                            std::to_string(descs[i].type) + ") has no GPU pass");
-  FL_CK(s, cudaStreamSynchronize(s->st));  // passes may be replaced below
+  // the same passes with the same per-node arrays: only scalars change, nothing in flight is
+  // touched, so no wait is needed; otherwise passes may be replaced below
+  bool same = count == (int32_t)s->plan.size();
+  for (int32_t i = 0; same && i < count; ++i) {
+    const Pass* p = s->plan[i].get();
+    same = p->key == descs[i].key && p->type == descs[i].type && !p->fresh &&
+           p->version == descs[i].version;
+  }
+  if (!same) FL_CK(s, cudaStreamSynchronize(s->st));
   std::vector<std::unique_ptr<Pass>> old = std::move(s->plan);
   std::vector<std::unique_ptr<Pass>> next;
   for (int32_t i = 0; i < count; ++i) {
@@ -730,6 +776,11 @@ int32_t fl_set_forces(fl_sim* s, int32_t count, const fl_force_desc* descs) {
     next.push_back(std::move(p));
   }
   s->plan = std::move(next);
+  std::vector<double> sig = plan_signature(s);
+  if (sig != s->plan_sig) {
+    clear_blocks(s);
+    s->plan_sig = std::move(sig);
+  }
   return FL_OK;
 }
 
@@ -744,8 +795,75 @@ int32_t fl_enqueue(fl_sim* s, const double* alphas, int32_t count, double decay)
   int32_t rc = check_sim(s);
   if (rc) return rc;
   if (count < 0 || (count && !alphas)) return fail(s, FL_E_ARG, "bad alphas");
-  if (s->n == 0) return FL_OK;
-  for (int32_t k = 0; k < count; ++k) encode_tick(s, (float)alphas[k], (float)decay);
+  if (s->n == 0 || count == 0) return FL_OK;
+  // the ticks' alphas, steps and seed, copied on the stream (after every tick already queued)
+  if (count > s->tick_cap) {
+    FL_CK(s, cudaStreamSynchronize(s->st));
+    clear_blocks(s);  // captured blocks point into the old buffer
+    FL_CK(s, s->tickbuf.alloc(sizeof(FlTick) * (size_t)count));
+    s->tick_cap = count;
+  }
+  s->htick.resize(count);
+  for (int32_t k = 0; k < count; ++k)
+    s->htick[k] = FlTick{(float)alphas[k], (float)decay, s->step + (uint32_t)k, s->seed};
+  FL_CK(s, cudaMemcpyAsync(s->tickbuf.p, s->htick.data(), sizeof(FlTick) * (size_t)count,
+                           cudaMemcpyHostToDevice, s->st));
+  const FlTick* tk = s->tickbuf.as<FlTick>();
+  auto encode = [&]() {
+    for (int32_t k = 0; k < count; ++k) {
+      s->tkp = tk + k;
+      encode_tick(s, (float)alphas[k], (float)decay);
+    }
+    s->tkp = nullptr;
+  };
+  // a block of ticks seen before (same length, same velocity buffer to start from) runs as one
+  // CUDA graph: captured the second time it is seen, replayed from then on
+  fl_sim::Block* b = nullptr;
+  if (s->use_graphs && !s->profiling)
+    for (auto& x : s->blocks)
+      if (x.count == count && x.cur_in == s->cur) b = &x;
+  if (b && b->captured) {
+    FL_CK(s, cudaGraphLaunch(b->exec, s->st));
+    s->cur = b->cur_out;
+    s->launches += b->launches;
+  } else if (b) {
+    const int cur0 = s->cur;
+    const int64_t l0 = s->launches;
+    cudaGraph_t g = nullptr;
+    bool ok = cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+      encode();
+      ok = cudaStreamEndCapture(s->st, &g) == cudaSuccess && g;
+    }
+    if (ok) {
+      ok = cudaGraphInstantiate(&b->exec, g, 0) == cudaSuccess;
+      cudaGraphDestroy(g);
+    }
+    if (ok) {
+      b->captured = true;
+      FL_CK(s, cudaGraphLaunch(b->exec, s->st));
+    } else {  // graphs unavailable: launch the ticks directly from now on
+      cudaGetLastError();
+      if (g) cudaGraphDestroy(g);
+      s->use_graphs = false;
+      s->cur = cur0;
+      s->launches = l0;
+      encode();
+    }
+  } else {
+    const int cur0 = s->cur;
+    const int64_t l0 = s->launches;
+    encode();
+    if (s->use_graphs && !s->profiling) {
+      if (s->blocks.size() >= 8) {
+        if (s->blocks.front().captured) cudaGraphExecDestroy(s->blocks.front().exec);
+        s->blocks.erase(s->blocks.begin());
+      }
+      s->blocks.push_back(fl_sim::Block{count, cur0, s->cur, s->launches - l0, false, nullptr});
+    }
+  }
+  s->step += (uint32_t)count;
+  s->ticks += count;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(s, e, "kernel launch");
   return FL_OK;
@@ -795,6 +913,7 @@ int32_t fl_buffers(fl_sim* s, fl_buffer_info* out) {
 int32_t fl_set_tuning(fl_sim* s, int32_t key, int32_t value) {
   int32_t rc = check_sim(s);
   if (rc) return rc;
+  clear_blocks(s);
   switch (key) {
     case FL_TUNE_WALK_GROUP:
       if (value != 16 && value != 32) return fail(s, FL_E_ARG, "walk group must be 16 or 32");
@@ -804,6 +923,10 @@ int32_t fl_set_tuning(fl_sim* s, int32_t key, int32_t value) {
       if (value != FL_CELLS_AUTO && value != FL_CELLS_FP64_TOP && value != FL_CELLS_FP32)
         return fail(s, FL_E_ARG, "cell sums must be FL_CELLS_AUTO, FL_CELLS_FP64_TOP or FL_CELLS_FP32");
       s->cell_sums = value;
+      return FL_OK;
+    case FL_TUNE_GRAPHS:
+      if (value != 0 && value != 1) return fail(s, FL_E_ARG, "graphs must be 0 or 1");
+      s->use_graphs = value != 0;
       return FL_OK;
     default:
       return fail(s, FL_E_ARG, "unknown tuning key");

@@ -6,6 +6,14 @@
 
 #include "common.cuh"
 
+// One tick's varying values, which the kernels read from device memory when given (null: the
+// values passed as parameters), so that a CUDA graph captured for a block of ticks can be
+// replayed with the next block's alphas.
+struct FlTick {
+  float alpha, decay;
+  uint32_t step, seed;
+};
+
 // ---------------------------------------------------------------- batches of graphs
 // One graph's values for a tick of a batch (device). The first five floats have the layout of a
 // single simulation's cube record (origin x, y, z, size, log2 size).
@@ -58,10 +66,13 @@ struct FlSortBufs {
   uint32_t* vals[2];
   uint32_t* hist;      // [8][256] digit counts per pass
   uint32_t* status;    // [8][tiles][256] look-back words
-  uint32_t* counters;  // [8] tile tickets
+  uint32_t* counters;  // [kSortCounters]: tile tickets of the 8 passes, then the run fix-up's
+  uint32_t* longs;     // [longs_cap] first positions of the runs the fix-up sorts in one block
+  uint32_t longs_cap;
   int64_t cap;         // pairs the buffers hold
   int64_t tiles_cap;
 };
+constexpr int kSortCounters = 16;
 constexpr int kSortThreads = 512, kSortItems = 8;  // threads of a onesweep tile, pairs each
 constexpr int kSortTile = kSortThreads * kSortItems;  // pairs per onesweep tile
 int fl_sort_tile();  // kSortTile
@@ -75,6 +86,13 @@ void fl_sort_histogram(const FlSortBufs* b, int64_t n, int lo_bit, cudaStream_t 
 // Run the passes from keys[0]/vals[0]; returns which buffer (0/1) holds the result.
 int fl_sort_passes(const FlSortBufs* b, int64_t n, int lo_bit, uint32_t* err, cudaStream_t st,
                    int64_t* launches);
+// The tree's key sort in two steps: digit passes over the top key bits [fl_sort_split(lo_bit),
+// 64) (at least the top 32, in whole digits), then fl_sort_runfix, which puts each run of pairs
+// equal in those bits in (key, value) order: together the stable sort on [lo_bit, 64) of pairs
+// whose values start as 0, 1, 2, ... Returns the buffer holding the result.
+int fl_sort_split(int lo_bit);
+int fl_sort_runfix(const FlSortBufs* b, int64_t n, int lo_bit, int lo_sort, int cur,
+                   cudaStream_t st, int64_t* launches);
 
 // ---------------------------------------------------------------- state kernels (state.cu)
 void fl_launch_reduce(const float4* pos, int n, int ndim, int want_box, int want_sum,
@@ -87,11 +105,12 @@ void fl_launch_center_apply(float4* pos, int n, int ndim, const FlReduce* red, d
 void fl_launch_integrate(float4* pos, float4* vel, const float4* fix, const uint32_t* mask, int n,
                          int ndim, float decay, const FlReduce* red, double cx, double cy,
                          double cz, double strength, cudaStream_t st, const FlGraph* gr = nullptr,
-                         const uint32_t* gid = nullptr);
+                         const uint32_t* gid = nullptr, const FlTick* tk = nullptr);
 void fl_launch_radial(const float4* pos, float4* vel, const float* radius, const float* strength,
-                      int n, int ndim, float cx, float cy, float cz, float alpha, cudaStream_t st);
+                      int n, int ndim, float cx, float cy, float cz, float alpha, cudaStream_t st,
+                      const FlTick* tk = nullptr);
 void fl_launch_position(const float4* pos, float4* vel, const float* target, const float* strength,
-                        int n, int axis, float alpha, cudaStream_t st);
+                        int n, int axis, float alpha, cudaStream_t st, const FlTick* tk = nullptr);
 
 // ---------------------------------------------------------------- link (link.cu)
 struct FlLinkCsr {
@@ -102,7 +121,8 @@ struct FlLinkCsr {
 // In a batch (gr, gid non-null) each node's links use its graph's alpha.
 void fl_launch_link(const float4* pos, const float4* vel_in, float4* vel_out, FlLinkCsr csr, int n,
                     int ndim, float alpha, uint32_t step, uint32_t seed, cudaStream_t st,
-                    const FlGraph* gr = nullptr, const uint32_t* gid = nullptr);
+                    const FlGraph* gr = nullptr, const uint32_t* gid = nullptr,
+                    const FlTick* tk = nullptr);
 
 // ---------------------------------------------------------------- many-body (tree.cu)
 struct FlTreeBufs {
@@ -167,16 +187,17 @@ int fl_fixed_exponent(int64_t n, double wmax);
 void fl_launch_walk(const FlTreeBufs* t, const uint32_t* perm, const float* cube, float4* vel,
                     float alpha, double theta2, double dmin2, double dmax2, uint32_t step,
                     uint32_t seed, uint32_t* err, unsigned long long* stats, int group,
-                    cudaStream_t st, FlSegs segs = FlSegs{});
+                    cudaStream_t st, FlSegs segs = FlSegs{}, const FlTick* tk = nullptr);
 // Exact all-pairs sum (theta ~ 0): O(n^2), tiled through shared memory.
 void fl_launch_allpairs(const float4* pos, const float* strength, float4* vel, int n, int ndim,
                         float alpha, float dmin2, float dmax2, uint32_t step, uint32_t seed,
-                        cudaStream_t st);
+                        cudaStream_t st, const FlTick* tk = nullptr);
 
 // ---------------------------------------------------------------- collide (collide.cu)
 void fl_launch_collide_allpairs(const float4* pos, const float4* vel_in, float4* vel_out,
                                 const float* radius, int n, int ndim, float strength,
-                                uint32_t step, uint32_t seed, cudaStream_t st);
+                                uint32_t step, uint32_t seed, cudaStream_t st,
+                                const FlTick* tk = nullptr);
 struct FlGridBufs {
   int n, bits;
   uint32_t* starts;   // [2^bits] run start per slot (validated against the sorted keys)
@@ -190,4 +211,5 @@ void fl_launch_grid_keys(const float4* pos, const float4* vel, int n, int ndim, 
 void fl_launch_grid_query(const FlGridBufs* g, const uint64_t* skeys, const uint32_t* perm,
                           const float4* pos, const float4* vel_in, float4* vel_out,
                           const float* radius, int ndim, float inv_cell, float strength,
-                          uint32_t step, uint32_t seed, cudaStream_t st, int64_t* launches);
+                          uint32_t step, uint32_t seed, cudaStream_t st, int64_t* launches,
+                          const FlTick* tk = nullptr);

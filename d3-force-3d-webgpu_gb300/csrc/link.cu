@@ -55,8 +55,10 @@ __global__ void __launch_bounds__(kThreads) k_link(const float4* __restrict__ po
                                                    const uint32_t* __restrict__ code, int n,
                                                    int ndim, float alpha, uint32_t step,
                                                    uint32_t seed, const FlGraph* __restrict__ gr,
-                                                   const uint32_t* __restrict__ gid) {
+                                                   const uint32_t* __restrict__ gid,
+                                                   const FlTick* __restrict__ tk) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tk) alpha = tk->alpha, step = tk->step, seed = tk->seed;
   const int lane = threadIdx.x & 31;
   const bool live = i < n;
   bool frozen = false;
@@ -101,9 +103,9 @@ __global__ void __launch_bounds__(kThreads) k_link(const float4* __restrict__ po
 
 void fl_launch_link(const float4* pos, const float4* vel_in, float4* vel_out, FlLinkCsr csr, int n,
                     int ndim, float alpha, uint32_t step, uint32_t seed, cudaStream_t st,
-                    const FlGraph* gr, const uint32_t* gid) {
+                    const FlGraph* gr, const uint32_t* gid, const FlTick* tk) {
   int g = (n + kThreads - 1) / kThreads;
   if (g < 1) g = 1;
   k_link<<<g, kThreads, 0, st>>>(pos, vel_in, vel_out, csr.row, csr.entry, csr.code, n, ndim, alpha,
-                                 step, seed, gr, gid);
+                                 step, seed, gr, gid, tk);
 }

@@ -196,9 +196,147 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(
   }
 }
 
+// ---- the run fix-up after a sort of the top key bits only
+//
+// Onesweep passes over the key bits [lo_sort, 64) leave the pairs ordered by those bits and, among
+// equal ones, by value (the passes are stable and the values start as 0, 1, 2, ...). A run of keys
+// equal above lo_sort is then put in (key, value) order, which makes the result that of the full
+// sort on [lo_bit, 64). Such runs are rare and short for Morton keys of a layout's points: the top
+// 32 bits resolve cells of 1/1600 of the cube's side. A run of up to kRunShort pairs is ranked by
+// each of its threads counting the pairs before its own; a longer one is recorded, and the last
+// block to finish sorts each recorded run by LSD passes of its own (no wait on other blocks: the
+// last block is the one that finds every other block done).
+constexpr int kRunThreads = 256;
+constexpr int kRunShort = 1024;
+
+__device__ __forceinline__ bool pair_less(uint64_t ka, uint32_t va, uint64_t kb, uint32_t vb) {
+  return ka < kb || (ka == kb && va < vb);
+}
+
+// One CTA: a stable LSD sort of the pairs [0, L) of (ka, va) on the key bits [lo_bit, hi_bit),
+// ping-ponging with (kb, vb); the result ends in (ka, va)'s place when `in_a`, else in (kb, vb).
+__device__ void cta_sort_run(uint64_t* ka, uint32_t* va, uint64_t* kb, uint32_t* vb, int64_t L,
+                             int lo_bit, int hi_bit, uint32_t* s_cnt, uint32_t* s_w) {
+  constexpr int kW = kRunThreads / 32;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t lt = fl::lanemask_lt();
+  uint64_t* ks = ka;
+  uint32_t* vs = va;
+  uint64_t* kd = kb;
+  uint32_t* vd = vb;
+  for (int shift = lo_bit; shift < hi_bit; shift += 8) {
+    const uint32_t dmask = (1u << (hi_bit - shift < 8 ? hi_bit - shift : 8)) - 1u;
+    for (int i = tid; i < 256; i += kRunThreads) s_cnt[i] = 0;
+    __syncthreads();
+    for (int64_t i = tid; i < L; i += kRunThreads) atomicAdd(&s_cnt[(uint32_t)(ks[i] >> shift) & dmask], 1u);
+    __syncthreads();
+    if (tid == 0) {  // exclusive offsets (a fallback path: a serial scan is enough)
+      uint32_t run = 0;
+      for (int d = 0; d < 256; ++d) {
+        const uint32_t c = s_cnt[d];
+        s_cnt[d] = run;
+        run += c;
+      }
+    }
+    __syncthreads();
+    for (int64_t base = 0; base < L; base += kRunThreads) {
+      const int64_t i = base + tid;
+      const bool ok = i < L;
+      const uint64_t k = ok ? ks[i] : 0;
+      const uint32_t v = ok ? vs[i] : 0;
+      const uint32_t d = ok ? (uint32_t)(k >> shift) & dmask : 256u + (uint32_t)lane;
+      for (int j = tid; j < kW * 256; j += kRunThreads) s_w[j] = 0;
+      __syncthreads();
+      const uint32_t peers = __match_any_sync(FL_FULL, d);
+      if (ok && (peers & lt) == 0) s_w[warp * 256 + d] = __popc(peers);
+      __syncthreads();
+      if (ok) {
+        uint32_t pos = s_cnt[d] + __popc(peers & lt);
+        for (int w = 0; w < warp; ++w) pos += s_w[w * 256 + d];
+        kd[pos] = k;
+        vd[pos] = v;
+      }
+      __syncthreads();
+      for (int dd = tid; dd < 256; dd += kRunThreads) {
+        uint32_t c = 0;
+        for (int w = 0; w < kW; ++w) c += s_w[w * 256 + dd];
+        s_cnt[dd] += c;
+      }
+      __syncthreads();
+    }
+    uint64_t* tk = ks;
+    ks = kd, kd = tk;
+    uint32_t* tv = vs;
+    vs = vd, vd = tv;
+  }
+  if (ks != kb) {  // the result must end in (kb, vb)
+    for (int64_t i = tid; i < L; i += kRunThreads) kb[i] = ks[i], vb[i] = vs[i];
+    __syncthreads();
+  }
+}
+
+// counters[0]: blocks done; counters[1]: long runs recorded in longs[].
+__global__ void __launch_bounds__(kRunThreads) k_runfix(
+    uint64_t* __restrict__ kin, uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
+    uint32_t* __restrict__ vout, int64_t n, int lo_bit, int lo_sort, uint32_t* counters,
+    uint32_t* longs, uint32_t longs_cap) {
+  __shared__ uint32_t s_cnt[256];
+  __shared__ uint32_t s_w[(kRunThreads / 32) * 256];
+  __shared__ bool s_last;
+  const int64_t i = (int64_t)blockIdx.x * kRunThreads + threadIdx.x;
+  if (i < n) {
+    const uint64_t k = kin[i];
+    const uint32_t v = vin[i];
+    const uint64_t h = k >> lo_sort;
+    const bool prev = i > 0 && (kin[i - 1] >> lo_sort) == h;
+    const bool next = i + 1 < n && (kin[i + 1] >> lo_sort) == h;
+    if (!prev && !next) {
+      kout[i] = k, vout[i] = v;
+    } else {
+      int64_t s = i, e = i + 1;
+      while (s > 0 && i - s < kRunShort && (kin[s - 1] >> lo_sort) == h) --s;
+      while (e < n && e - s <= kRunShort && (kin[e] >> lo_sort) == h) ++e;
+      const bool open = (s > 0 && (kin[s - 1] >> lo_sort) == h) || (e < n && (kin[e] >> lo_sort) == h);
+      if (!open) {  // a short run: this pair's place is the run's start plus the pairs before it
+        uint32_t r = 0;
+        for (int64_t j = s; j < e; ++j) r += pair_less(kin[j], vin[j], k, v);
+        kout[s + r] = k, vout[s + r] = v;
+      } else if (!prev) {  // a long run's first pair records it
+        const uint32_t slot = atomicAdd(&counters[1], 1u);
+        if (slot < longs_cap) longs[slot] = (uint32_t)i;
+      }
+    }
+  }
+  // the last block to finish sorts the long runs
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(&counters[0], 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  const uint32_t count = *((volatile uint32_t*)&counters[1]);
+  for (uint32_t r = 0; r < count && r < longs_cap; ++r) {
+    const int64_t s = *((volatile uint32_t*)&longs[r]);
+    const uint64_t h = kin[s] >> lo_sort;
+    // the run's end: the first pair past s whose top bits differ
+    __shared__ unsigned long long s_end;
+    if (threadIdx.x == 0) s_end = (unsigned long long)n;
+    __syncthreads();
+    for (int64_t base = s + 1; base < n; base += kRunThreads) {
+      const int64_t j = base + threadIdx.x;
+      if (j < n && (kin[j] >> lo_sort) != h) atomicMin(&s_end, (unsigned long long)j);
+      if (__syncthreads_or(j < n && (kin[j] >> lo_sort) != h)) break;
+    }
+    const int64_t L = (int64_t)s_end - s;
+    cta_sort_run(kin + s, vin + s, kout + s, vout + s, L, lo_bit, lo_sort, s_cnt, s_w);
+    __syncthreads();
+  }
+}
+
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 int64_t tiles_for(int64_t n) { return (n + kTile - 1) / kTile; }
+uint32_t longs_cap_for(int64_t n) { return (uint32_t)(n / (kRunShort + 1) + 1); }
 
 }  // namespace
 
@@ -207,7 +345,8 @@ int fl_sort_tile() { return kTile; }
 size_t fl_sort_bytes(int64_t n) {
   int64_t cap = n > 0 ? n : 1, tiles = tiles_for(cap);
   return 2 * align256(8 * (size_t)cap) + 2 * align256(4 * (size_t)cap) + align256(8 * 256 * 4) +
-         align256(8 * (size_t)tiles * 256 * 4) + align256(8 * 4);
+         align256(8 * (size_t)tiles * 256 * 4) + align256(kSortCounters * 4) +
+         align256(4 * (size_t)longs_cap_for(cap));
 }
 
 void fl_sort_carve(FlSortBufs* b, void* base, int64_t n) {
@@ -217,7 +356,9 @@ void fl_sort_carve(FlSortBufs* b, void* base, int64_t n) {
   for (int i = 0; i < 2; ++i) b->vals[i] = reinterpret_cast<uint32_t*>(p), p += align256(4 * (size_t)cap);
   b->hist = reinterpret_cast<uint32_t*>(p), p += align256(8 * 256 * 4);
   b->status = reinterpret_cast<uint32_t*>(p), p += align256(8 * (size_t)tiles * 256 * 4);
-  b->counters = reinterpret_cast<uint32_t*>(p);
+  b->counters = reinterpret_cast<uint32_t*>(p), p += align256(kSortCounters * 4);
+  b->longs = reinterpret_cast<uint32_t*>(p);
+  b->longs_cap = longs_cap_for(cap);
   b->cap = cap;
   b->tiles_cap = tiles;
 }
@@ -226,12 +367,12 @@ void fl_sort_reset(const FlSortBufs* b, int64_t n, int passes, cudaStream_t st) 
   int64_t tiles = tiles_for(n > 0 ? n : 1);
   if (tiles == b->tiles_cap) {  // histogram, look-back words and tickets are contiguous
     const char* a = reinterpret_cast<const char*>(b->hist);
-    const char* e = reinterpret_cast<const char*>(b->counters) + 8 * 4;
+    const char* e = reinterpret_cast<const char*>(b->counters) + kSortCounters * 4;
     cudaMemsetAsync(b->hist, 0, (size_t)(e - a), st);
     return;
   }
   cudaMemsetAsync(b->hist, 0, 8 * 256 * 4, st);
-  cudaMemsetAsync(b->counters, 0, 8 * 4, st);
+  cudaMemsetAsync(b->counters, 0, kSortCounters * 4, st);
   for (int p = 0; p < passes; ++p)
     cudaMemsetAsync(b->status + (size_t)p * b->tiles_cap * 256, 0, (size_t)tiles * 256 * 4, st);
 }
@@ -266,4 +407,20 @@ int fl_sort_passes(const FlSortBufs* b, int64_t n, int lo_bit, uint32_t* err, cu
     cur = 1 - cur;
   }
   return cur;
+}
+
+int fl_sort_split(int lo_bit) {
+  const int rest = 32 - lo_bit;
+  return rest > 0 ? lo_bit + 8 * ((rest + 7) / 8) : lo_bit;
+}
+
+int fl_sort_runfix(const FlSortBufs* b, int64_t n, int lo_bit, int lo_sort, int cur,
+                   cudaStream_t st, int64_t* launches) {
+  if (n <= 0 || lo_sort <= lo_bit) return cur;
+  const int64_t blocks = (n + kRunThreads - 1) / kRunThreads;
+  k_runfix<<<(unsigned)blocks, kRunThreads, 0, st>>>(b->keys[cur], b->vals[cur], b->keys[1 - cur],
+                                                     b->vals[1 - cur], n, lo_bit, lo_sort,
+                                                     b->counters + 8, b->longs, b->longs_cap);
+  ++*launches;
+  return 1 - cur;
 }

@@ -104,6 +104,8 @@ extern "C" int32_t fl_radix_sort_noalloc(const uint64_t* keys, const uint32_t* v
   sb.hist = reinterpret_cast<uint32_t*>(base + kHistOff);
   sb.status = reinterpret_cast<uint32_t*>(base + kStatusOff);
   sb.counters = reinterpret_cast<uint32_t*>(base + kCountersOff);
+  sb.longs = nullptr;  // no run fix-up: every digit pass runs
+  sb.longs_cap = 0;
   sb.cap = n;
   sb.tiles_cap = kTiles;
   int64_t launches = 0;

@@ -159,8 +159,10 @@ __global__ void __launch_bounds__(kThreads) k_integrate(float4* __restrict__ pos
                                                         int ndim, float decay, const FlReduce* red,
                                                         double cx, double cy, double cz,
                                                         double strength, const FlGraph* gr,
-                                                        const uint32_t* __restrict__ gid) {
+                                                        const uint32_t* __restrict__ gid,
+                                                        const FlTick* __restrict__ tk) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tk) decay = tk->decay;
   float2 sh[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
   if (red) center_shift(red, n, ndim, cx, cy, cz, strength, sh);  // block-uniform branch
   if (i >= n) return;
@@ -202,8 +204,9 @@ __global__ void __launch_bounds__(kThreads) k_radial(const float4* __restrict__ 
                                                      const float* __restrict__ radius,
                                                      const float* __restrict__ strength, int n,
                                                      int ndim, float cx, float cy, float cz,
-                                                     float alpha) {
+                                                     float alpha, const FlTick* __restrict__ tk) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tk) alpha = tk->alpha;
   if (i >= n) return;
   float4 p = pos[i];
   float dx = or1e6(p.x - cx);
@@ -223,8 +226,10 @@ __global__ void __launch_bounds__(kThreads) k_position(const float4* __restrict_
                                                        float4* __restrict__ vel,
                                                        const float* __restrict__ target,
                                                        const float* __restrict__ strength, int n,
-                                                       int axis, float alpha) {
+                                                       int axis, float alpha,
+                                                       const FlTick* __restrict__ tk) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tk) alpha = tk->alpha;
   if (i >= n) return;
   float p = axis == 0 ? pos[i].x : axis == 1 ? pos[i].y : pos[i].z;
   float dv = (target[i] - p) * strength[i] * alpha;
@@ -257,18 +262,20 @@ void fl_launch_breduce(const float4* pos, int n, int ndim, const uint32_t* gid, 
 void fl_launch_integrate(float4* pos, float4* vel, const float4* fix, const uint32_t* mask, int n,
                          int ndim, float decay, const FlReduce* red, double cx, double cy,
                          double cz, double strength, cudaStream_t st, const FlGraph* gr,
-                         const uint32_t* gid) {
+                         const uint32_t* gid, const FlTick* tk) {
   k_integrate<<<grid_for(n, kThreads), kThreads, 0, st>>>(pos, vel, fix, mask, n, ndim, decay, red,
-                                                          cx, cy, cz, strength, gr, gid);
+                                                          cx, cy, cz, strength, gr, gid, tk);
 }
 
 void fl_launch_radial(const float4* pos, float4* vel, const float* radius, const float* strength,
-                      int n, int ndim, float cx, float cy, float cz, float alpha, cudaStream_t st) {
+                      int n, int ndim, float cx, float cy, float cz, float alpha, cudaStream_t st,
+                      const FlTick* tk) {
   k_radial<<<grid_for(n, kThreads), kThreads, 0, st>>>(pos, vel, radius, strength, n, ndim, cx, cy,
-                                                       cz, alpha);
+                                                       cz, alpha, tk);
 }
 
 void fl_launch_position(const float4* pos, float4* vel, const float* target, const float* strength,
-                        int n, int axis, float alpha, cudaStream_t st) {
-  k_position<<<grid_for(n, kThreads), kThreads, 0, st>>>(pos, vel, target, strength, n, axis, alpha);
+                        int n, int axis, float alpha, cudaStream_t st, const FlTick* tk) {
+  k_position<<<grid_for(n, kThreads), kThreads, 0, st>>>(pos, vel, target, strength, n, axis, alpha,
+                                                         tk);
 }

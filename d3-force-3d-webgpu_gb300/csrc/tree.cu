@@ -844,7 +844,8 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
     const float* __restrict__ cube, float4* __restrict__ vel, int n, float alpha,
     double theta2, float dmin2, float dmax2, uint32_t step, uint32_t seed, uint32_t* err,
     unsigned long long* stats, uint4* __restrict__ spill, int nwarps, uint32_t* work,
-    FlSegs segs) {
+    FlSegs segs, const FlTick* __restrict__ tk) {
+  if (tk) alpha = tk->alpha, step = tk->step, seed = tk->seed;
   constexpr int NG = 32 / G;
   // the stack of a group: kStack entries in shared memory, then up to kWalkStack(NDIM, G) in
   // all, the rest in this warp slot's region of the spill buffer
@@ -1091,7 +1092,9 @@ __global__ void __launch_bounds__(kPairThreads) k_allpairs(const float4* __restr
                                                            float4* __restrict__ vel, int n,
                                                            int ndim, float alpha, float dmin2,
                                                            float dmax2, uint32_t step,
-                                                           uint32_t seed, int split) {
+                                                           uint32_t seed, int split,
+                                                           const FlTick* __restrict__ tk) {
+  if (tk) alpha = tk->alpha, step = tk->step, seed = tk->seed;
   __shared__ float4 tile[kPairThreads];
   __shared__ float3 part[kPairThreads];
   const int per = kPairThreads / split;
@@ -1285,7 +1288,7 @@ int walk_blocks_per_sm() {
 void fl_launch_walk(const FlTreeBufs* t, const uint32_t* perm, const float* cube, float4* vel,
                     float alpha, double theta2, double dmin2, double dmax2, uint32_t step,
                     uint32_t seed, uint32_t* err, unsigned long long* stats, int group,
-                    cudaStream_t st, FlSegs segs) {
+                    cudaStream_t st, FlSegs segs, const FlTick* tk) {
   const int n = t->n;
   const int warps = (n + 31) / 32;
   // a persistent grid of the blocks that fit on the device at once (and that the spill buffer
@@ -1300,7 +1303,7 @@ void fl_launch_walk(const FlTreeBufs* t, const uint32_t* perm, const float* cube
     if (g < 1) g = 1;                                                                          \
     k_walk<D, G, S, M, B><<<g, kWalkThreads, 0, st>>>(                                         \
         t->child_data, t->child_meta, t->leaf, perm, cube, vel, n, alpha, theta2,              \
-        (float)dmin2, fmax2, step, seed, err, stats, t->spill, warps, t->work, segs);          \
+        (float)dmin2, fmax2, step, seed, err, stats, t->spill, warps, t->work, segs, tk);      \
   } while (0)
 #define FL_WALK(D, G)                                                                          \
   do {                                                                                         \
@@ -1334,14 +1337,14 @@ void fl_launch_walk(const FlTreeBufs* t, const uint32_t* perm, const float* cube
 
 void fl_launch_allpairs(const float4* pos, const float* strength, float4* vel, int n, int ndim,
                         float alpha, float dmin2, float dmax2, uint32_t step, uint32_t seed,
-                        cudaStream_t st) {
+                        cudaStream_t st, const FlTick* tk) {
   // threads per point: enough threads in flight for small graphs (2^18 in all), at most 16
   int split = 1;
   while (split < 16 && (int64_t)n * split < (1 << 18)) split *= 2;
   const int per = kPairThreads / split;
   const int g = (n + per - 1) / per;
   k_allpairs<<<g < 1 ? 1 : g, kPairThreads, 0, st>>>(pos, strength, vel, n, ndim, alpha, dmin2,
-                                                     dmax2, step, seed, split);
+                                                     dmax2, step, seed, split, tk);
 }
 
 void fl_launch_bgraph(int graphs, int ndim, const int32_t* off, const FlReduce* red,

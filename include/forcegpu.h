@@ -142,8 +142,10 @@ int32_t fl_buffers(fl_sim* sim, fl_buffer_info* out);
  * and centroids are summed: FL_CELLS_AUTO (default: exact fixed-point prefix sums when the
  * strengths share one sign, else the bottom-up recursion with FP64 sums near the root),
  * FL_CELLS_FP64_TOP (always that recursion) or FL_CELLS_FP32 (the recursion all in FP32, for
- * precision comparisons). */
-enum { FL_TUNE_WALK_GROUP = 1, FL_TUNE_CELL_SUMS = 2 };
+ * precision comparisons); FL_TUNE_GRAPHS, 1 (default) to run a block of ticks that fl_enqueue
+ * has seen before (same length, same forces) as one CUDA graph, captured the second time it is
+ * seen, or 0 to launch every kernel of every block directly. */
+enum { FL_TUNE_WALK_GROUP = 1, FL_TUNE_CELL_SUMS = 2, FL_TUNE_GRAPHS = 3 };
 enum { FL_CELLS_AUTO = 0, FL_CELLS_FP64_TOP = 1, FL_CELLS_FP32 = 2 };
 int32_t fl_set_tuning(fl_sim* sim, int32_t key, int32_t value);
 

@@ -69,10 +69,44 @@ def _tree_of(nodes, dims):
     return sim
 
 
+def clustered_nodes(dims, clusters, per, spread, tight, seed, loose=0):
+    """`clusters` clusters of `per` points each, their centres spread over `spread` and their
+    points within `tight` of the centre (some exactly coincident), plus `loose` spread points:
+    many points share the top 32 bits of their Morton codes but differ below."""
+    rng = np.random.default_rng(seed)
+    xyz = []
+    for c in range(clusters):
+        centre = rng.uniform(-spread / 2, spread / 2, dims)
+        off = rng.uniform(0, tight, (per, dims))
+        off[per // 3] = off[0]  # a coincident pair
+        xyz.append(centre + off)
+    xyz.append(rng.uniform(-spread / 2, spread / 2, (loose, dims)))
+    xyz = np.float32(np.concatenate(xyz)).astype(np.float64)
+    rng.shuffle(xyz)
+    return [{k: float(v) for k, v in zip("xyz", row)} for row in xyz]
+
+
+# the tree's sort orders the top 32 key bits by digit passes and then the runs of equal top
+# bits by a fix-up: runs of a few points, of up to 1024 (ranked in place) and longer ones (sorted
+# by the last block of the fix-up)
+CLUSTERED = {
+    "short runs 3d": (3, 200, 30, 200.0, 1e-3, 1, 0),
+    "long run 3d": (3, 1, 3000, 200.0, 1e-3, 2, 2000),
+    "several long runs 3d": (3, 3, 1500, 200.0, 1e-3, 3, 500),
+    "short and long runs 2d": (2, 50, 40, 200.0, 1e-5, 4, 0),
+    "long run 2d": (2, 1, 2500, 200.0, 1e-5, 5, 300),
+}
+
+
 @pytest.mark.parametrize("dims,n,size", [(1, 500, 200), (2, 2000, 200), (3, 5000, 200),
-                                         (3, 3000, 2), (3, 1000, 2e5), (2, 257, 1)])
+                                         (3, 3000, 2), (3, 1000, 2e5), (2, 257, 1)]
+                         + [pytest.param(v[0], None, k, id=k) for k, v in CLUSTERED.items()])
 def test_tree_matches_cpu_rebuild(dims, n, size):
-    nodes = make_nodes(n, dims, size)
+    if n is None:
+        nodes = clustered_nodes(*CLUSTERED[size])
+        n = len(nodes)
+    else:
+        nodes = make_nodes(n, dims, size)
     nodes[0]["x"] = nodes[1]["x"]  # shared coordinates
     if dims > 1:
         nodes[2]["x"], nodes[2]["y"] = nodes[3]["x"], nodes[3]["y"]
