@@ -66,6 +66,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--block", type=int, default=50,
                    help="ticks queued per enqueue call (a block seen twice runs as a CUDA graph)")
+    p.add_argument("--no-autotune", action="store_true",
+                   help="keep the default tuning (else fl_autotune picks it before the warm-up)")
     p.add_argument("--walk-group", type=int, default=32, choices=[16, 32],
                    help="points per tree-walk traversal (FL_TUNE_WALK_GROUP)")
     p.add_argument("--precision", action="store_true",
@@ -318,6 +320,7 @@ def run_batched(args):
     nodes = int(sum(len(s.xyz) for s in specs))
     b = Batch(0)
     b.set_graphs(specs, ndim=3, seed=12345)
+    tuning = None if args.no_autotune else b.autotune(ticks=3)
     stream = torch.cuda.ExternalStream(b.stream(), device=0)
     # warm-up on a copy of the schedule, then the timed full layout from the start
     b.run(args.warmup)
@@ -374,7 +377,8 @@ def run_batched(args):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "%d 3D graphs, sizes log-uniform in [100, 20000] (seed 2024), "
                                    "1.5 links/node, link+charge(theta 0.9)+center, 300 ticks each"
-                                   % len(specs), "graphs": len(specs), "nodes": nodes},
+                                   % len(specs), "graphs": len(specs), "nodes": nodes,
+                       "tuning": tuning},
             "e2e": {"value": len(specs) / wall, "unit": "layouts/s",
                     "h2d_bytes_per_step": 8 * len(specs), "d2h_bytes_per_step": 32 * nodes / ticks},
             "serial_plain": {"value": serial, "unit": "layouts/s", "sample_graphs": len(sample),
@@ -612,6 +616,9 @@ def main():
     eng.set_seed(12345)
     eng.set_tuning(TUNE_WALK_GROUP, args.walk_group)
     decay = 0.6
+    tuning = None
+    if not args.no_autotune:  # outside the timed region, from the same start
+        tuning = eng.autotune(ticks=10, alpha=0.5, decay=decay)
     # ticks are queued in blocks of B, as an application queues a frame's or a batch's worth:
     # the engine runs a block it has seen before as one CUDA graph
     B = max(1, min(args.block, args.steps))
@@ -725,7 +732,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "3D layout, %d nodes, %d links, link+charge(theta 0.9)+center, "
                                    "ticks %d-%d from the phyllotaxis start" % (n, len(src), warm + 1, warm + args.steps),
-                       "tick_block": B,
+                       "tick_block": B, "tuning": tuning,
                        "nodes": n, "links": int(len(src)), "parallelism": "replicas" if world > 1 else "single",
                        "l2": "working set %.0f MB > 126 MB L2 (no flush)" % (dev_bytes / 1e6)},
             "gpu_launches": int(launches), "clocks": clk, "roofline": roof, "kernels": kernels}

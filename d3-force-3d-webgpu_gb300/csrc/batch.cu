@@ -17,6 +17,7 @@
 
 #include "../../include/forcegpu.h"
 #include "kernels.h"
+#include "tune.h"
 
 namespace {
 
@@ -78,6 +79,7 @@ struct fl_batch {
   };
   std::vector<Block> blocks;
   bool use_graphs = true;
+  int sort_passes = 0, walk_blocks = 0;  // tuning (FL_TUNE_SORT_PASSES, FL_TUNE_WALK_BLOCKS)
 };
 
 namespace {
@@ -138,7 +140,7 @@ void encode_batch_tick(fl_batch* b, const double* alpha, const FlTick* tk) {
   // many-body: sort by Morton code, then (stably) by graph; one tree per graph
   if (n >= 2) {
     const int bits = (b->ndim == 3 ? 21 : 24) * b->ndim, lo_bit = 64 - bits;
-    const int lo_sort = fl_sort_split(lo_bit);
+    const int lo_sort = fl_sort_split(lo_bit, b->sort_passes);
     fl_sort_reset(&b->sb, n, (64 - lo_sort + 7) / 8, st);
     fl_launch_bmorton(b->pos.as<float4>(), n, b->ndim, gid, gr, b->sb.keys[0], b->sb.vals[0],
                       b->sb.hist, lo_sort, st);
@@ -157,6 +159,7 @@ void encode_batch_tick(fl_batch* b, const double* alpha, const FlTick* tk) {
                     nullptr, b->fx_exp, st, &b->launches, segs);
     fl_launch_aggregate(&b->tb, skeys, b->closed, b->sign, nullptr, b->fx_exp, 6, err, st,
                         &b->launches, segs);
+    b->tb.walk_blocks = b->walk_blocks;
     fl_launch_walk(&b->tb, perm, nullptr, bvel(b), 0.f, 1.0, 0.0, b->dmax_any, b->step, b->seed,
                    err, nullptr, 32, st, segs, tk);
     ++b->launches;
@@ -349,6 +352,28 @@ int32_t fl_batch_set_seed(fl_batch* b, uint32_t seed) {
   return FL_OK;
 }
 
+int32_t fl_batch_set_tuning(fl_batch* b, int32_t key, int32_t value) {
+  int32_t rc = bcheck(b);
+  if (rc) return rc;
+  clear_blocks(b);
+  switch (key) {
+    case FL_TUNE_GRAPHS:
+      if (value != 0 && value != 1) return bfail(b, FL_E_ARG, "graphs must be 0 or 1");
+      b->use_graphs = value != 0;
+      return FL_OK;
+    case FL_TUNE_SORT_PASSES:
+      if (value < 0 || value > 8) return bfail(b, FL_E_ARG, "sort passes must be 0..8");
+      b->sort_passes = value;
+      return FL_OK;
+    case FL_TUNE_WALK_BLOCKS:
+      if (value < 0 || value > 32) return bfail(b, FL_E_ARG, "walk blocks per SM must be 0..32");
+      b->walk_blocks = value;
+      return FL_OK;
+    default:
+      return bfail(b, FL_E_ARG, "unknown tuning key for a batch");
+  }
+}
+
 int32_t fl_batch_enqueue(fl_batch* b, const double* alphas, int32_t ticks) {
   int32_t rc = bcheck(b);
   if (rc) return rc;
@@ -444,6 +469,81 @@ int32_t fl_batch_sync(fl_batch* b, float* pos4_out, float* vel4_out) {
     if (w & FL_ERR_LOOKBACK) return bfail(b, FL_E_TIMEOUT, "a device-side look-back wait gave up");
     return bfail(b, FL_E_OVERFLOW, "a tree was malformed or a walk overflowed");
   }
+  return FL_OK;
+}
+
+int32_t fl_batch_autotune(fl_batch* b, int32_t ticks, double alpha, const char* cache_path,
+                          fl_tune_result* out) {
+  int32_t rc = bcheck(b);
+  if (rc) return rc;
+  if (!out) return bfail(b, FL_E_ARG, "out is NULL");
+  if (ticks < 1 || !(alpha >= 0.0)) return bfail(b, FL_E_ARG, "ticks must be >= 1 and alpha >= 0");
+  *out = fl_tune_result{32, b->sort_passes, b->walk_blocks, 100, 0, 0, 0, 0};
+  const int n = b->n;
+  if (!b->graphs || n < 2) return FL_OK;
+  const int bits = (b->ndim == 3 ? 21 : 24) * b->ndim, lo_bit = 64 - bits;
+  std::vector<int> passes{0}, seen{fl_sort_split(lo_bit, 0)};
+  for (int c : {3, 5, 8}) {
+    const int lo = fl_sort_split(lo_bit, c);
+    if (std::find(seen.begin(), seen.end(), lo) == seen.end()) seen.push_back(lo), passes.push_back(c);
+  }
+  std::vector<FlTuneKnob> knobs{{FL_TUNE_SORT_PASSES, "sort_passes", passes, 0},
+                                {FL_TUNE_WALK_BLOCKS, "walk_blocks", {0, 8, 6, 4}, 0}};
+  const std::string key = fl_tune_arch() + " batch ndim=" + std::to_string(b->ndim) +
+                          " log2graphs=" + std::to_string((int)std::floor(std::log2((double)b->graphs))) +
+                          " log2n=" + std::to_string((int)std::floor(std::log2((double)n))) +
+                          " links=" + std::to_string(b->m > 0 ? 1 : 0) +
+                          " graphs=" + std::to_string((int)b->use_graphs);
+  FB_CK(b, cudaStreamSynchronize(b->st));
+  Buf snap;
+  const size_t v4 = 16 * (size_t)n;
+  FB_CK(b, snap.alloc(2 * v4));
+  FB_CK(b, cudaMemcpyAsync(snap.p, b->pos.p, v4, cudaMemcpyDeviceToDevice, b->st));
+  FB_CK(b, cudaMemcpyAsync(snap.as<char>() + v4, bvel(b), v4, cudaMemcpyDeviceToDevice, b->st));
+  const uint32_t step0 = b->step;
+  const int64_t ticks0 = b->ticks, launches0 = b->launches;
+  auto restore = [&]() -> int32_t {
+    FB_CK(b, cudaMemcpyAsync(b->pos.p, snap.p, v4, cudaMemcpyDeviceToDevice, b->st));
+    FB_CK(b, cudaMemcpyAsync(b->vel[0].p, snap.as<char>() + v4, v4, cudaMemcpyDeviceToDevice, b->st));
+    b->cur = 0;
+    b->step = step0;
+    return FL_OK;
+  };
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  FB_CK(b, cudaEventCreate(&e0));
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return bfail(b, FL_E_DEVICE, "cudaEventCreate");
+  }
+  const std::vector<double> al((size_t)ticks * (size_t)b->graphs, alpha);
+  auto time = [&](double* ms) -> int {  // as fl_autotune: direct, captured, then timed
+    for (int rep = 0; rep < 3; ++rep) {
+      int32_t r = restore();
+      if (r) return r;
+      if (rep == 2) FB_CK(b, cudaEventRecord(e0, b->st));
+      if ((r = fl_batch_enqueue(b, al.data(), ticks)) != FL_OK) return r;
+      if (rep == 2) FB_CK(b, cudaEventRecord(e1, b->st));
+    }
+    int32_t r = fl_batch_sync(b, nullptr, nullptr);
+    if (r) return r;
+    float t = 0.f;
+    FB_CK(b, cudaEventElapsedTime(&t, e0, e1));
+    *ms = (double)t / ticks;
+    return FL_OK;
+  };
+  auto set = [&](int k, int v) -> int { return fl_batch_set_tuning(b, k, v); };
+  FlTuneOutcome o;
+  rc = fl_tune_search(cache_path, key, knobs, set, time, &o);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  const int32_t rr = restore();
+  if (!rc) rc = rr;
+  cudaError_t e = cudaStreamSynchronize(b->st);
+  b->ticks = ticks0, b->launches = launches0;
+  if (rc) return rc;
+  if (e != cudaSuccess) return bcuda(b, e, "cudaStreamSynchronize");
+  *out = fl_tune_result{32, b->sort_passes, b->walk_blocks, 100, o.best_ms, o.default_ms,
+                        o.candidates, o.cached ? 1 : 0};
   return FL_OK;
 }
 

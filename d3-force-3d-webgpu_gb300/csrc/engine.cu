@@ -19,6 +19,7 @@
 
 #include "../../include/forcegpu.h"
 #include "kernels.h"
+#include "tune.h"
 
 namespace {
 
@@ -125,6 +126,9 @@ struct fl_sim {
   std::vector<double> plan_sig;
   bool use_graphs = true;
   int cell_sums = 0;    // tuning FL_TUNE_CELL_SUMS
+  int sort_passes = 0;  // tuning FL_TUNE_SORT_PASSES (0: the default)
+  int walk_blocks = 0;  // tuning FL_TUNE_WALK_BLOCKS (0: as many as fit)
+  int collide_cell = 100;  // tuning FL_TUNE_COLLIDE_CELL (percent of the largest diameter)
   bool profiling = false;
   int prof_level = 0;
   DevMem wstats;  // walk counters (profiling level 2)
@@ -352,7 +356,7 @@ void encode_tree(fl_sim* s, Pass* p, const FlReduce* box, cudaStream_t st) {
   const int n = s->n;
   FlTreeBufs* t = &p->tb;
   const float* strength = p->a.as<float>();
-  const int lo_bit = 64 - t->bits, lo_sort = fl_sort_split(lo_bit);
+  const int lo_bit = 64 - t->bits, lo_sort = fl_sort_split(lo_bit, s->sort_passes);
   if (!box) {
     Scope sc(s, G_REDUCE, st);
     cudaMemsetAsync(p->red.p, 0, sizeof(FlReduce), st);
@@ -407,6 +411,7 @@ void encode_manybody(fl_sim* s, Pass* p, float alpha, const FlReduce* box, bool 
   else encode_tree(s, p, box, s->st);
   {
     Scope sc(s, G_WALK);
+    p->tb.walk_blocks = s->walk_blocks;
     fl_launch_walk(&p->tb, p->sb.vals[p->sorted_in], p->cube.as<float>(), vel_cur(s), alpha,
                    p->d.theta2, p->d.distance_min2, p->d.distance_max2, s->step, s->seed,
                    s->errw.as<uint32_t>(),
@@ -429,7 +434,7 @@ void encode_collide(fl_sim* s, Pass* p) {
     } else {
       FlGridBufs* g = &p->gb;
       const int lo_bit = 64 - g->bits;
-      const float inv = 1.f / (2.f * p->rmax);
+      const float inv = 1.f / (2.f * p->rmax * (float)s->collide_cell * 0.01f);
       {
         Scope sc(s, G_CKEYS);
         fl_sort_reset(&p->sb, n, (64 - lo_bit + 7) / 8, s->st);
@@ -928,9 +933,114 @@ int32_t fl_set_tuning(fl_sim* s, int32_t key, int32_t value) {
       if (value != 0 && value != 1) return fail(s, FL_E_ARG, "graphs must be 0 or 1");
       s->use_graphs = value != 0;
       return FL_OK;
+    case FL_TUNE_SORT_PASSES:
+      if (value < 0 || value > 8) return fail(s, FL_E_ARG, "sort passes must be 0..8");
+      s->sort_passes = value;
+      return FL_OK;
+    case FL_TUNE_WALK_BLOCKS:
+      if (value < 0 || value > 32) return fail(s, FL_E_ARG, "walk blocks per SM must be 0..32");
+      s->walk_blocks = value;
+      return FL_OK;
+    case FL_TUNE_COLLIDE_CELL:
+      if (value < 100 || value > 1000) return fail(s, FL_E_ARG, "collide cell must be 100..1000 percent");
+      s->collide_cell = value;
+      return FL_OK;
     default:
       return fail(s, FL_E_ARG, "unknown tuning key");
   }
+}
+
+int32_t fl_autotune(fl_sim* s, int32_t ticks, double alpha, double decay,
+                    const char* cache_path, fl_tune_result* out) {
+  int32_t rc = check_sim(s);
+  if (rc) return rc;
+  if (!out) return fail(s, FL_E_ARG, "out is NULL");
+  if (ticks < 1) return fail(s, FL_E_ARG, "ticks must be >= 1");
+  const int n = s->n;
+  bool tree = false, grid = false;
+  int key_bits = 0;
+  std::string forces;
+  for (auto& p : s->plan) {
+    forces += std::to_string(p->type);
+    if (is_tree(p.get()) && n >= 2) tree = true, key_bits = p->tb.bits, forces += 't';
+    if (p->type == FL_FORCE_COLLIDE && n >= kGridMin && p->rmax > 0.f) grid = true, forces += 'g';
+    forces += ',';
+  }
+  std::vector<FlTuneKnob> knobs;
+  if (tree) {
+    // digit-pass counts that give distinct splits of the key, the default (0) first
+    std::vector<int> passes{0};
+    const int lo_bit = 64 - key_bits;
+    std::vector<int> seen{fl_sort_split(lo_bit, 0)};
+    for (int c : {3, 5, 8}) {
+      const int lo = fl_sort_split(lo_bit, c);
+      if (std::find(seen.begin(), seen.end(), lo) == seen.end()) seen.push_back(lo), passes.push_back(c);
+    }
+    knobs.push_back({FL_TUNE_SORT_PASSES, "sort_passes", passes, 0});
+    knobs.push_back({FL_TUNE_WALK_GROUP, "walk_group", {32, 16}, 32});
+    knobs.push_back({FL_TUNE_WALK_BLOCKS, "walk_blocks", {0, 8, 6, 4}, 0});
+  }
+  if (grid) knobs.push_back({FL_TUNE_COLLIDE_CELL, "collide_cell", {100, 150, 200}, 100});
+  *out = fl_tune_result{s->walk_group, s->sort_passes, s->walk_blocks, s->collide_cell, 0, 0, 0, 0};
+  if (knobs.empty() || n < 2) return FL_OK;  // nothing to choose
+  const std::string key = fl_tune_arch() + " sim ndim=" + std::to_string(s->ndim) +
+                          " log2n=" + std::to_string((int)std::floor(std::log2((double)n))) +
+                          " forces=" + forces + " graphs=" + std::to_string((int)s->use_graphs);
+  // the state to come back to
+  FL_CK(s, cudaStreamSynchronize(s->st));
+  DevMem snap;
+  FL_CK(s, snap.alloc(32 * (size_t)n));
+  const size_t v4 = 16 * (size_t)n;
+  FL_CK(s, cudaMemcpyAsync(snap.p, s->pos.p, v4, cudaMemcpyDeviceToDevice, s->st));
+  FL_CK(s, cudaMemcpyAsync(snap.as<char>() + v4, vel_cur(s), v4, cudaMemcpyDeviceToDevice, s->st));
+  const uint32_t step0 = s->step;
+  const int64_t ticks0 = s->ticks, launches0 = s->launches;
+  auto restore = [&]() -> int32_t {
+    FL_CK(s, cudaMemcpyAsync(s->pos.p, snap.p, v4, cudaMemcpyDeviceToDevice, s->st));
+    FL_CK(s, cudaMemcpyAsync(s->vel[0].p, snap.as<char>() + v4, v4, cudaMemcpyDeviceToDevice, s->st));
+    s->cur = 0;
+    s->step = step0;
+    return FL_OK;
+  };
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  FL_CK(s, cudaEventCreate(&e0));
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return fail(s, FL_E_DEVICE, "cudaEventCreate");
+  }
+  const std::vector<double> al((size_t)ticks, alpha);
+  // a configuration's time: its block of ticks run three times from the same state (the first
+  // direct, the second captured, the third timed: as an application's steady state runs it)
+  auto time = [&](double* ms) -> int {
+    for (int rep = 0; rep < 3; ++rep) {
+      int32_t r = restore();
+      if (r) return r;
+      if (rep == 2 && cudaEventRecord(e0, s->st) != cudaSuccess) return cuda_fail(s, cudaGetLastError(), "cudaEventRecord");
+      if ((r = fl_enqueue(s, al.data(), ticks, decay)) != FL_OK) return r;
+      if (rep == 2 && cudaEventRecord(e1, s->st) != cudaSuccess) return cuda_fail(s, cudaGetLastError(), "cudaEventRecord");
+    }
+    FL_CK(s, cudaEventSynchronize(e1));
+    int32_t r = collect_errors(s);
+    if (r) return r;
+    float t = 0.f;
+    FL_CK(s, cudaEventElapsedTime(&t, e0, e1));
+    *ms = (double)t / ticks;
+    return FL_OK;
+  };
+  auto set = [&](int k, int v) -> int { return fl_set_tuning(s, k, v); };
+  FlTuneOutcome o;
+  rc = fl_tune_search(cache_path, key, knobs, set, time, &o);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  const int32_t rr = restore();
+  if (!rc) rc = rr;
+  cudaError_t e = cudaStreamSynchronize(s->st);
+  s->ticks = ticks0, s->launches = launches0;
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_fail(s, e, "cudaStreamSynchronize");
+  *out = fl_tune_result{s->walk_group, s->sort_passes, s->walk_blocks, s->collide_cell,
+                        o.best_ms, o.default_ms, o.candidates, o.cached ? 1 : 0};
+  return FL_OK;
 }
 
 int32_t fl_stream(fl_sim* s, void** stream) {

@@ -76,6 +76,7 @@ constexpr int kSortCounters = 16;
 constexpr int kSortThreads = 512, kSortItems = 8;  // threads of a onesweep tile, pairs each
 constexpr int kSortTile = kSortThreads * kSortItems;  // pairs per onesweep tile
 int fl_sort_tile();  // kSortTile
+int fl_sms();        // SMs of the current device (cached per process)
 size_t fl_sort_bytes(int64_t n);
 // Carve the buffers out of one allocation of fl_sort_bytes(n) bytes.
 void fl_sort_carve(FlSortBufs* b, void* base, int64_t n);
@@ -86,11 +87,11 @@ void fl_sort_histogram(const FlSortBufs* b, int64_t n, int lo_bit, cudaStream_t 
 // Run the passes from keys[0]/vals[0]; returns which buffer (0/1) holds the result.
 int fl_sort_passes(const FlSortBufs* b, int64_t n, int lo_bit, uint32_t* err, cudaStream_t st,
                    int64_t* launches);
-// The tree's key sort in two steps: digit passes over the top key bits [fl_sort_split(lo_bit),
-// 64) (at least the top 32, in whole digits), then fl_sort_runfix, which puts each run of pairs
-// equal in those bits in (key, value) order: together the stable sort on [lo_bit, 64) of pairs
-// whose values start as 0, 1, 2, ... Returns the buffer holding the result.
-int fl_sort_split(int lo_bit);
+// The tree's key sort in two steps: `passes` digit passes over the top key bits
+// [fl_sort_split(lo_bit, passes), 64) (0: 4 passes), then fl_sort_runfix, which puts each run of
+// pairs equal in those bits in (key, value) order: together the stable sort on [lo_bit, 64) of
+// pairs whose values start as 0, 1, 2, ... fl_sort_runfix returns the buffer holding the result.
+int fl_sort_split(int lo_bit, int passes = 0);
 int fl_sort_runfix(const FlSortBufs* b, int64_t n, int lo_bit, int lo_sort, int cur,
                    cudaStream_t st, int64_t* launches);
 
@@ -148,6 +149,7 @@ struct FlTreeBufs {
   uint4* spill;          // the walk stacks' overflow, one region per warp slot of its grid
   uint32_t* work;        // the walk's next group of 32 points to hand out
   int walk_slots;        // warp slots of the persistent walk grid
+  int walk_blocks;       // blocks per SM of that grid (0: as many as fit)
   int sms;               // SMs of the device
 };
 struct FlWalkParams {

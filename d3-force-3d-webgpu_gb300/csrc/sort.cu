@@ -19,6 +19,7 @@ constexpr int kTile = kSortTile;
 constexpr uint32_t kValMask = (1u << 30) - 1;
 constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagPre = 2u << 30;
+constexpr int kLook = 8;  // look-back words read per round (64 registers: two tiles per SM)
 
 // Block-wide exclusive scan of one value per thread (kThreads); returns the exclusive prefix,
 // and the block total in *total.
@@ -66,7 +67,7 @@ __global__ void __launch_bounds__(256) k_hist(const uint64_t* __restrict__ keys,
     if (sh[i]) atomicAdd(&hist[i], sh[i]);
 }
 
-__global__ void __launch_bounds__(kThreads) k_onesweep(
+__global__ void __launch_bounds__(kThreads, 2) k_onesweep(
     const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
     uint32_t* __restrict__ vout, int64_t n, int shift, const uint32_t* __restrict__ ghist,
     uint32_t* status, uint32_t* ticket, uint32_t* err) {
@@ -141,18 +142,21 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(
 
   uint32_t prefix = 0;
   if (dt && tile > 0) {
-    // look back four tiles per round (independent loads), up to the nearest inclusive prefix
+    // look back kLook tiles per round (independent loads), up to the nearest inclusive prefix:
+    // all tiles of a pass start at once and publish their counts together, so the inclusive
+    // prefixes spread from tile 0 while the last tiles walk back to meet them; a wide round
+    // shortens that walk
     int64_t p = (int64_t)tile - 1;
     uint32_t spins = 0;
     for (;;) {
-      uint32_t w[4];
+      uint32_t w[kLook];
 #pragma unroll
-      for (int k = 0; k < 4; ++k)
+      for (int k = 0; k < kLook; ++k)
         w[k] = p - k >= 0 ? fl::ld_relaxed(status + (size_t)(p - k) * 256 + d) : kFlagPre;
       int used = 0;
       bool done = false;
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
+      for (int k = 0; k < kLook; ++k) {
         if (done || used < k) break;
         const uint32_t f = w[k] & ~kValMask;
         if (f == 0) break;  // not published yet: wait for it
@@ -283,8 +287,10 @@ __global__ void __launch_bounds__(kRunThreads) k_runfix(
   __shared__ uint32_t s_cnt[256];
   __shared__ uint32_t s_w[(kRunThreads / 32) * 256];
   __shared__ bool s_last;
-  const int64_t i = (int64_t)blockIdx.x * kRunThreads + threadIdx.x;
-  if (i < n) {
+  // a grid-stride loop over few blocks: the fence and ticket each block takes at its end then
+  // cost little next to its work
+  for (int64_t i = (int64_t)blockIdx.x * kRunThreads + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * kRunThreads) {
     const uint64_t k = kin[i];
     const uint32_t v = vin[i];
     const uint64_t h = k >> lo_sort;
@@ -341,6 +347,16 @@ uint32_t longs_cap_for(int64_t n) { return (uint32_t)(n / (kRunShort + 1) + 1); 
 }  // namespace
 
 int fl_sort_tile() { return kTile; }
+
+int fl_sms() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    sms = cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0 ? v : 1;
+  }
+  return sms;
+}
 
 size_t fl_sort_bytes(int64_t n) {
   int64_t cap = n > 0 ? n : 1, tiles = tiles_for(cap);
@@ -409,15 +425,17 @@ int fl_sort_passes(const FlSortBufs* b, int64_t n, int lo_bit, uint32_t* err, cu
   return cur;
 }
 
-int fl_sort_split(int lo_bit) {
-  const int rest = 32 - lo_bit;
-  return rest > 0 ? lo_bit + 8 * ((rest + 7) / 8) : lo_bit;
+int fl_sort_split(int lo_bit, int passes) {
+  const int full = (64 - lo_bit + 7) / 8;
+  if (passes <= 0) passes = 4;
+  return passes >= full ? lo_bit : lo_bit + 8 * (full - passes);
 }
 
 int fl_sort_runfix(const FlSortBufs* b, int64_t n, int lo_bit, int lo_sort, int cur,
                    cudaStream_t st, int64_t* launches) {
   if (n <= 0 || lo_sort <= lo_bit) return cur;
-  const int64_t blocks = (n + kRunThreads - 1) / kRunThreads;
+  int64_t blocks = (n + kRunThreads - 1) / kRunThreads;
+  if (blocks > 8 * (int64_t)fl_sms()) blocks = 8 * (int64_t)fl_sms();  // one full wave
   k_runfix<<<(unsigned)blocks, kRunThreads, 0, st>>>(b->keys[cur], b->vals[cur], b->keys[1 - cur],
                                                      b->vals[1 - cur], n, lo_bit, lo_sort,
                                                      b->counters + 8, b->longs, b->longs_cap);

@@ -1198,6 +1198,7 @@ void fl_tree_carve(FlTreeBufs* t, void* base, int64_t n, int ndim) {
   t->omask = (uint32_t*)take(4 * m);
   t->head_of = (uint32_t*)take(4 * (2 * N));
   t->walk_slots = fl_walk_slots(n);
+  t->walk_blocks = 0;
   int dev = 0;
   cudaGetDevice(&dev);
   if (cudaDeviceGetAttribute(&t->sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || t->sms < 1)
@@ -1209,10 +1210,10 @@ void fl_tree_carve(FlTreeBufs* t, void* base, int64_t n, int ndim) {
 void fl_launch_morton(const float4* pos, int n, int ndim, const FlReduce* red, uint64_t* keys,
                       uint32_t* vals, uint32_t* hist, int lo_bit, float* cube_out,
                       cudaStream_t st) {
-  // two blocks per SM: each flushes its digit histograms with up to 2048 global atomics, so
-  // fewer, longer blocks keep that flush small
+  // one full wave (8 blocks of 256 per SM, so that enough loads are in flight); each block
+  // flushes its digit histograms with up to 1024 global atomics (4 passes)
   int g = (n + kThreads - 1) / kThreads;
-  if (g > 2 * 152) g = 2 * 152;
+  if (g > 8 * fl_sms()) g = 8 * fl_sms();
   if (g < 1) g = 1;
   k_morton<<<g, kThreads, 0, st>>>(pos, n, ndim, red, keys, vals, hist, lo_bit, cube_out);
 }
@@ -1298,7 +1299,9 @@ void fl_launch_walk(const FlTreeBufs* t, const uint32_t* perm, const float* cube
   const float fmax2 = dmax2 > 3e38 ? INFINITY : (float)dmax2;
 #define FL_WALK_ONE(D, G, S, M, B)                                                             \
   do {                                                                                         \
-    int g = t->sms * walk_blocks_per_sm<D, G, S, M, B>();                                      \
+    int per = walk_blocks_per_sm<D, G, S, M, B>();                                             \
+    if (t->walk_blocks > 0 && t->walk_blocks < per) per = t->walk_blocks;                      \
+    int g = t->sms * per;                                                                      \
     if (g > cap) g = cap;                                                                      \
     if (g < 1) g = 1;                                                                          \
     k_walk<D, G, S, M, B><<<g, kWalkThreads, 0, st>>>(                                         \
@@ -1356,7 +1359,7 @@ void fl_launch_bgraph(int graphs, int ndim, const int32_t* off, const FlReduce* 
 void fl_launch_bmorton(const float4* pos, int n, int ndim, const uint32_t* gid, const FlGraph* gr,
                        uint64_t* keys, uint32_t* vals, uint32_t* hist, int lo_bit, cudaStream_t st) {
   int g = (n + kThreads - 1) / kThreads;
-  if (g > 2 * 152) g = 2 * 152;
+  if (g > 8 * fl_sms()) g = 8 * fl_sms();
   if (g < 1) g = 1;
   k_bmorton<<<g, kThreads, 0, st>>>(pos, n, ndim, gid, gr, keys, vals, hist, lo_bit);
 }

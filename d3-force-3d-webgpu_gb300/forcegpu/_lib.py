@@ -27,9 +27,11 @@ EXPORTS = ["fl_create", "fl_destroy", "fl_last_error", "fl_fits", "fl_set_nodes"
            "fl_stream", "fl_query", "fl_profile", "fl_profile_read", "fl_radix_sort",
            "fl_debug_tree", "fl_set_tuning", "fl_radix_sort_noalloc", "fl_batch_create",
            "fl_batch_destroy", "fl_batch_last_error", "fl_batch_set_graphs", "fl_batch_set_seed",
-           "fl_batch_enqueue", "fl_batch_sync", "fl_batch_query", "fl_batch_stream"]
+           "fl_batch_enqueue", "fl_batch_sync", "fl_batch_query", "fl_batch_stream",
+           "fl_autotune", "fl_batch_set_tuning", "fl_batch_autotune"]
 SORT_NOALLOC_MAX_PAIRS = 262144  # FL_SORT_NOALLOC_MAX_PAIRS
 TUNE_WALK_GROUP, TUNE_CELL_SUMS, TUNE_GRAPHS = 1, 2, 3
+TUNE_SORT_PASSES, TUNE_WALK_BLOCKS, TUNE_COLLIDE_CELL = 4, 5, 6
 CELLS_AUTO, CELLS_FP64_TOP, CELLS_FP32 = 0, 1, 2
 
 
@@ -69,6 +71,16 @@ class GraphDesc(ctypes.Structure):
         ("center_x", ctypes.c_double), ("center_y", ctypes.c_double), ("center_z", ctypes.c_double),
         ("center_strength", ctypes.c_double), ("velocity_decay", ctypes.c_double),
     ]
+
+
+class TuneResult(ctypes.Structure):
+    _fields_ = [("walk_group", ctypes.c_int32), ("sort_passes", ctypes.c_int32),
+                ("walk_blocks", ctypes.c_int32), ("collide_cell", ctypes.c_int32),
+                ("ms_per_tick", ctypes.c_double), ("ms_default", ctypes.c_double),
+                ("candidates", ctypes.c_int32), ("from_cache", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class BufferInfo(ctypes.Structure):
@@ -121,6 +133,9 @@ def load():
         "fl_batch_sync": (I32, [P, P, P]),
         "fl_batch_query": (I32, [P, I32, ctypes.POINTER(I64)]),
         "fl_batch_stream": (I32, [P, ctypes.POINTER(P)]),
+        "fl_autotune": (I32, [P, I32, D, D, ctypes.c_char_p, ctypes.POINTER(TuneResult)]),
+        "fl_batch_set_tuning": (I32, [P, I32, I32]),
+        "fl_batch_autotune": (I32, [P, I32, D, ctypes.c_char_p, ctypes.POINTER(TuneResult)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -233,6 +248,15 @@ class Engine:
 
     def set_tuning(self, key, value):
         self._check(self.L.fl_set_tuning(self.h, int(key), int(value)))
+
+    def autotune(self, ticks=10, alpha=0.5, decay=0.6, cache=None):
+        """Time candidate tunings on the current nodes and forces, keep the fastest (fl_autotune);
+        the state is left as it was. Returns the choice and its timing as a dict."""
+        out = TuneResult()
+        c = None if cache is None else os.fsencode(cache)
+        self._check(self.L.fl_autotune(self.h, int(ticks), float(alpha), float(decay), c,
+                                       ctypes.byref(out)))
+        return out.as_dict()
 
     def stream(self):
         out = ctypes.c_void_p()

@@ -15,11 +15,12 @@ from __future__ import annotations
 
 import ctypes
 import math
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
 
-from ._lib import FL_OK, FlError, GraphDesc, Q_DEVICE_BYTES, Q_LAUNCHES, load
+from ._lib import FL_OK, FlError, GraphDesc, Q_DEVICE_BYTES, Q_LAUNCHES, TuneResult, load
 
 
 @dataclass
@@ -163,6 +164,16 @@ class Batch:
 
     def device_bytes(self):
         return self.query(Q_DEVICE_BYTES)
+
+    def set_tuning(self, key, value):
+        self._check(self.L.fl_batch_set_tuning(self.h, int(key), int(value)))
+
+    def autotune(self, ticks=5, alpha=0.5, cache=None):
+        """fl_batch_autotune: the fastest sort passes and walk grid for this batch, state kept."""
+        out = TuneResult()
+        c = None if cache is None else os.fsencode(cache)
+        self._check(self.L.fl_batch_autotune(self.h, int(ticks), float(alpha), c, ctypes.byref(out)))
+        return out.as_dict()
 
     def stream(self):
         out = ctypes.c_void_p()

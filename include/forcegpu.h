@@ -144,10 +144,41 @@ int32_t fl_buffers(fl_sim* sim, fl_buffer_info* out);
  * FL_CELLS_FP64_TOP (always that recursion) or FL_CELLS_FP32 (the recursion all in FP32, for
  * precision comparisons); FL_TUNE_GRAPHS, 1 (default) to run a block of ticks that fl_enqueue
  * has seen before (same length, same forces) as one CUDA graph, captured the second time it is
- * seen, or 0 to launch every kernel of every block directly. */
-enum { FL_TUNE_WALK_GROUP = 1, FL_TUNE_CELL_SUMS = 2, FL_TUNE_GRAPHS = 3 };
+ * seen, or 0 to launch every kernel of every block directly; FL_TUNE_SORT_PASSES, the 8-bit digit
+ * passes of the tree's radix sort, from the top of the Morton key (0 = 4, the default: the top
+ * 31 bits in 3D, 32 in 2D; 8 = every bit in 3D), the bits below ordered within runs of equal top
+ * bits by a fix-up pass: fewer passes, longer runs; FL_TUNE_WALK_BLOCKS, blocks per SM of the
+ * persistent tree-walk grid (0 = as many as fit, the default); FL_TUNE_COLLIDE_CELL, the collide
+ * grid's cell side in percent of the largest diameter (>= 100; 100 = the default).
+ * fl_autotune picks these by timing. */
+enum {
+  FL_TUNE_WALK_GROUP = 1,
+  FL_TUNE_CELL_SUMS = 2,
+  FL_TUNE_GRAPHS = 3,
+  FL_TUNE_SORT_PASSES = 4,
+  FL_TUNE_WALK_BLOCKS = 5,
+  FL_TUNE_COLLIDE_CELL = 6
+};
 enum { FL_CELLS_AUTO = 0, FL_CELLS_FP64_TOP = 1, FL_CELLS_FP32 = 2 };
 int32_t fl_set_tuning(fl_sim* sim, int32_t key, int32_t value);
+
+/* The autotuner (no reference counterpart: the reference's block sizes, digit widths and stack
+ * depths are constants). It times `ticks`-tick blocks of the current nodes and forces at the
+ * given alpha and decay under candidate values of FL_TUNE_SORT_PASSES, FL_TUNE_WALK_GROUP,
+ * FL_TUNE_WALK_BLOCKS and FL_TUNE_COLLIDE_CELL (those that the forces use), one knob at a time,
+ * keeps the fastest, and restores the state: positions, velocities and the tick count are as
+ * before the call. With a cache file (NULL: none) the result is stored under a key of the
+ * device's compute capability, the dimensions, log2 of the node count and the forces, and a
+ * later call with the same key applies it without timing. */
+typedef struct {
+  int32_t walk_group, sort_passes, walk_blocks, collide_cell;  /* the values chosen */
+  double ms_per_tick;  /* with them */
+  double ms_default;   /* with the defaults, timed the same way */
+  int32_t candidates;  /* configurations timed (0 when read from the cache) */
+  int32_t from_cache;
+} fl_tune_result;
+int32_t fl_autotune(fl_sim* sim, int32_t ticks, double alpha, double decay,
+                    const char* cache_path, fl_tune_result* out);
 
 /* The cudaStream_t every kernel of this simulation runs on. */
 int32_t fl_stream(fl_sim* sim, void** stream);
@@ -210,6 +241,12 @@ int32_t fl_batch_sync(fl_batch* b, float* pos4_out, float* vel4_out);
 /* FL_Q_LAUNCHES, FL_Q_TICKS, FL_Q_NODES, FL_Q_DEVICE_BYTES */
 int32_t fl_batch_query(fl_batch* b, int32_t what, int64_t* out);
 int32_t fl_batch_stream(fl_batch* b, void** stream);
+/* Tuning of a batch, as fl_set_tuning: FL_TUNE_GRAPHS, FL_TUNE_SORT_PASSES, FL_TUNE_WALK_BLOCKS. */
+int32_t fl_batch_set_tuning(fl_batch* b, int32_t key, int32_t value);
+/* fl_autotune for a batch: FL_TUNE_SORT_PASSES and FL_TUNE_WALK_BLOCKS, every graph at `alpha`;
+ * the key adds log2 of the graph count. */
+int32_t fl_batch_autotune(fl_batch* b, int32_t ticks, double alpha, const char* cache_path,
+                          fl_tune_result* out);
 
 /* ---- integer stages, exposed for bit-exact checks against a CPU rebuild ---- */
 
