@@ -104,8 +104,13 @@ struct fl_sim {
   cudaEvent_t ev_fork = nullptr, ev_tree = nullptr;
   std::string err;
   int32_t n = 0, ndim = 2;
-  DevMem pos, vel[2], fix, mask, red, errw;
+  DevMem pos, vel[2], fix, mask, errw;
   int cur = 0;
+  // the box and sums of the tick's starting positions: reds[red_cur]; the integrate of the tick
+  // before fills it (pre_valid) unless the positions changed since
+  DevMem reds[2];
+  int red_cur = 0;
+  bool pre_valid = false;
   std::vector<std::unique_ptr<Pass>> plan;
   uint32_t seed = 0, step = 0;
   int64_t ticks = 0, launches = 0;
@@ -117,7 +122,8 @@ struct fl_sim {
   std::vector<FlTick> htick;
   struct Block {
     int32_t count;
-    int cur_in, cur_out;
+    int cur_in, cur_out, red_in, red_out;
+    bool pre_in, pre_out;
     int64_t launches;
     bool captured;
     cudaGraphExec_t exec;
@@ -206,6 +212,7 @@ void drain_profile(fl_sim* s) {
 }
 
 float4* vel_cur(fl_sim* s) { return s->vel[s->cur].as<float4>(); }
+FlReduce* red_of(fl_sim* s) { return s->reds[s->red_cur].as<FlReduce>(); }
 float4* vel_next(fl_sim* s) { return s->vel[1 - s->cur].as<float4>(); }
 
 // Host-side CSR of the links (src/gpu/passes/link.js:65-101): per node, its links in link order;
@@ -474,11 +481,11 @@ void encode_tick(fl_sim* s, float alpha, float decay) {
     if (is_tree(p.get()) && n >= 2) tree_at_start = true;
   }
   const bool pre = fuse_center || tree_at_start;
-  if (pre) {
+  if (pre && !s->pre_valid) {  // else the last tick's integrate reduced these positions
     Scope sc(s, G_REDUCE);
-    cudaMemsetAsync(s->red.p, 0, sizeof(FlReduce), s->st);
-    fl_launch_reduce(s->pos.as<float4>(), n, s->ndim, tree_at_start, fuse_center,
-                     s->red.as<FlReduce>(), s->st);
+    cudaMemsetAsync(red_of(s), 0, sizeof(FlReduce), s->st);
+    fl_launch_reduce(s->pos.as<float4>(), n, s->ndim, tree_at_start, fuse_center, red_of(s),
+                     s->st);
     ++s->launches;
   }
   // the first tree before any centre force is built from the tick's starting positions, which
@@ -495,7 +502,7 @@ void encode_tick(fl_sim* s, float alpha, float decay) {
   if (early >= 0) {
     cudaEventRecord(s->ev_fork, s->st);
     cudaStreamWaitEvent(s->aux, s->ev_fork, 0);
-    encode_tree(s, plan[early].get(), s->red.as<FlReduce>(), s->aux);
+    encode_tree(s, plan[early].get(), red_of(s), s->aux);
     cudaEventRecord(s->ev_tree, s->aux);
   }
   bool before_center = true;
@@ -503,7 +510,7 @@ void encode_tick(fl_sim* s, float alpha, float decay) {
     Pass* p = plan[k].get();
     switch (p->type) {
       case FL_FORCE_MANYBODY:
-        encode_manybody(s, p, alpha, before_center && tree_at_start ? s->red.as<FlReduce>() : nullptr,
+        encode_manybody(s, p, alpha, before_center && tree_at_start ? red_of(s) : nullptr,
                         k == early);
         break;
       case FL_FORCE_LINK:
@@ -553,11 +560,16 @@ void encode_tick(fl_sim* s, float alpha, float decay) {
   {
     Scope sc(s, G_INTEGRATE);
     const Pass* c = fuse_center ? plan[np - 1].get() : nullptr;
+    // the next tick needs the same reduction of the positions this integrate writes
+    FlReduce* next = pre ? s->reds[1 - s->red_cur].as<FlReduce>() : nullptr;
+    if (next) cudaMemsetAsync(next, 0, sizeof(FlReduce), s->st);
     fl_launch_integrate(s->pos.as<float4>(), vel_cur(s), s->fix.as<float4>(),
-                        s->mask.as<uint32_t>(), n, s->ndim, decay,
-                        c ? s->red.as<FlReduce>() : nullptr, c ? c->d.x : 0, c ? c->d.y : 0,
-                        c ? c->d.z : 0, c ? c->d.strength : 0, s->st, nullptr, nullptr, s->tkp);
+                        s->mask.as<uint32_t>(), n, s->ndim, decay, c ? red_of(s) : nullptr,
+                        c ? c->d.x : 0, c ? c->d.y : 0, c ? c->d.z : 0, c ? c->d.strength : 0,
+                        s->st, nullptr, nullptr, s->tkp, next, tree_at_start, fuse_center);
     ++s->launches;
+    if (next) s->red_cur = 1 - s->red_cur;
+    s->pre_valid = next != nullptr;
   }
 }
 
@@ -633,7 +645,8 @@ int32_t fl_create(int32_t device, fl_sim** out) {
     if (s->aux) cudaStreamDestroy(s->aux);
     s->aux = nullptr;
   }
-  if ((e = s->red.alloc(sizeof(FlReduce))) != cudaSuccess) return cuda_fail(nullptr, e, "cudaMalloc");
+  for (auto& r : s->reds)
+    if ((e = r.alloc(sizeof(FlReduce))) != cudaSuccess) return cuda_fail(nullptr, e, "cudaMalloc");
   if ((e = s->errw.alloc(256)) != cudaSuccess) return cuda_fail(nullptr, e, "cudaMalloc");
   if ((e = cudaMemset(s->errw.p, 0, 256)) != cudaSuccess) return cuda_fail(nullptr, e, "cudaMemset");
   *out = s.release();
@@ -684,6 +697,7 @@ int32_t fl_set_nodes(fl_sim* s, int32_t n, int32_t ndim, const float* pos4, cons
   s->n = n;
   s->ndim = std::min(3, std::max(1, (int)ndim));
   s->cur = 0;
+  s->pre_valid = false;
   const size_t v4 = 16 * (size_t)std::max(n, 1);
   FL_CK(s, s->pos.alloc(v4));
   FL_CK(s, s->vel[0].alloc(v4));
@@ -707,9 +721,11 @@ int32_t fl_update_positions(fl_sim* s, int32_t first, int32_t count, const float
   if (rc) return rc;
   if (first < 0 || count < 0 || first + (int64_t)count > s->n || (count && !pos4))
     return fail(s, FL_E_ARG, "range out of bounds");
-  if (count)
+  if (count) {
     FL_CK(s, cudaMemcpyAsync(s->pos.as<float4>() + first, pos4, 16 * (size_t)count,
                              cudaMemcpyHostToDevice, s->st));
+    s->pre_valid = false;  // the next tick reduces the positions afresh
+  }
   FL_CK(s, cudaStreamSynchronize(s->st));
   return FL_OK;
 }
@@ -785,6 +801,7 @@ int32_t fl_set_forces(fl_sim* s, int32_t count, const fl_force_desc* descs) {
   if (sig != s->plan_sig) {
     clear_blocks(s);
     s->plan_sig = std::move(sig);
+    s->pre_valid = false;  // the reduction the new passes want may differ
   }
   return FL_OK;
 }
@@ -826,13 +843,16 @@ int32_t fl_enqueue(fl_sim* s, const double* alphas, int32_t count, double decay)
   fl_sim::Block* b = nullptr;
   if (s->use_graphs && !s->profiling)
     for (auto& x : s->blocks)
-      if (x.count == count && x.cur_in == s->cur) b = &x;
+      if (x.count == count && x.cur_in == s->cur && x.red_in == s->red_cur &&
+          x.pre_in == s->pre_valid)
+        b = &x;
   if (b && b->captured) {
     FL_CK(s, cudaGraphLaunch(b->exec, s->st));
-    s->cur = b->cur_out;
+    s->cur = b->cur_out, s->red_cur = b->red_out, s->pre_valid = b->pre_out;
     s->launches += b->launches;
   } else if (b) {
-    const int cur0 = s->cur;
+    const int cur0 = s->cur, red0 = s->red_cur;
+    const bool pre0 = s->pre_valid;
     const int64_t l0 = s->launches;
     cudaGraph_t g = nullptr;
     bool ok = cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
@@ -851,12 +871,13 @@ int32_t fl_enqueue(fl_sim* s, const double* alphas, int32_t count, double decay)
       cudaGetLastError();
       if (g) cudaGraphDestroy(g);
       s->use_graphs = false;
-      s->cur = cur0;
+      s->cur = cur0, s->red_cur = red0, s->pre_valid = pre0;
       s->launches = l0;
       encode();
     }
   } else {
-    const int cur0 = s->cur;
+    const int cur0 = s->cur, red0 = s->red_cur;
+    const bool pre0 = s->pre_valid;
     const int64_t l0 = s->launches;
     encode();
     if (s->use_graphs && !s->profiling) {
@@ -864,7 +885,8 @@ int32_t fl_enqueue(fl_sim* s, const double* alphas, int32_t count, double decay)
         if (s->blocks.front().captured) cudaGraphExecDestroy(s->blocks.front().exec);
         s->blocks.erase(s->blocks.begin());
       }
-      s->blocks.push_back(fl_sim::Block{count, cur0, s->cur, s->launches - l0, false, nullptr});
+      s->blocks.push_back(fl_sim::Block{count, cur0, s->cur, red0, s->red_cur, pre0, s->pre_valid,
+                                        s->launches - l0, false, nullptr});
     }
   }
   s->step += (uint32_t)count;
@@ -1000,6 +1022,7 @@ int32_t fl_autotune(fl_sim* s, int32_t ticks, double alpha, double decay,
     FL_CK(s, cudaMemcpyAsync(s->vel[0].p, snap.as<char>() + v4, v4, cudaMemcpyDeviceToDevice, s->st));
     s->cur = 0;
     s->step = step0;
+    s->pre_valid = false;
     return FL_OK;
   };
   cudaEvent_t e0 = nullptr, e1 = nullptr;

@@ -103,10 +103,13 @@ void fl_launch_center_apply(float4* pos, int n, int ndim, const FlReduce* red, d
 // v *= decay; p += v; pinned axes: p = fix, v = 0. When red != NULL, first shifts p by the
 // centre force of (cx, cy, cz, strength) computed from red->sum (the centre force fused).
 // In a batch (gr, gid non-null) each node takes its graph's decay and centre shift.
+// With `out` (not in a batch), the new positions are also reduced into it (box and/or sums, as
+// fl_launch_reduce): the next tick's reduction, fused.
 void fl_launch_integrate(float4* pos, float4* vel, const float4* fix, const uint32_t* mask, int n,
                          int ndim, float decay, const FlReduce* red, double cx, double cy,
                          double cz, double strength, cudaStream_t st, const FlGraph* gr = nullptr,
-                         const uint32_t* gid = nullptr, const FlTick* tk = nullptr);
+                         const uint32_t* gid = nullptr, const FlTick* tk = nullptr,
+                         FlReduce* out = nullptr, int want_box = 0, int want_sum = 0);
 void fl_launch_radial(const float4* pos, float4* vel, const float* radius, const float* strength,
                       int n, int ndim, float cx, float cy, float cz, float alpha, cudaStream_t st,
                       const FlTick* tk = nullptr);

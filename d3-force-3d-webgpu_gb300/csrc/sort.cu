@@ -279,16 +279,11 @@ __device__ void cta_sort_run(uint64_t* ka, uint32_t* va, uint64_t* kb, uint32_t*
   }
 }
 
-// counters[0]: blocks done; counters[1]: long runs recorded in longs[].
+// counters[1]: long runs recorded in longs[] (k_longruns sorts them and resets the count).
 __global__ void __launch_bounds__(kRunThreads) k_runfix(
-    uint64_t* __restrict__ kin, uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
-    uint32_t* __restrict__ vout, int64_t n, int lo_bit, int lo_sort, uint32_t* counters,
-    uint32_t* longs, uint32_t longs_cap) {
-  __shared__ uint32_t s_cnt[256];
-  __shared__ uint32_t s_w[(kRunThreads / 32) * 256];
-  __shared__ bool s_last;
-  // a grid-stride loop over few blocks: the fence and ticket each block takes at its end then
-  // cost little next to its work
+    const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
+    uint32_t* __restrict__ vout, int64_t n, int lo_sort, uint32_t* counters, uint32_t* longs,
+    uint32_t longs_cap) {
   for (int64_t i = (int64_t)blockIdx.x * kRunThreads + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * kRunThreads) {
     const uint64_t k = kin[i];
@@ -313,16 +308,20 @@ __global__ void __launch_bounds__(kRunThreads) k_runfix(
       }
     }
   }
-  // the last block to finish sorts the long runs
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) s_last = atomicAdd(&counters[0], 1u) == gridDim.x - 1;
-  __syncthreads();
-  if (!s_last) return;
-  __threadfence();
-  const uint32_t count = *((volatile uint32_t*)&counters[1]);
+}
+
+// One block: the long runs k_runfix recorded, each sorted on the bits below lo_sort (none, in
+// the common case: the block reads the count and returns). Leaves the count at zero.
+__global__ void __launch_bounds__(kRunThreads) k_longruns(
+    uint64_t* __restrict__ kin, uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
+    uint32_t* __restrict__ vout, int64_t n, int lo_bit, int lo_sort, uint32_t* counters,
+    const uint32_t* longs, uint32_t longs_cap) {
+  __shared__ uint32_t s_cnt[256];
+  __shared__ uint32_t s_w[(kRunThreads / 32) * 256];
+  const uint32_t count = counters[1];
+  if (count == 0) return;
   for (uint32_t r = 0; r < count && r < longs_cap; ++r) {
-    const int64_t s = *((volatile uint32_t*)&longs[r]);
+    const int64_t s = longs[r];
     const uint64_t h = kin[s] >> lo_sort;
     // the run's end: the first pair past s whose top bits differ
     __shared__ unsigned long long s_end;
@@ -337,6 +336,7 @@ __global__ void __launch_bounds__(kRunThreads) k_runfix(
     cta_sort_run(kin + s, vin + s, kout + s, vout + s, L, lo_bit, lo_sort, s_cnt, s_w);
     __syncthreads();
   }
+  if (threadIdx.x == 0) counters[1] = 0u;
 }
 
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -437,8 +437,11 @@ int fl_sort_runfix(const FlSortBufs* b, int64_t n, int lo_bit, int lo_sort, int 
   int64_t blocks = (n + kRunThreads - 1) / kRunThreads;
   if (blocks > 8 * (int64_t)fl_sms()) blocks = 8 * (int64_t)fl_sms();  // one full wave
   k_runfix<<<(unsigned)blocks, kRunThreads, 0, st>>>(b->keys[cur], b->vals[cur], b->keys[1 - cur],
-                                                     b->vals[1 - cur], n, lo_bit, lo_sort,
-                                                     b->counters + 8, b->longs, b->longs_cap);
-  ++*launches;
+                                                     b->vals[1 - cur], n, lo_sort, b->counters + 8,
+                                                     b->longs, b->longs_cap);
+  k_longruns<<<1, kRunThreads, 0, st>>>(b->keys[cur], b->vals[cur], b->keys[1 - cur],
+                                        b->vals[1 - cur], n, lo_bit, lo_sort, b->counters + 8,
+                                        b->longs, b->longs_cap);
+  *launches += 2;
   return 1 - cur;
 }

@@ -25,16 +25,12 @@ __device__ __forceinline__ void two_sum(float s, float x, float& t, float& e) {
 // its positions as an FP32 value plus an FP32 compensation (TwoSum: every rounding error is
 // kept), about 48 bits, and only the per-thread totals are added in FP64, which runs at a
 // small fraction of the FP32 rate on this part.
-__global__ void __launch_bounds__(kThreads) k_reduce(const float4* __restrict__ pos, int n,
-                                                     int ndim, int want_box, int want_sum,
-                                                     FlReduce* red) {
+// One thread's share of the reduction: box and compensated sums of the positions it saw.
+struct Partial {
   float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
   float fs[3] = {0.f, 0.f, 0.f}, fc[3] = {0.f, 0.f, 0.f};
-  // a few blocks, many positions per thread: the warp shuffles and atomics of the reduction
-  // are paid once per warp, not per handful of positions
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    float4 p = pos[i];
-    float c[3] = {p.x, p.y, p.z};
+  __device__ __forceinline__ void add(float4 p, int want_sum) {
+    const float c[3] = {p.x, p.y, p.z};
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       lo[k] = fminf(lo[k], c[k]);
@@ -46,6 +42,28 @@ __global__ void __launch_bounds__(kThreads) k_reduce(const float4* __restrict__ 
       }
     }
   }
+};
+
+// The block's partials into red: warp shuffles, then one atomic per axis and quantity.
+__device__ void flush_partial(const Partial& q, int ndim, int want_box, int want_sum,
+                              FlReduce* red);
+
+__global__ void __launch_bounds__(kThreads) k_reduce(const float4* __restrict__ pos, int n,
+                                                     int ndim, int want_box, int want_sum,
+                                                     FlReduce* red) {
+  Partial q;
+  // a few blocks, many positions per thread: the warp shuffles and atomics of the reduction
+  // are paid once per warp, not per handful of positions
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    q.add(pos[i], want_sum);
+  flush_partial(q, ndim, want_box, want_sum, red);
+}
+
+__device__ void flush_partial(const Partial& q, int ndim, int want_box, int want_sum,
+                              FlReduce* red) {
+  float lo[3] = {q.lo[0], q.lo[1], q.lo[2]}, hi[3] = {q.hi[0], q.hi[1], q.hi[2]};
+  const float* fs = q.fs;
+  const float* fc = q.fc;
   double sum[3] = {(double)fs[0] + (double)fc[0], (double)fs[1] + (double)fc[1],
                    (double)fs[2] + (double)fc[2]};
 #pragma unroll
@@ -152,6 +170,49 @@ __global__ void k_center_apply(float4* __restrict__ pos, int n, int ndim, const 
 // src/simulation.js:61-73 (and src/gpu/wgsl.js INTEGRATE): v *= decay; p += v; a pinned axis
 // takes p = fixed, v = 0. With the centre force fused (it was the last force), positions are
 // first shifted by it, as the reference applies it before integrating.
+// One node of k_integrate (no batch): decay, move, shift by the centre force, pins.
+__device__ __forceinline__ void integrate_node(float4& p, float4& v, const float4* __restrict__ fix,
+                                               uint32_t m, int i, int ndim, float decay,
+                                               bool shift, const float2* sh) {
+  if (shift) {
+    p.x = sub_shift(p.x, sh[0]);
+    p.y = sub_shift(p.y, sh[1]);
+    p.z = sub_shift(p.z, sh[2]);
+  }
+  v.x *= decay, v.y *= decay, v.z *= decay;
+  p.x += v.x, p.y += v.y, p.z += v.z;
+  if (m) {
+    float4 f = fix[i];
+    if (m & 1u) p.x = f.x, v.x = 0.f;
+    if (m & 2u) p.y = f.y, v.y = 0.f;
+    if (m & 4u) p.z = f.z, v.z = 0.f;
+  }
+  if (ndim < 3) p.z = 0.f, v.z = 0.f;
+  if (ndim < 2) p.y = 0.f, v.y = 0.f;
+  p.w = 0.f, v.w = 0.f;
+}
+
+// k_integrate that also reduces the new positions (box and/or sums) into `out`: the next
+// tick's k_reduce, fused. A grid-stride loop over few blocks, as k_reduce.
+__global__ void __launch_bounds__(kThreads) k_integrate_reduce(
+    float4* __restrict__ pos, float4* __restrict__ vel, const float4* __restrict__ fix,
+    const uint32_t* __restrict__ mask, int n, int ndim, float decay, const FlReduce* red,
+    double cx, double cy, double cz, double strength, const FlTick* __restrict__ tk,
+    FlReduce* out, int want_box, int want_sum) {
+  if (tk) decay = tk->decay;
+  float2 sh[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+  if (red) center_shift(red, n, ndim, cx, cy, cz, strength, sh);  // block-uniform branch
+  Partial q;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float4 p = pos[i], v = vel[i];
+    integrate_node(p, v, fix, mask[i], i, ndim, decay, red != nullptr, sh);
+    pos[i] = p;
+    vel[i] = v;
+    q.add(p, want_sum);
+  }
+  flush_partial(q, ndim, want_box, want_sum, out);
+}
+
 __global__ void __launch_bounds__(kThreads) k_integrate(float4* __restrict__ pos,
                                                         float4* __restrict__ vel,
                                                         const float4* __restrict__ fix,
@@ -173,23 +234,7 @@ __global__ void __launch_bounds__(kThreads) k_integrate(float4* __restrict__ pos
     decay = g.decay;
     sh[0] = g.shift[0], sh[1] = g.shift[1], sh[2] = g.shift[2];
   }
-  if (red || gr) {
-    p.x = sub_shift(p.x, sh[0]);
-    p.y = sub_shift(p.y, sh[1]);
-    p.z = sub_shift(p.z, sh[2]);
-  }
-  uint32_t m = mask[i];
-  v.x *= decay, v.y *= decay, v.z *= decay;
-  p.x += v.x, p.y += v.y, p.z += v.z;
-  if (m) {
-    float4 f = fix[i];
-    if (m & 1u) p.x = f.x, v.x = 0.f;
-    if (m & 2u) p.y = f.y, v.y = 0.f;
-    if (m & 4u) p.z = f.z, v.z = 0.f;
-  }
-  if (ndim < 3) p.z = 0.f, v.z = 0.f;
-  if (ndim < 2) p.y = 0.f, v.y = 0.f;
-  p.w = 0.f, v.w = 0.f;
+  integrate_node(p, v, fix, mask[i], i, ndim, decay, red || gr, sh);
   pos[i] = p;
   vel[i] = v;
 }
@@ -262,7 +307,15 @@ void fl_launch_breduce(const float4* pos, int n, int ndim, const uint32_t* gid, 
 void fl_launch_integrate(float4* pos, float4* vel, const float4* fix, const uint32_t* mask, int n,
                          int ndim, float decay, const FlReduce* red, double cx, double cy,
                          double cz, double strength, cudaStream_t st, const FlGraph* gr,
-                         const uint32_t* gid, const FlTick* tk) {
+                         const uint32_t* gid, const FlTick* tk, FlReduce* out, int want_box,
+                         int want_sum) {
+  if (out && !gr) {
+    int g = grid_for(n, kThreads * 4);
+    if (g > 4 * fl_sms()) g = 4 * fl_sms();
+    k_integrate_reduce<<<g, kThreads, 0, st>>>(pos, vel, fix, mask, n, ndim, decay, red, cx, cy,
+                                                cz, strength, tk, out, want_box, want_sum);
+    return;
+  }
   k_integrate<<<grid_for(n, kThreads), kThreads, 0, st>>>(pos, vel, fix, mask, n, ndim, decay, red,
                                                           cx, cy, cz, strength, gr, gid, tk);
 }

@@ -554,6 +554,7 @@ __device__ __forceinline__ void top_scan(T* tot, int nb, T zero) {
   const int per = (nb + kTopThreads - 1) / kTopThreads, a = threadIdx.x * per;
   const int b = a + per < nb ? a + per : nb;
   T sum = zero;
+#pragma unroll 8
   for (int t = a; t < b; ++t) sum = top_add(sum, tot[t]);
   T x = sum;  // inclusive scan within the warp
 #pragma unroll
@@ -576,6 +577,7 @@ __device__ __forceinline__ void top_scan(T* tot, int nb, T zero) {
   T run = warp ? s_warp[warp - 1] : zero;
   const T y = top_up(x, 1);  // exclusive within the warp: the previous lane's inclusive sum
   if (lane) run = top_add(run, y);
+#pragma unroll 8
   for (int t = a; t < b; ++t) {
     const T v = tot[t];
     tot[t] = run;
