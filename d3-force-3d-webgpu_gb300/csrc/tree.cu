@@ -89,13 +89,41 @@ __device__ __forceinline__ float damp(int ndim, int k) {
   return ldexpf(odd, e2 >> 1);
 }
 
+// Conversions between FP32 and 64-bit integers in integer arithmetic: the hardware's 64-bit
+// conversions issue on the FP64 pipe, a small fraction of the FP32 rate on this part.
+// f2ll_rn: round to nearest even, |v| < 2^63 (above 2^24 a float is an integer: its significand
+// shifted into place; below, the 32-bit conversion rounds).
+__device__ __forceinline__ long long f2ll_rn(float v) {
+  const uint32_t b = __float_as_uint(v);
+  const int e = (int)((b >> 23) & 255u) - 150;  // |v| = significand * 2^e
+  if (e < 0) return (long long)__float2int_rn(v);
+  const long long m = (long long)((b & 0x7fffffu) | 0x800000u) << e;
+  return (b >> 31) ? -m : m;
+}
+// ll2f_rn: the nearest float (ties to even) to a 64-bit integer.
+__device__ __forceinline__ float ll2f_rn(long long v) {
+  const unsigned long long u = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+  float r;
+  if (u < (1ull << 24)) {
+    r = (float)(uint32_t)u;
+  } else {
+    const int lz = __clzll((long long)u);
+    const unsigned long long w = u << lz;  // top bit at 63
+    uint32_t m = (uint32_t)(w >> 40);      // 24 significant bits
+    const unsigned long long rest = w & ((1ull << 40) - 1);
+    if (rest > (1ull << 39) || (rest == (1ull << 39) && (m & 1u))) ++m;
+    r = (float)m * __int_as_float((127 + 40 - lz) << 23);  // m <= 2^24, 2^(40 - lz): exact
+  }
+  return v < 0 ? -r : r;
+}
+
 // (x - o) * 2^F as an exact integer: x - o is rounded once in FP32 and its rounding error
 // recovered exactly (Knuth's TwoSum); both parts scale exactly by the power of two 2^F.
 __device__ __forceinline__ long long fx_offset(float x, float o, float scaleF) {
   const float s = x - o;
   const float bb = s - x;
   const float e = (x - (s - bb)) + (-o - bb);
-  const long long d = __float2ll_rn(s * scaleF) + __float2ll_rn(e * scaleF);
+  const long long d = f2ll_rn(s * scaleF) + f2ll_rn(e * scaleF);
   return d < 0 ? 0 : d;
 }
 // floor(W * D / 2^62) for W, D >= 0 (the 128-bit product's bits 62..125)
@@ -114,19 +142,25 @@ __device__ __forceinline__ float offset_scale(const float* cube) {
 // 4^-k as an exact float (k <= 31)
 __device__ __forceinline__ float pow4neg(uint32_t k) { return __int_as_float((127 - 2 * (int)k) << 23); }
 
+// floor((floor(x) - origin) * 2^e) for e < 0, in FP64 where every step is exact. Not inlined:
+// inlined, the compiler predicates it into the common path, which then pays its FP64 work.
+__device__ __noinline__ float cell_of_wide(float x, float origin, int e) {
+  return (float)floor(ldexp(floor((double)x) - (double)origin, e));
+}
+
 // The cell index of x at the finest level, floor((x - origin) * 2^e), in exact arithmetic:
 // e >= 0: floor(x * 2^e) and origin * 2^e are exact floats, and so is their difference, an
-// integer below 2^24; e < 0 (cubes wider than 2^LEVELS): in FP64, where every step is exact.
+// integer below 2^24; e < 0 (cubes wider than 2^LEVELS): cell_of_wide.
 __device__ __forceinline__ uint64_t cell_of(float x, float origin, int e, uint32_t top) {
   float c;
   if (e >= 0) {
     const float s = __int_as_float((e + 127) << 23);
     c = floorf(x * s) - origin * s;
   } else {
-    c = (float)floor(ldexp(floor((double)x) - (double)origin, e));
+    c = cell_of_wide(x, origin, e);
   }
   c = fminf(fmaxf(c, 0.f), (float)top);
-  return (uint64_t)c;
+  return (uint64_t)(uint32_t)c;  // below 2^24: a 32-bit conversion (the 64-bit one is FP64-pipe)
 }
 
 // d3 cover() of a bounding box (d3-octree): origin = floor(min); a power-of-two size doubled
@@ -381,7 +415,7 @@ __global__ void __launch_bounds__(kThreads) k_build(
       const int lD = (dmx >= bits ? L : dmx / ndim) + 1;  // the point's d3 leaf depth
       const float sF = offset_scale(cb);
       const long long W =
-          __float2ll_rn(fabsf(p.w * damp(ndim, lD)) * __int_as_float((fx_exp + 127) << 23));
+          f2ll_rn(fabsf(p.w * damp(ndim, lD)) * __int_as_float((fx_exp + 127) << 23));
       wrec = mk4(W, mulhi62(W, fx_offset(p.x, cb[0], sF)),
                  ndim > 1 ? mulhi62(W, fx_offset(p.y, cb[1], sF)) : 0,
                  ndim > 2 ? mulhi62(W, fx_offset(p.z, cb[2], sF)) : 0);
@@ -626,11 +660,12 @@ __global__ void __launch_bounds__(kThreads) k_cells_closed(int n, int ndim, floa
     // centroid = p0 + size * sum(w (u - u0)) / sum(w), about the range's first point p0: the
     // integer sums give the offsets exactly, so FP32 keeps the precision of the cell, not the cube
     const float4 p0 = leaf[a];
-    const float sF = offset_scale(cube), r = cube[3] / (float)W;
-    out.x = p0.x + (float)(hi.y - lo.y - mulhi62(W, fx_offset(p0.x, cube[0], sF))) * r;
-    out.y = ndim > 1 ? p0.y + (float)(hi.z - lo.z - mulhi62(W, fx_offset(p0.y, cube[1], sF))) * r : 0.f;
-    out.z = ndim > 2 ? p0.z + (float)(hi.w - lo.w - mulhi62(W, fx_offset(p0.z, cube[2], sF))) * r : 0.f;
-    out.w = sign * (float)W * __int_as_float((127 - fx_exp) << 23) * damp(ndim, -D);
+    const float fW = ll2f_rn(W);
+    const float sF = offset_scale(cube), r = cube[3] / fW;
+    out.x = p0.x + ll2f_rn(hi.y - lo.y - mulhi62(W, fx_offset(p0.x, cube[0], sF))) * r;
+    out.y = ndim > 1 ? p0.y + ll2f_rn(hi.z - lo.z - mulhi62(W, fx_offset(p0.y, cube[1], sF))) * r : 0.f;
+    out.z = ndim > 2 ? p0.z + ll2f_rn(hi.w - lo.w - mulhi62(W, fx_offset(p0.z, cube[2], sF))) * r : 0.f;
+    out.w = sign * fW * __int_as_float((127 - fx_exp) << 23) * damp(ndim, -D);
   } else {
     out = leaf[a];
     out.w = 0.f;
@@ -858,8 +893,12 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
   const int grp = lane / G, gl = lane % G, gbase = grp * G;
   const uint32_t gmask = G == 32 ? FL_FULL : (((1u << G) - 1u) << gbase);
   const uint32_t lanebit = 1u << lane;
-  // (size / 2^k)^2 / theta^2 = T0 * 4^-k, exactly (a power-of-two scaling)
-  const float T0 = BATCH ? 0.f : (float)((double)cube[3] * (double)cube[3] / theta2);
+  // (size / 2^k)^2 / theta^2 = T0 * 4^-k, exactly (a power-of-two scaling); the FP64 division
+  // once per block
+  __shared__ float s_T0;
+  if (!BATCH && threadIdx.x == 0) s_T0 = (float)((double)cube[3] * (double)cube[3] / theta2);
+  __syncthreads();
+  const float T0 = BATCH ? 0.f : s_T0;
   // l < dmin2  <=>  l <= the largest float below dmin2 (l >= 0)
   const float dmin_le = below(dmin2);
   const uint32_t slot_cap = 2u * (uint32_t)n + 1u;
