@@ -65,17 +65,20 @@ struct FlSortBufs {
   uint64_t* keys[2];
   uint32_t* vals[2];
   uint32_t* hist;      // [8][256] digit counts per pass
-  uint32_t* status;    // [8][tiles][256] look-back words
+  uint32_t* status;    // [passes][tiles][256] look-back words (tiles of this sort's tile size)
   uint32_t* counters;  // [kSortCounters]: tile tickets of the 8 passes, then the run fix-up's
   uint32_t* longs;     // [longs_cap] first positions of the runs the fix-up sorts in one block
   uint32_t longs_cap;
   int64_t cap;         // pairs the buffers hold
-  int64_t tiles_cap;
+  int64_t tiles_cap;   // tiles of kSortTileSmall pairs the look-back words have room for
 };
 constexpr int kSortCounters = 16;
-constexpr int kSortThreads = 512, kSortItems = 8;  // threads of a onesweep tile, pairs each
-constexpr int kSortTile = kSortThreads * kSortItems;  // pairs per onesweep tile
-int fl_sort_tile();  // kSortTile
+// A onesweep tile: kSortItems pairs per thread; 1024 threads, or 256 for up to kSortSmallMax
+// pairs (small sorts take more, shorter tiles: the time of a pass is that of one tile's steps).
+constexpr int kSortThreads = 1024, kSortThreadsSmall = 256, kSortItems = 8;
+constexpr int kSortTile = kSortThreads * kSortItems, kSortTileSmall = kSortThreadsSmall * kSortItems;
+constexpr int64_t kSortSmallMax = 131072;
+int fl_sort_tile(int64_t n);  // pairs per tile for a sort of n pairs
 int fl_sms();        // SMs of the current device (cached per process)
 size_t fl_sort_bytes(int64_t n);
 // Carve the buffers out of one allocation of fl_sort_bytes(n) bytes.

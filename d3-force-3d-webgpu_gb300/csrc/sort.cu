@@ -3,7 +3,8 @@
 // Replaces the reference's three-dispatch-per-digit sort (src/gpu/sort.js:4-20, 139-190) with
 // the GB300 form of Adinets & Merrill's "Onesweep" (2022): the digit histograms of every pass
 // come from one read of the keys (fused into the key producer where possible); each pass is one
-// kernel that ranks a tile of kSortTile keys by digit with warp match (__match_any_sync), publishes
+// kernel that ranks a tile of kSortTile keys by digit within each warp (eight ballots, one per digit
+// bit, give the lanes that share a lane's digit: cheaper here than the match instruction), publishes
 // the tile's digit counts, and takes its global offsets from a decoupled look-back over the
 // preceding tiles (bounded: a wait gives up after FL_SPIN_LIMIT polls and raises an error bit
 // instead of hanging); keys are then staged in shared memory in digit order and written out in
@@ -12,18 +13,17 @@
 
 namespace {
 
-constexpr int kThreads = kSortThreads;
-constexpr int kWarps = kThreads / 32;
 constexpr int kItems = kSortItems;
-constexpr int kTile = kSortTile;
 constexpr uint32_t kValMask = (1u << 30) - 1;
 constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagPre = 2u << 30;
-constexpr int kLook = 8;  // look-back words read per round (64 registers: two tiles per SM)
+constexpr int kLook = 8;  // look-back words read per round (within 64 registers)
 
 // Block-wide exclusive scan of one value per thread (kThreads); returns the exclusive prefix,
 // and the block total in *total.
+template <int kThreads>
 __device__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_warp, uint32_t* total) {
+  constexpr int kWarps = kThreads / 32;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t x = v;
 #pragma unroll
@@ -67,10 +67,23 @@ __global__ void __launch_bounds__(256) k_hist(const uint64_t* __restrict__ keys,
     if (sh[i]) atomicAdd(&hist[i], sh[i]);
 }
 
-__global__ void __launch_bounds__(kThreads, 2) k_onesweep(
+// The lanes of the warp whose digit equals this lane's (d < 256), or this lane alone (!valid).
+__device__ __forceinline__ uint32_t match_digit(uint32_t d, bool valid) {
+  uint32_t m = __ballot_sync(FL_FULL, valid);
+#pragma unroll
+  for (int b = 0; b < 8; ++b) {
+    const uint32_t v = __ballot_sync(FL_FULL, (d >> b) & 1u);
+    m &= ((d >> b) & 1u) ? v : ~v;
+  }
+  return valid ? m : (1u << (threadIdx.x & 31));
+}
+
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_onesweep(
     const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
     uint32_t* __restrict__ vout, int64_t n, int shift, const uint32_t* __restrict__ ghist,
     uint32_t* status, uint32_t* ticket, uint32_t* err) {
+  constexpr int kWarps = kThreads / 32, kTile = kThreads * kItems;
   extern __shared__ __align__(16) unsigned char smem[];
   uint64_t* sk = reinterpret_cast<uint64_t*>(smem);
   uint32_t* sv = reinterpret_cast<uint32_t*>(sk + kTile);
@@ -87,7 +100,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_onesweep(
   uint32_t total;
   // digit-wise phases: threads 0..255 take one digit each (a block of 256 or more threads)
   const bool dt = tid < 256;
-  const uint32_t gx = block_excl_scan(dt ? ghist[tid] : 0u, s_warp, &total);  // syncs inside
+  const uint32_t gx = block_excl_scan<kThreads>(dt ? ghist[tid] : 0u, s_warp, &total);  // syncs inside
   if (dt) s_gexcl[tid] = gx;
   const uint32_t tile = s_tile;
   const int64_t tbase = (int64_t)tile * kTile;
@@ -111,7 +124,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_onesweep(
   const uint32_t lt = fl::lanemask_lt();
 #pragma unroll
   for (int j = 0; j < kItems; ++j) {
-    uint32_t peers = __match_any_sync(FL_FULL, dig[j]);
+    uint32_t peers = match_digit(dig[j], dig[j] < 256u);
     int leader = 31 - __clz(peers);
     uint32_t before = 0;
     if (lane == leader && dig[j] < 256u) {
@@ -137,7 +150,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_onesweep(
     }
     fl::st_relaxed(mine, (tile == 0 ? kFlagPre : kFlagAgg) | run);
   }
-  const uint32_t tx = block_excl_scan(run, s_warp, &total);
+  const uint32_t tx = block_excl_scan<kThreads>(run, s_warp, &total);
   if (dt) s_texcl[d] = tx;
 
   uint32_t prefix = 0;
@@ -341,12 +354,30 @@ __global__ void __launch_bounds__(kRunThreads) k_longruns(
 
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-int64_t tiles_for(int64_t n) { return (n + kTile - 1) / kTile; }
+int64_t tiles_for(int64_t n) {
+  const int64_t t = fl_sort_tile(n);
+  return (n + t - 1) / t;
+}
+int64_t tiles_cap_for(int64_t cap) { return (cap + kSortTileSmall - 1) / kSortTileSmall; }
+
+template <int T>
+void launch_pass(const uint64_t* kin, const uint32_t* vin, uint64_t* kout, uint32_t* vout,
+                 int64_t n, int shift, const uint32_t* ghist, uint32_t* status, uint32_t* ticket,
+                 uint32_t* err, cudaStream_t st) {
+  static bool configured = false;
+  const size_t dyn = (size_t)T * kItems * 12;
+  if (!configured) {
+    cudaFuncSetAttribute(k_onesweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    configured = true;
+  }
+  const int64_t tiles = (n + T * kItems - 1) / (T * kItems);
+  k_onesweep<T><<<(int)tiles, T, dyn, st>>>(kin, vin, kout, vout, n, shift, ghist, status, ticket, err);
+}
 uint32_t longs_cap_for(int64_t n) { return (uint32_t)(n / (kRunShort + 1) + 1); }
 
 }  // namespace
 
-int fl_sort_tile() { return kTile; }
+int fl_sort_tile(int64_t n) { return n <= kSortSmallMax ? kSortTileSmall : kSortTile; }
 
 int fl_sms() {
   static int sms = 0;
@@ -359,20 +390,21 @@ int fl_sms() {
 }
 
 size_t fl_sort_bytes(int64_t n) {
-  int64_t cap = n > 0 ? n : 1, tiles = tiles_for(cap);
+  int64_t cap = n > 0 ? n : 1, tiles = tiles_cap_for(cap);
   return 2 * align256(8 * (size_t)cap) + 2 * align256(4 * (size_t)cap) + align256(8 * 256 * 4) +
-         align256(8 * (size_t)tiles * 256 * 4) + align256(kSortCounters * 4) +
+         align256(kSortCounters * 4) + align256(8 * (size_t)tiles * 256 * 4) +
          align256(4 * (size_t)longs_cap_for(cap));
 }
 
+// hist, counters and the look-back words in that order: one memset clears what a sort uses
 void fl_sort_carve(FlSortBufs* b, void* base, int64_t n) {
-  int64_t cap = n > 0 ? n : 1, tiles = tiles_for(cap);
+  int64_t cap = n > 0 ? n : 1, tiles = tiles_cap_for(cap);
   char* p = static_cast<char*>(base);
   for (int i = 0; i < 2; ++i) b->keys[i] = reinterpret_cast<uint64_t*>(p), p += align256(8 * (size_t)cap);
   for (int i = 0; i < 2; ++i) b->vals[i] = reinterpret_cast<uint32_t*>(p), p += align256(4 * (size_t)cap);
   b->hist = reinterpret_cast<uint32_t*>(p), p += align256(8 * 256 * 4);
-  b->status = reinterpret_cast<uint32_t*>(p), p += align256(8 * (size_t)tiles * 256 * 4);
   b->counters = reinterpret_cast<uint32_t*>(p), p += align256(kSortCounters * 4);
+  b->status = reinterpret_cast<uint32_t*>(p), p += align256(8 * (size_t)tiles * 256 * 4);
   b->longs = reinterpret_cast<uint32_t*>(p);
   b->longs_cap = longs_cap_for(cap);
   b->cap = cap;
@@ -380,17 +412,10 @@ void fl_sort_carve(FlSortBufs* b, void* base, int64_t n) {
 }
 
 void fl_sort_reset(const FlSortBufs* b, int64_t n, int passes, cudaStream_t st) {
-  int64_t tiles = tiles_for(n > 0 ? n : 1);
-  if (tiles == b->tiles_cap) {  // histogram, look-back words and tickets are contiguous
-    const char* a = reinterpret_cast<const char*>(b->hist);
-    const char* e = reinterpret_cast<const char*>(b->counters) + kSortCounters * 4;
-    cudaMemsetAsync(b->hist, 0, (size_t)(e - a), st);
-    return;
-  }
-  cudaMemsetAsync(b->hist, 0, 8 * 256 * 4, st);
-  cudaMemsetAsync(b->counters, 0, kSortCounters * 4, st);
-  for (int p = 0; p < passes; ++p)
-    cudaMemsetAsync(b->status + (size_t)p * b->tiles_cap * 256, 0, (size_t)tiles * 256 * 4, st);
+  const int64_t tiles = tiles_for(n > 0 ? n : 1);
+  const char* a = reinterpret_cast<const char*>(b->hist);
+  const char* e = reinterpret_cast<const char*>(b->status + (size_t)passes * tiles * 256);
+  cudaMemsetAsync(b->hist, 0, (size_t)(e - a), st);
 }
 
 void fl_sort_histogram(const FlSortBufs* b, int64_t n, int lo_bit, cudaStream_t st,
@@ -405,20 +430,19 @@ void fl_sort_histogram(const FlSortBufs* b, int64_t n, int lo_bit, cudaStream_t 
 
 int fl_sort_passes(const FlSortBufs* b, int64_t n, int lo_bit, uint32_t* err, cudaStream_t st,
                    int64_t* launches) {
-  static bool configured = false;
-  const size_t dyn = (size_t)kTile * 12;
-  if (!configured) {
-    cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
-    configured = true;
-  }
   int passes = (64 - lo_bit + 7) / 8;
   int cur = 0;
-  int64_t tiles = tiles_for(n);
   if (n <= 0) return 0;
+  const int64_t tiles = tiles_for(n);
   for (int p = 0; p < passes; ++p) {
-    k_onesweep<<<(int)tiles, kThreads, dyn, st>>>(
-        b->keys[cur], b->vals[cur], b->keys[1 - cur], b->vals[1 - cur], n, lo_bit + 8 * p,
-        b->hist + p * 256, b->status + (size_t)p * b->tiles_cap * 256, b->counters + p, err);
+    uint32_t* status = b->status + (size_t)p * tiles * 256;
+    if (fl_sort_tile(n) == kSortTileSmall)
+      launch_pass<kSortThreadsSmall>(b->keys[cur], b->vals[cur], b->keys[1 - cur], b->vals[1 - cur],
+                                     n, lo_bit + 8 * p, b->hist + p * 256, status, b->counters + p,
+                                     err, st);
+    else
+      launch_pass<kSortThreads>(b->keys[cur], b->vals[cur], b->keys[1 - cur], b->vals[1 - cur], n,
+                                lo_bit + 8 * p, b->hist + p * 256, status, b->counters + p, err, st);
     ++*launches;
     cur = 1 - cur;
   }

@@ -25,7 +25,7 @@ void fl_set_sim_free_error(const std::string& msg);  // engine.cu: the message o
 namespace {
 
 constexpr int64_t kMaxPairs = FL_SORT_NOALLOC_MAX_PAIRS;
-constexpr int64_t kTile = kSortTile;  // pairs per onesweep tile
+constexpr int64_t kTile = kSortTileSmall;  // the smallest onesweep tile: the most tiles
 constexpr int64_t kTiles = (kMaxPairs + kTile - 1) / kTile;
 constexpr size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
 constexpr size_t kErrOff = 0;

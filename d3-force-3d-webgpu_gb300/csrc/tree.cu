@@ -1045,28 +1045,27 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
       float v0 = pb.z, v1 = pb.w;
       const bool c0 = a0 && (l.x <= __uint_as_float(r0.y) || zp.x == 0.f);
       const bool c1 = a1 && (l.y <= __uint_as_float(r1.y) || zp.y == 0.f);
-      // a warp-uniform branch: the common path never executes the uncommon code, even predicated
-      if (__any_sync(FL_FULL, c0 || c1)) {
-        if (STATS && lane == 0) ++st_rare;
-        float2 dx = up2(DX), dy = up2(DY), dz = up2(DZ);
-        if (c0) {
-          const uint2 k0 = scold[j];
-          rare_case<NDIM>(k0.x, k0.y & 0xffu, r0.w, myT0, mydmin2, myid, perm, n, step, seed, v0, dx.x, dy.x, dz.x, l.x);
+      // one warp-uniform branch for everything but the common case (no lane opens either child,
+      // no uncommon case): the common path runs one vote, and never the code inside, even
+      // predicated
+      uint32_t om0 = 0, om1 = 0;
+      if (__any_sync(FL_FULL, c0 || c1 || o0 || o1)) {
+        if (__any_sync(FL_FULL, c0 || c1)) {
+          if (STATS && lane == 0) ++st_rare;
+          float2 dx = up2(DX), dy = up2(DY), dz = up2(DZ);
+          if (c0) {
+            const uint2 k0 = scold[j];
+            rare_case<NDIM>(k0.x, k0.y & 0xffu, r0.w, myT0, mydmin2, myid, perm, n, step, seed, v0, dx.x, dy.x, dz.x, l.x);
+          }
+          if (c1) {
+            const uint2 k1 = scold[j + 1];
+            rare_case<NDIM>(k1.x, k1.y & 0xffu, r1.w, myT0, mydmin2, myid, perm, n, step, seed, v1, dx.y, dy.y, dz.y, l.y);
+          }
+          DX = pk2(dx.x, dx.y), DY = pk2(dy.x, dy.y), DZ = pk2(dz.x, dz.y);
         }
-        if (c1) {
-          const uint2 k1 = scold[j + 1];
-          rare_case<NDIM>(k1.x, k1.y & 0xffu, r1.w, myT0, mydmin2, myid, perm, n, step, seed, v1, dx.y, dy.y, dz.y, l.y);
-        }
-        DX = pk2(dx.x, dx.y), DY = pk2(dy.x, dy.y), DZ = pk2(dz.x, dz.y);
-      }
-      const float2 w = up2(mul2(pk2(v0, v1), pk2(rcp_approx(l.x), rcp_approx(l.y))));
-      const uint64_t W = pk2(a0 ? w.x : 0.f, a1 ? w.y : 0.f);
-      AX = fma2(DX, W, AX);
-      if (NDIM > 1) AY = fma2(DY, W, AY);
-      if (NDIM > 2) AZ = fma2(DZ, W, AZ);
-      const uint32_t om0 = __ballot_sync(FL_FULL, o0) & gmask;
-      const uint32_t om1 = __ballot_sync(FL_FULL, o1) & gmask;
-      if (om0 | om1) {  // push the children some lanes must open (rare next to the tests)
+        om0 = __ballot_sync(FL_FULL, o0) & gmask;
+        om1 = __ballot_sync(FL_FULL, o1) & gmask;
+        // push the children some lanes of this group must open
         if (om0) {
           const uint2 k0 = scold[j];
           if (sp < kAll && gl == 0)
@@ -1085,6 +1084,11 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
         }
         if (STATS && sp > maxsp) maxsp = sp;
       }
+      const float2 w = up2(mul2(pk2(v0, v1), pk2(rcp_approx(l.x), rcp_approx(l.y))));
+      const uint64_t W = pk2(a0 ? w.x : 0.f, a1 ? w.y : 0.f);
+      AX = fma2(DX, W, AX);
+      if (NDIM > 1) AY = fma2(DY, W, AY);
+      if (NDIM > 2) AZ = fma2(DZ, W, AZ);
       if (STATS) {
         const uint32_t ap = __ballot_sync(FL_FULL, a0) & gmask, aq = __ballot_sync(FL_FULL, a1) & gmask;
         if (gl == 0) {

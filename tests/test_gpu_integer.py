@@ -13,7 +13,7 @@ from gpu_helpers import make_nodes
 
 pytestmark = pytest.mark.gpu
 
-TILE = 4096  # pairs per onesweep tile
+SMALL_TILE, TILE = 2048, 8192  # pairs per onesweep tile: up to 131,072 pairs, and above
 
 
 def lcg_keys(n, spread, seed=7):
@@ -28,7 +28,8 @@ def stable_order(keys):
     return np.argsort(keys, kind="stable")
 
 
-@pytest.mark.parametrize("n", [1, 2, 3, 255, 256, 257, TILE - 1, TILE, TILE + 1, 3 * TILE + 17, 100000])
+@pytest.mark.parametrize("n", [1, 2, 3, 255, 256, 257, SMALL_TILE - 1, SMALL_TILE, SMALL_TILE + 1,
+                               3 * SMALL_TILE + 17, 100000, 131072, 131073, 131072 + 3 * TILE + 5])
 def test_sort_random_32bit_keys(n):
     keys32 = lcg_keys(n, 1 << 32)
     keys = keys32 << np.uint64(32)
