@@ -84,9 +84,9 @@ __device__ __forceinline__ int levels_of(int ndim) { return ndim == 3 ? 21 : 24;
 // of sqrt(2), c^k = 2^(k (2 - DIMS) / 2), so it is an exact power of two, times sqrt(2) when the
 // exponent is odd.
 __device__ __forceinline__ float damp(int ndim, int k) {
-  const int e2 = k * (2 - ndim);
+  const int e2 = k * (2 - ndim);  // |e2| <= 2 * 24 (levels): the power of two is a normal float
   const float odd = (e2 & 1) ? 1.41421356237309515f : 1.f;
-  return ldexpf(odd, e2 >> 1);
+  return odd * __int_as_float((127 + (e2 >> 1)) << 23);
 }
 
 // Conversions between FP32 and 64-bit integers in integer arithmetic: the hardware's 64-bit
@@ -383,6 +383,9 @@ __device__ void block_prefix4(D4 v, D4* out, D4* tot, int i) {
 // [0, 1) the position in the d3 cube, as exact fixed point (scale 2^fx_exp, chosen so that no
 // sum over all points overflows), prefix-summed within the block. Integer sums are exact, and
 // cheap where FP64 is not.
+// PART: 1, the points (sorted leaves, records, their block prefix); 2, the internal nodes;
+// 0, both in one kernel.
+template <int PART>
 __global__ void __launch_bounds__(kThreads) k_build(
     const uint64_t* __restrict__ k, const uint32_t* __restrict__ perm,
     const float4* __restrict__ pos, const float* __restrict__ strength, int n, int ndim,
@@ -403,9 +406,9 @@ __global__ void __launch_bounds__(kThreads) k_build(
   const uint64_t ki = i < n ? k[i] : 0;
   const int up = i < n ? kdelta(k, lo, hi, ki, i, i + 1) : -1;
   const int dn = i < n ? kdelta(k, lo, hi, ki, i, i - 1) : -1;
-  if (i < n && lo == hi) leaf_parent[i] = kNoParent;  // alone in its graph: no tree
+  if (PART != 2 && i < n && lo == hi) leaf_parent[i] = kNoParent;  // alone in its graph: no tree
   D4 wrec = mk4(0, 0, 0, 0);
-  if (i < n) {
+  if (PART != 2 && i < n) {
     const uint32_t node = perm[i];
     float4 p = pos[node];
     p.w = strength[node];
@@ -421,9 +424,9 @@ __global__ void __launch_bounds__(kThreads) k_build(
                  ndim > 2 ? mulhi62(W, fx_offset(p.z, cb[2], sF)) : 0);
     }
   }
-  if (wsum)  // block-uniform
+  if (PART != 2 && wsum)  // block-uniform
     block_prefix4(wrec, wsum, wtot, i < n ? i : -1);
-  if (i >= n - 1) return;
+  if (PART == 1 || i >= n - 1) return;
   if (i == hi) {  // the last point of a graph: this internal index belongs to no tree
     left[i] = right[i] = kNoParent;
     range[2 * i] = range[2 * i + 1] = (uint32_t)i;
@@ -533,43 +536,6 @@ __global__ void __launch_bounds__(kThreads) k_frontier(
   head_of[t] = rec;
 }
 
-// Whether internal node i heads a d3 cell, and how many d3 children that cell has (its occupied
-// octants; at the deepest level, where the keys are equal, its points); the counts' exclusive
-// prefix within the block (first[]) and the block's total (ctot[]), for the slots.
-__global__ void __launch_bounds__(kThreads) k_heads(int n, int ndim,
-                                                    const uint32_t* __restrict__ parent,
-                                                    const uint32_t* __restrict__ range,
-                                                    const uint8_t* __restrict__ depth,
-                                                    const uint32_t* __restrict__ omask,
-                                                    uint32_t* __restrict__ count,
-                                                    uint32_t* __restrict__ first,
-                                                    uint32_t* __restrict__ ctot) {
-  __shared__ uint32_t s_warp[kThreads / 32];
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  uint32_t c = 0;
-  if (i < n - 1) {
-    const int D = depth[i];
-    if (D != kGapDepth) {
-      const uint32_t pa = parent[i];
-      const bool head = pa == (uint32_t)i || depth[pa] < D;  // a graph's root, or a deeper cell
-      if (head) c = D >= levels_of(ndim) ? range[2 * i + 1] - range[2 * i] + 1 : __popc(omask[i]);
-    }
-    count[i] = c;
-  }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t x = c;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    uint32_t y = __shfl_up_sync(FL_FULL, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) s_warp[warp] = x;
-  __syncthreads();
-  uint32_t before = 0;
-  for (int w = 0; w < warp; ++w) before += s_warp[w];
-  if (i < n - 1) first[i] = before + x - c;
-  if (threadIdx.x == kThreads - 1) ctot[blockIdx.x] = before + x;
-}
 
 // Exclusive prefix of the block totals, in place, by one block of kTopThreads: each thread sums
 // a run of consecutive totals, a warp-shuffle scan of the threads' sums (two levels) gives each
@@ -634,20 +600,15 @@ __device__ __forceinline__ uint32_t first_slot(const uint32_t* first, const uint
   return roots + first[x] + ctot[x >> 8];
 }
 
-// Cells from the prefix sums (strengths of one sign, `sign`): value and centroid of every head.
-__global__ void __launch_bounds__(kThreads) k_cells_closed(int n, int ndim, float sign,
-                                                           const uint32_t* __restrict__ range,
-                                                           const uint8_t* __restrict__ depth,
-                                                           const uint32_t* __restrict__ count,
-                                                           const D4* __restrict__ P,
-                                                           const D4* __restrict__ Ptot,
-                                                           const float4* __restrict__ leaf,
-                                                           const float* __restrict__ cube1,
-                                                           int fx_exp,
-                                                           float4* __restrict__ cell,
-                                                           FlSegs seg) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n - 1 || !count[i]) return;
+// The cell of head i from the prefix sums (strengths of one sign, `sign`): its centroid and its
+// value at its own depth, in closed form.
+__device__ __forceinline__ float4 closed_cell(uint32_t i, int ndim, float sign,
+                                              const uint32_t* __restrict__ range,
+                                              const uint8_t* __restrict__ depth,
+                                              const D4* __restrict__ P, const D4* __restrict__ Ptot,
+                                              const float4* __restrict__ leaf,
+                                              const float* __restrict__ cube1, int fx_exp,
+                                              const FlSegs& seg) {
   const uint32_t a = range[2 * i], b = range[2 * i + 1];
   const float* cube = seg.graphs ? seg.g[seg.gid_pos[a]].origin : cube1;
   // prefix sums: within the 256-point block, plus the blocks before it; exact in fixed point
@@ -670,7 +631,54 @@ __global__ void __launch_bounds__(kThreads) k_cells_closed(int n, int ndim, floa
     out = leaf[a];
     out.w = 0.f;
   }
-  cell[i] = out;
+  return out;
+}
+
+// Whether internal node i heads a d3 cell, and how many d3 children that cell has (its occupied
+// octants; at the deepest level, where the keys are equal, its points); the counts' exclusive
+// prefix within the block (first[]) and the block's total (ctot[]), for the slots. CLOSED (strengths
+// of one sign): a head's cell from the prefix sums too (closed_cell), into cell[].
+template <bool CLOSED>
+__global__ void __launch_bounds__(kThreads) k_heads(int n, int ndim,
+                                                    const uint32_t* __restrict__ parent,
+                                                    const uint32_t* __restrict__ range,
+                                                    const uint8_t* __restrict__ depth,
+                                                    const uint32_t* __restrict__ omask,
+                                                    uint32_t* __restrict__ count,
+                                                    uint32_t* __restrict__ first,
+                                                    uint32_t* __restrict__ ctot, float sign,
+                                                    const D4* __restrict__ P,
+                                                    const D4* __restrict__ Ptot,
+                                                    const float4* __restrict__ leaf,
+                                                    const float* __restrict__ cube, int fx_exp,
+                                                    float4* __restrict__ cell, FlSegs seg) {
+  __shared__ uint32_t s_warp[kThreads / 32];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t c = 0;
+  if (i < n - 1) {
+    const int D = depth[i];
+    if (D != kGapDepth) {
+      const uint32_t pa = parent[i];
+      const bool head = pa == (uint32_t)i || depth[pa] < D;  // a graph's root, or a deeper cell
+      if (head) c = D >= levels_of(ndim) ? range[2 * i + 1] - range[2 * i] + 1 : __popc(omask[i]);
+    }
+    count[i] = c;
+    if (CLOSED && c)
+      cell[i] = closed_cell((uint32_t)i, ndim, sign, range, depth, P, Ptot, leaf, cube, fx_exp, seg);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = c;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(FL_FULL, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  uint32_t before = 0;
+  for (int w = 0; w < warp; ++w) before += s_warp[w];
+  if (i < n - 1) first[i] = before + x - c;
+  if (threadIdx.x == kThreads - 1) ctot[blockIdx.x] = before + x;
 }
 
 // The recursion itself (strengths of both signs), bottom-up with arrival flags: the second
@@ -1274,11 +1282,16 @@ void fl_launch_build(const FlTreeBufs* t, const uint64_t* skeys, const uint32_t*
                      int fx_exp, cudaStream_t st, int64_t* launches, FlSegs segs) {
   const int n = t->n;
   const int nb = (n + kThreads - 1) / kThreads;
-  k_build<<<nb, kThreads, 0, st>>>(skeys, perm, pos, strength, n, t->ndim, t->left, t->right,
-                                   t->parent, t->leaf_parent, t->range, t->depth, t->leaf,
-                                   closed ? reinterpret_cast<D4*>(t->wsum) : nullptr,
-                                   reinterpret_cast<D4*>(t->wtiles), cube, fx_exp, segs);
-  ++*launches;
+  // two kernels: the internal nodes' searches are latency chains that want every warp an SM
+  // can hold, which the points' fixed-point records and prefix (more registers) would limit
+  k_build<1><<<nb, kThreads, 0, st>>>(skeys, perm, pos, strength, n, t->ndim, t->left, t->right,
+                                      t->parent, t->leaf_parent, t->range, t->depth, t->leaf,
+                                      closed ? reinterpret_cast<D4*>(t->wsum) : nullptr,
+                                      reinterpret_cast<D4*>(t->wtiles), cube, fx_exp, segs);
+  k_build<2><<<nb, kThreads, 0, st>>>(skeys, perm, pos, strength, n, t->ndim, t->left, t->right,
+                                      t->parent, t->leaf_parent, t->range, t->depth, t->leaf,
+                                      nullptr, nullptr, cube, fx_exp, segs);
+  *launches += 2;
   if (closed) {
     k_top4<<<1, kTopThreads, 0, st>>>(reinterpret_cast<D4*>(t->wtiles), nb);
     ++*launches;
@@ -1294,17 +1307,19 @@ void fl_launch_aggregate(const FlTreeBufs* t, const uint64_t* skeys, bool closed
   cudaMemsetAsync(t->omask, 0, 4 * (size_t)m, st);
   k_frontier<<<g2, kThreads, 0, st>>>(n, t->ndim, skeys, t->parent, t->leaf_parent, t->range,
                                       t->depth, t->omask, t->head_of, err);
-  k_heads<<<g, kThreads, 0, st>>>(n, t->ndim, t->parent, t->range, t->depth, t->omask, t->count,
-                                  t->first, ctot);
+  const D4* P = reinterpret_cast<const D4*>(t->wsum);
+  const D4* Ptot = reinterpret_cast<const D4*>(t->wtiles);
+  if (closed)
+    k_heads<true><<<g, kThreads, 0, st>>>(n, t->ndim, t->parent, t->range, t->depth, t->omask,
+                                          t->count, t->first, ctot, sign, P, Ptot, t->leaf, cube,
+                                          fx_exp, t->cell, segs);
+  else
+    k_heads<false><<<g, kThreads, 0, st>>>(n, t->ndim, t->parent, t->range, t->depth, t->omask,
+                                           t->count, t->first, ctot, sign, P, Ptot, t->leaf, cube,
+                                           fx_exp, t->cell, segs);
   k_top_u32<<<1, kTopThreads, 0, st>>>(ctot, g);
   *launches += 3;
-  if (closed) {
-    k_cells_closed<<<g, kThreads, 0, st>>>(n, t->ndim, sign, t->range, t->depth, t->count,
-                                           reinterpret_cast<const D4*>(t->wsum),
-                                           reinterpret_cast<const D4*>(t->wtiles), t->leaf, cube,
-                                           fx_exp, t->cell, segs);
-    ++*launches;
-  } else {
+  if (!closed) {
     cudaMemsetAsync(t->flag, 0, 4 * (size_t)m, st);
     k_cells_climb<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(
         n, t->ndim, t->left, t->right, t->parent, t->leaf_parent, t->range, t->depth, t->count,
