@@ -721,11 +721,10 @@ int32_t fl_update_positions(fl_sim* s, int32_t first, int32_t count, const float
   if (rc) return rc;
   if (first < 0 || count < 0 || first + (int64_t)count > s->n || (count && !pos4))
     return fail(s, FL_E_ARG, "range out of bounds");
-  if (count) {
+  if (count)
     FL_CK(s, cudaMemcpyAsync(s->pos.as<float4>() + first, pos4, 16 * (size_t)count,
                              cudaMemcpyHostToDevice, s->st));
-    s->pre_valid = false;  // the next tick reduces the positions afresh
-  }
+  s->pre_valid = false;  // the next tick reduces the positions afresh (count 0: written on the device)
   FL_CK(s, cudaStreamSynchronize(s->st));
   return FL_OK;
 }

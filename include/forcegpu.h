@@ -130,7 +130,10 @@ int32_t fl_sync(fl_sim* sim, float* pos4_out, float* vel4_out);
 int32_t fl_idle(fl_sim* sim);
 /* Whether queued work is still running (engine.busy, src/gpu/engine.js:393-396). */
 int32_t fl_busy(fl_sim* sim, int32_t* busy);
-/* Device pointers of the state (engine.buffers). */
+/* Device pointers of the state (engine.buffers), for reading (rendering): positions written
+ * through them are not seen by the next tick's bounding box and centre sums, which the last
+ * integrate already took; write positions with fl_update_positions, or call
+ * fl_update_positions(sim, 0, 0, NULL) after writing them on the device. */
 int32_t fl_buffers(fl_sim* sim, fl_buffer_info* out);
 
 /* ---- measurement (no reference counterpart: the reference times only with performance.now()
