@@ -419,7 +419,7 @@ def run_served(args):
     jobs = served_jobs(args.jobs, args.rate)
     work = copy.deepcopy(jobs)
     # the server, in real time: arrivals are offsets from the start
-    srv = LayoutServer(hbm_budget=96 << 30, block=50)
+    srv = LayoutServer(hbm_budget=96 << 30, block=50).warmup()
     clocks = Clocks()
     clocks.start()
     t0 = time.perf_counter()
@@ -434,7 +434,7 @@ def run_served(args):
     served = latency_summary(work)
     # serial plain solves, FIFO under the same arrivals: each job's service time measured alone
     serial = copy.deepcopy(jobs)
-    one = LayoutServer(hbm_budget=96 << 30, block=50, batching=False)
+    one = LayoutServer(hbm_budget=96 << 30, block=50, batching=False, plain_graphs=True).warmup()
     service = []
     for j in serial:
         j.arrival = None

@@ -39,6 +39,13 @@ struct Buf {
     else bytes = b ? b : 256;
     return e;
   }
+  // At least b bytes, keeping the buffer when it is large enough: freeing device memory waits
+  // for the whole device (every other stream's work too), so a batch rebuilt with fewer nodes
+  // reuses its buffers, and one that grows takes half as much again as it needs.
+  cudaError_t reserve(size_t b) {
+    if (p && b <= bytes) return cudaSuccess;
+    return alloc(b + b / 2);
+  }
   template <typename T>
   T* as() const {
     return static_cast<T*>(p);
@@ -70,6 +77,7 @@ struct fl_batch {
   Buf tickbuf;
   int32_t tick_cap = 0;
   std::vector<FlTick> htick;
+  std::vector<int32_t> hoff;  // first node of each graph, and the total
   struct Block {
     int32_t count;
     int cur_in, cur_out;
@@ -305,41 +313,47 @@ int32_t fl_batch_set_graphs(fl_batch* b, int32_t ndim, int32_t graphs, const fl_
   }
   // device buffers
   const size_t N = (size_t)std::max<int64_t>(n, 1);
-  FB_CK(b, b->pos.alloc(16 * N));
-  FB_CK(b, b->vel[0].alloc(16 * N));
-  FB_CK(b, b->vel[1].alloc(16 * N));
-  FB_CK(b, b->fix.alloc(16 * N));
-  FB_CK(b, b->mask.alloc(4 * N));
-  FB_CK(b, b->gid.alloc(4 * N));
-  FB_CK(b, b->gid_pos.alloc(4 * N));
-  FB_CK(b, b->charge.alloc(4 * N));
-  FB_CK(b, b->off.alloc(4 * (size_t)(graphs + 1)));
-  FB_CK(b, b->prm.alloc(sizeof(FlBatchParams) * (size_t)graphs));
-  FB_CK(b, b->red.alloc(sizeof(FlReduce) * (size_t)graphs));
-  FB_CK(b, b->gr.alloc(sizeof(FlGraph) * (size_t)graphs));
-  FB_CK(b, b->row.alloc(4 * ((size_t)n + 1)));
-  FB_CK(b, b->entry.alloc(16 * (size_t)std::max<int64_t>(2 * m, 1)));
-  FB_CK(b, b->code.alloc(4 * (size_t)std::max<int64_t>(2 * m, 1)));
-  FB_CK(b, b->sort1.alloc(fl_sort_bytes(n)));
-  FB_CK(b, b->sort2.alloc(fl_sort_bytes(n)));
-  FB_CK(b, b->tree.alloc(fl_tree_bytes(n)));
+  FB_CK(b, b->pos.reserve(16 * N));
+  FB_CK(b, b->vel[0].reserve(16 * N));
+  FB_CK(b, b->vel[1].reserve(16 * N));
+  FB_CK(b, b->fix.reserve(16 * N));
+  FB_CK(b, b->mask.reserve(4 * N));
+  FB_CK(b, b->gid.reserve(4 * N));
+  FB_CK(b, b->gid_pos.reserve(4 * N));
+  FB_CK(b, b->charge.reserve(4 * N));
+  b->hoff = off;
+  FB_CK(b, b->off.reserve(4 * (size_t)(graphs + 1)));
+  FB_CK(b, b->prm.reserve(sizeof(FlBatchParams) * (size_t)graphs));
+  FB_CK(b, b->red.reserve(sizeof(FlReduce) * (size_t)graphs));
+  FB_CK(b, b->gr.reserve(sizeof(FlGraph) * (size_t)graphs));
+  FB_CK(b, b->row.reserve(4 * ((size_t)n + 1)));
+  FB_CK(b, b->entry.reserve(16 * (size_t)std::max<int64_t>(2 * m, 1)));
+  FB_CK(b, b->code.reserve(4 * (size_t)std::max<int64_t>(2 * m, 1)));
+  FB_CK(b, b->sort1.reserve(fl_sort_bytes(n)));
+  FB_CK(b, b->sort2.reserve(fl_sort_bytes(n)));
+  FB_CK(b, b->tree.reserve(fl_tree_bytes(n)));
   fl_sort_carve(&b->sb, b->sort1.p, n);
   fl_sort_carve(&b->sb2, b->sort2.p, n);
   fl_tree_carve(&b->tb, b->tree.p, n, ndim);
-  FB_CK(b, cudaMemcpy(b->pos.p, pos.data(), 16 * N, cudaMemcpyHostToDevice));
-  FB_CK(b, cudaMemcpy(b->vel[0].p, vel.data(), 16 * N, cudaMemcpyHostToDevice));
-  FB_CK(b, cudaMemset(b->vel[1].p, 0, 16 * N));
-  FB_CK(b, cudaMemset(b->fix.p, 0, 16 * N));
-  FB_CK(b, cudaMemset(b->mask.p, 0, 4 * N));
-  FB_CK(b, cudaMemcpy(b->gid.p, gid.data(), 4 * N, cudaMemcpyHostToDevice));
-  FB_CK(b, cudaMemcpy(b->charge.p, charge.data(), 4 * N, cudaMemcpyHostToDevice));
-  FB_CK(b, cudaMemcpy(b->off.p, off.data(), 4 * (size_t)(graphs + 1), cudaMemcpyHostToDevice));
-  FB_CK(b, cudaMemcpy(b->prm.p, prm.data(), sizeof(FlBatchParams) * (size_t)graphs, cudaMemcpyHostToDevice));
-  FB_CK(b, cudaMemcpy(b->row.p, row.data(), 4 * ((size_t)n + 1), cudaMemcpyHostToDevice));
+  // uploads on the batch's own stream (from pageable memory: staged before each call returns)
+  cudaStream_t st = b->st;
+  FB_CK(b, cudaMemcpyAsync(b->pos.p, pos.data(), 16 * N, cudaMemcpyHostToDevice, st));
+  FB_CK(b, cudaMemcpyAsync(b->vel[0].p, vel.data(), 16 * N, cudaMemcpyHostToDevice, st));
+  FB_CK(b, cudaMemsetAsync(b->vel[1].p, 0, 16 * N, st));
+  FB_CK(b, cudaMemsetAsync(b->fix.p, 0, 16 * N, st));
+  FB_CK(b, cudaMemsetAsync(b->mask.p, 0, 4 * N, st));
+  FB_CK(b, cudaMemcpyAsync(b->gid.p, gid.data(), 4 * N, cudaMemcpyHostToDevice, st));
+  FB_CK(b, cudaMemcpyAsync(b->charge.p, charge.data(), 4 * N, cudaMemcpyHostToDevice, st));
+  FB_CK(b, cudaMemcpyAsync(b->off.p, off.data(), 4 * (size_t)(graphs + 1), cudaMemcpyHostToDevice, st));
+  FB_CK(b, cudaMemcpyAsync(b->prm.p, prm.data(), sizeof(FlBatchParams) * (size_t)graphs,
+                           cudaMemcpyHostToDevice, st));
+  FB_CK(b, cudaMemcpyAsync(b->row.p, row.data(), 4 * ((size_t)n + 1), cudaMemcpyHostToDevice, st));
   if (m) {
-    FB_CK(b, cudaMemcpy(b->entry.p, entry.data(), 32 * (size_t)m, cudaMemcpyHostToDevice));
-    FB_CK(b, cudaMemcpy(b->code.p, code.data(), 8 * (size_t)m, cudaMemcpyHostToDevice));
+    FB_CK(b, cudaMemcpyAsync(b->entry.p, entry.data(), 32 * (size_t)m, cudaMemcpyHostToDevice, st));
+    FB_CK(b, cudaMemcpyAsync(b->code.p, code.data(), 8 * (size_t)m, cudaMemcpyHostToDevice, st));
   }
+  // the host vectors go out of scope at return: wait for the copies that read them
+  FB_CK(b, cudaStreamSynchronize(st));
   b->cur = 0;
   b->step = 0;
   return FL_OK;
@@ -544,6 +558,29 @@ int32_t fl_batch_autotune(fl_batch* b, int32_t ticks, double alpha, const char* 
   if (e != cudaSuccess) return bcuda(b, e, "cudaStreamSynchronize");
   *out = fl_tune_result{32, b->sort_passes, b->walk_blocks, 100, o.best_ms, o.default_ms,
                         o.candidates, o.cached ? 1 : 0};
+  return FL_OK;
+}
+
+int32_t fl_batch_read(fl_batch* b, int32_t first, int32_t count, float* pos4_out,
+                      float* vel4_out) {
+  int32_t rc = bcheck(b);
+  if (rc) return rc;
+  if (first < 0 || count < 0 || first + (int64_t)count > b->graphs)
+    return bfail(b, FL_E_ARG, "graph range out of bounds");
+  const int32_t a = count ? b->hoff[first] : 0, e = count ? b->hoff[first + count] : 0;
+  const size_t bytes = 16 * (size_t)(e - a);
+  if (bytes && pos4_out)
+    FB_CK(b, cudaMemcpyAsync(pos4_out, b->pos.as<float4>() + a, bytes, cudaMemcpyDeviceToHost, b->st));
+  if (bytes && vel4_out)
+    FB_CK(b, cudaMemcpyAsync(vel4_out, bvel(b) + a, bytes, cudaMemcpyDeviceToHost, b->st));
+  uint32_t w = 0;
+  FB_CK(b, cudaMemcpyAsync(&w, b->errw.p, 4, cudaMemcpyDeviceToHost, b->st));
+  FB_CK(b, cudaStreamSynchronize(b->st));
+  if (w) {
+    cudaMemsetAsync(b->errw.p, 0, 4, b->st);
+    if (w & FL_ERR_LOOKBACK) return bfail(b, FL_E_TIMEOUT, "a device-side look-back wait gave up");
+    return bfail(b, FL_E_OVERFLOW, "a tree was malformed or a walk overflowed");
+  }
   return FL_OK;
 }
 

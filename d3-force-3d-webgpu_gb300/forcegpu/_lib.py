@@ -28,7 +28,7 @@ EXPORTS = ["fl_create", "fl_destroy", "fl_last_error", "fl_fits", "fl_set_nodes"
            "fl_debug_tree", "fl_set_tuning", "fl_radix_sort_noalloc", "fl_batch_create",
            "fl_batch_destroy", "fl_batch_last_error", "fl_batch_set_graphs", "fl_batch_set_seed",
            "fl_batch_enqueue", "fl_batch_sync", "fl_batch_query", "fl_batch_stream",
-           "fl_autotune", "fl_batch_set_tuning", "fl_batch_autotune"]
+           "fl_autotune", "fl_batch_set_tuning", "fl_batch_autotune", "fl_batch_read"]
 SORT_NOALLOC_MAX_PAIRS = 262144  # FL_SORT_NOALLOC_MAX_PAIRS
 TUNE_WALK_GROUP, TUNE_CELL_SUMS, TUNE_GRAPHS = 1, 2, 3
 TUNE_SORT_PASSES, TUNE_WALK_BLOCKS, TUNE_COLLIDE_CELL = 4, 5, 6
@@ -136,6 +136,7 @@ def load():
         "fl_autotune": (I32, [P, I32, D, D, ctypes.c_char_p, ctypes.POINTER(TuneResult)]),
         "fl_batch_set_tuning": (I32, [P, I32, I32]),
         "fl_batch_autotune": (I32, [P, I32, D, ctypes.c_char_p, ctypes.POINTER(TuneResult)]),
+        "fl_batch_read": (I32, [P, I32, I32, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -148,6 +148,20 @@ class Batch:
         self._check(self.L.fl_batch_sync(self.h, pos.ctypes.data, vel.ctypes.data))
         return pos[:n], vel[:n]
 
+    def read(self, first, count=1):
+        """Wait, then the positions and velocities of graphs [first, first + count), float32
+        (n, 4) each (fl_batch_read: only those graphs' nodes cross to the host)."""
+        n = int(self.sizes[first:first + count].sum())
+        pos = np.empty((max(n, 1), 4), np.float32)
+        vel = np.empty((max(n, 1), 4), np.float32)
+        self._check(self.L.fl_batch_read(self.h, int(first), int(count), pos.ctypes.data,
+                                         vel.ctypes.data))
+        return pos[:n], vel[:n]
+
+    def wait(self):
+        """Wait for the queued ticks (and report a device-side error), reading nothing back."""
+        self._check(self.L.fl_batch_sync(self.h, None, None))
+
     def positions(self):
         """Wait, then each graph's positions, (n_g, ndim)."""
         pos, _ = self.sync()

@@ -30,7 +30,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from ._lib import Engine, desc_from_gpu
+from ._lib import TUNE_GRAPHS, Engine, desc_from_gpu
 from .batch import Batch, GraphSpec
 from .graphs import link_defaults
 
@@ -89,57 +89,87 @@ class Job:
 
 
 class _Lane:
-    """The batch of one dimensionality: running jobs, rebuilt between blocks."""
+    """The batch of one dimensionality. Jobs join at block boundaries (the batch is rebuilt from
+    the running jobs' current state plus the new ones). A job that finishes stays in the batch,
+    sitting every tick out, until the finished jobs hold `dead_share` of the batch's nodes or
+    another job joins: a rebuild reads every running job's state back, so it is not done for
+    each job that ends. Only a finished job's own nodes are read back when it ends."""
 
-    def __init__(self, ndim, device):
+    def __init__(self, ndim, device, dead_share=0.3):
         self.ndim = ndim
         self.batch = Batch(device)
-        self.jobs = []
-        self.dirty = False
+        self.jobs = []       # in the batch, in its order (finished ones included until a rebuild)
+        self.incoming = []   # admitted, waiting for the next block boundary
+        self.dead = 0        # nodes of finished jobs still in the batch
+        self.dead_share = dead_share
         self.pending = None  # alphas of the block in flight
+
+    def live(self):
+        return [j for j in self.jobs if j.done_ticks < j.ticks]
+
+    def busy(self):
+        return bool(self.incoming) or any(j.done_ticks < j.ticks for j in self.jobs)
 
     def spec(self, j):
         return GraphSpec(xyz=j.pos[:, :self.ndim], source=j.source, target=j.target,
                          theta=j.theta, velocity_decay=j.velocity_decay,
                          vel=j.vel[:, :self.ndim] if j.vel is not None else None)
 
-    def launch(self, block, seed):
-        if not self.jobs:
-            return
-        if self.dirty:
+    def _rebuild(self, seed):
+        live = self.live()
+        if live:  # the running jobs' state, from the device
+            pos, vel = self.batch.sync()
+            cuts = np.cumsum([j.n for j in self.jobs])[:-1]
+            for j, p, v in zip(self.jobs, np.split(pos, cuts), np.split(vel, cuts)):
+                if j.done_ticks < j.ticks:
+                    j.pos, j.vel = p[:, :3].astype(np.float64), v[:, :3].astype(np.float64)
+        self.jobs = live + self.incoming
+        self.incoming = []
+        self.dead = 0
+        if self.jobs:
             self.batch.set_graphs([self.spec(j) for j in self.jobs], ndim=self.ndim, seed=seed)
-            self.dirty = False
+
+    def launch(self, block, seed):
+        total = sum(j.n for j in self.jobs)
+        if self.incoming or (self.jobs and self.dead > self.dead_share * total):
+            self._rebuild(seed)
+        if not any(j.done_ticks < j.ticks for j in self.jobs):
+            return
         al = np.stack([j.next_alphas(block) for j in self.jobs], axis=1)
         self.batch.enqueue(al)
         self.pending = al
 
     def land(self, now):
-        """Wait for the block, update the jobs; returns the finished ones."""
+        """Wait for the block, update the jobs; returns the ones that finished in it."""
         if self.pending is None:
             return []
-        pos, vel = self.batch.sync()
-        cuts = np.cumsum([j.n for j in self.jobs])[:-1]
         done = []
-        for j, p, v, col in zip(self.jobs, np.split(pos, cuts), np.split(vel, cuts), self.pending.T):
+        ended = []
+        for g, (j, col) in enumerate(zip(self.jobs, self.pending.T)):
             ran = int((col >= 0).sum())
-            j.pos, j.vel = p[:, :3].astype(np.float64), v[:, :3].astype(np.float64)
-            if ran:
-                j.alpha = float(col[ran - 1])
+            if not ran:
+                continue
+            j.alpha = float(col[ran - 1])
             j.done_ticks += ran
             if j.done_ticks >= j.ticks:
+                ended.append((g, j))
+        if ended:
+            for g, j in ended:
+                p, _ = self.batch.read(g, 1)
                 j.result = p[:, :self.ndim].copy()
                 j.finished = now()
+                j.pos = j.vel = None
+                self.dead += j.n
                 done.append(j)
+        else:
+            self.batch.wait()
         self.pending = None
-        if done:
-            self.jobs = [j for j in self.jobs if j.done_ticks < j.ticks]
-            self.dirty = True
         return done
 
 
 class LayoutServer:
     def __init__(self, device=0, hbm_budget=64 << 30, block=50, seed=12345, clock=time.perf_counter,
-                 batching=True):
+                 batching=True, plain_graphs=False):
         self.device = device
         self.batching = batching  # False: every job on its own plain engine
         self.hbm_budget = hbm_budget
@@ -147,11 +177,37 @@ class LayoutServer:
         self.seed = seed
         self.now = clock
         self.queue = deque()
-        self.lanes = {}
+        # the batches of 2D and 3D jobs exist from the start (creating one loads its kernels)
+        self.lanes = {d: _Lane(d, device) for d in (2, 3)} if batching else {}
         self.plain = []  # (job, engine) with a collide force
+        # finished plain engines: freeing device memory waits for the whole device, so they are
+        # closed when nothing else is in flight (or at close())
+        self.retired = []
+        # a plain job runs a few blocks only: capturing each as a CUDA graph costs more than
+        # the launches it saves
+        self.plain_graphs = plain_graphs
         self.used = 0
         self.finished = []
         self._ids = 0
+
+    def warmup(self):
+        """Lay out two tiny jobs per dimensionality, with and without collide, outside any
+        measurement: the first launch of each kernel in a process loads it, which a server pays
+        once at start-up, not per request."""
+        from .graphs import benchmark_links, phyllotaxis
+        jobs = []
+        for dims in (2, 3):
+            for radii in (None, np.full(300, 2.0)):
+                src, dst = benchmark_links(300, 150, seed=1)
+                jobs.append(Job(xyz=phyllotaxis(300, dims)[:, :dims], source=src, target=dst,
+                                ticks=2 * self.block, radii=radii, arrival=self.now()))
+        for j in jobs:
+            self.submit(j)
+        self.run_until_idle()
+        mine = {id(j) for j in jobs}
+        self.finished = [j for j in self.finished if id(j) not in mine]
+        self._ids = 0
+        return self
 
     # --- requests ---
     def submit(self, job):
@@ -163,7 +219,7 @@ class LayoutServer:
         return job
 
     def busy(self):
-        return bool(self.queue or self.plain or any(l.jobs for l in self.lanes.values()))
+        return bool(self.queue or self.plain or any(l.busy() for l in self.lanes.values()))
 
     # --- scheduling ---
     def _admit(self):
@@ -182,8 +238,7 @@ class LayoutServer:
                 lane = self.lanes.get(j.ndim)
                 if lane is None:
                     lane = self.lanes[j.ndim] = _Lane(j.ndim, self.device)
-                lane.jobs.append(j)
-                lane.dirty = True
+                lane.incoming.append(j)
 
     def _start_plain(self, j):
         n = j.n
@@ -207,6 +262,8 @@ class LayoutServer:
                                            "iterations": 1}, 3, n))
         eng.set_forces(descs)
         eng.set_seed(self.seed)
+        if not self.plain_graphs:
+            eng.set_tuning(TUNE_GRAPHS, 0)
         self.plain.append((j, eng, descs))
 
     def step(self):
@@ -215,8 +272,7 @@ class LayoutServer:
         host while the batches wait); land the finished plain jobs and the batches' blocks.
         Returns the jobs finished in this round."""
         self._admit()
-        for lane in self.lanes.values():
-            lane.launch(self.block, self.seed)
+        # the plain jobs' blocks first: the GPU runs them while the host rebuilds a batch
         for j, eng, _ in self.plain:
             k = min(self.block, j.ticks - j.done_ticks)
             if k > 0:
@@ -224,6 +280,8 @@ class LayoutServer:
                 eng.enqueue(al, 1 - j.velocity_decay)
                 j.alpha = float(al[-1])
                 j.done_ticks += k
+        for lane in self.lanes.values():
+            lane.launch(self.block, self.seed)
         done = []
         still = []
         for j, eng, descs in self.plain:
@@ -231,7 +289,7 @@ class LayoutServer:
                 still.append((j, eng, descs))
                 continue
             pos, _ = eng.sync()
-            eng.close()
+            self.retired.append(eng)
             j.result = pos[:, :j.ndim].copy()
             j.finished = self.now()
             done.append(j)
@@ -241,13 +299,17 @@ class LayoutServer:
         for j in done:
             self.used -= j.footprint
         self.finished += done
-        if not done and not any(l.jobs for l in self.lanes.values()) and self.plain == [] and self.queue:
+        lanes_busy = any(l.busy() for l in self.lanes.values())
+        if self.retired and not lanes_busy and not self.plain:
+            for eng in self.retired:
+                eng.close()
+            self.retired = []
+        if not done and not lanes_busy and self.plain == [] and self.queue:
             # nothing running: wait for the next arrival
             wait = self.queue[0].arrival - self.now()
             if wait > 0:
                 time.sleep(min(wait, 0.05))
-        elif not any(l.jobs for l in self.lanes.values()) and self.plain and \
-                all(j.done_ticks >= j.ticks for j, _, _ in self.plain):
+        elif not lanes_busy and self.plain and all(j.done_ticks >= j.ticks for j, _, _ in self.plain):
             time.sleep(0.0005)  # only queued plain work left: poll gently
         return done
 
@@ -261,7 +323,9 @@ class LayoutServer:
             lane.batch.close()
         for _, eng, _ in self.plain:
             eng.close()
-        self.lanes, self.plain = {}, []
+        for eng in self.retired:
+            eng.close()
+        self.lanes, self.plain, self.retired = {}, [], []
 
 
 def latency_summary(jobs):

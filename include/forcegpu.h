@@ -241,6 +241,10 @@ int32_t fl_batch_enqueue(fl_batch* b, const double* alphas, int32_t ticks);
 /* Wait, then copy the concatenated positions / velocities (4 floats per node; either may be
  * NULL). Reports a device-side error raised since the previous sync. */
 int32_t fl_batch_sync(fl_batch* b, float* pos4_out, float* vel4_out);
+/* Wait, then read back the positions and velocities (float4 per node) of graphs
+ * [first, first + count) only; NULL outputs are skipped. */
+int32_t fl_batch_read(fl_batch* b, int32_t first, int32_t count, float* pos4_out,
+                      float* vel4_out);
 /* FL_Q_LAUNCHES, FL_Q_TICKS, FL_Q_NODES, FL_Q_DEVICE_BYTES */
 int32_t fl_batch_query(fl_batch* b, int32_t what, int64_t* out);
 int32_t fl_batch_stream(fl_batch* b, void** stream);
