@@ -8,7 +8,7 @@ import pytest
 
 from forcegpu import (forceCenter, forceCollide, forceLink, forceManyBody, forceRadial, forceX,
                       forceY, forceZ)
-from forcegpu._lib import CELLS_FP32, CELLS_FP64_TOP, TUNE_CELL_SUMS
+from forcegpu._lib import CELLS_FP32, CELLS_FP64_TOP, TUNE_CELL_SUMS, TUNE_WALK_GROUP
 from gpu_helpers import assert_nodes_close, make_nodes, run_both, tree_outliers
 
 pytestmark = pytest.mark.gpu
@@ -128,6 +128,27 @@ def test_tree_theta(theta):
 def test_tree_strength_distance_min_max():
     r = run_both(3, 2000, 1, lambda: [("charge", forceManyBody().strength(lambda d, i, *a: -10 - i % 7)
                                        .distanceMin(3).distanceMax(60))])
+    assert_nodes_close(r["gpu"], r["cpu"], 3, rtol=1e-3, outliers=tree_outliers(2000))
+
+
+def _walk_group(group):
+    return lambda sim, _: sim._engine.eng.set_tuning(TUNE_WALK_GROUP, group)
+
+
+@pytest.mark.parametrize("group", [32, 16])
+def test_tree_walk_groups_distances_theta(group):
+    r = run_both(3, 2000, 2, lambda: [("charge", forceManyBody().theta(0.7)
+                                       .strength(lambda d, i, *a: -10 - i % 7)
+                                       .distanceMin(2).distanceMax(80))],
+                 setup=_walk_group(group))
+    assert_nodes_close(r["gpu"], r["cpu"], 3, rtol=1e-3, outliers=tree_outliers(2000))
+
+
+@pytest.mark.parametrize("group", [32, 16])
+def test_tree_walk_groups_mixed_signs(group):
+    r = run_both(3, 2000, 2, lambda: [("charge", forceManyBody().theta(0.7)
+                                       .strength(lambda d, i, *a: -20 if i % 4 else 12))],
+                 setup=_walk_group(group))
     assert_nodes_close(r["gpu"], r["cpu"], 3, rtol=1e-3, outliers=tree_outliers(2000))
 
 
