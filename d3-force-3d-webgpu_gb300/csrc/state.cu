@@ -96,37 +96,70 @@ __device__ void flush_partial(const Partial& q, int ndim, int want_box, int want
   }
 }
 
-// Per-graph bounding boxes and position sums of a batch, one node per thread. Nodes are grouped
-// by graph, so a warp's graph ids do not decrease along its lanes: each run of equal ids is
-// reduced toward its first lane (shuffles that stop at the run's end), which adds the run to
-// its graph's record.
+// Per-graph bounding boxes and position sums of a batch. Nodes are grouped by graph, so graph
+// ids do not decrease along the nodes: a block takes kBreduceItems * kThreads consecutive nodes;
+// in each of its warps every run of equal ids is reduced toward its first lane (shuffles that
+// stop at the run's end), which adds the run to the block's table of the graphs it covers
+// (shared-memory atomics); the table then goes to the graphs' records with one global atomic
+// per graph, axis and quantity. A run whose graph falls past the table (a block over many tiny
+// graphs) goes to its record directly.
+constexpr int kBreduceItems = 8, kBreduceSlots = 16;
 __global__ void __launch_bounds__(kThreads) k_breduce(const float4* __restrict__ pos, int n,
                                                       int ndim, const uint32_t* __restrict__ gid,
                                                       FlReduce* red) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ uint32_t s_lo[kBreduceSlots][3], s_hi[kBreduceSlots][3];
+  __shared__ double s_sum[kBreduceSlots][3];
   const int lane = threadIdx.x & 31;
-  const bool ok = i < n;
-  const uint32_t g = ok ? gid[i] : 0xffffffffu;
-  float4 p = ok ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-  float lo[3] = {p.x, p.y, p.z}, hi[3] = {p.x, p.y, p.z}, sm[3] = {p.x, p.y, p.z};
+  const int64_t first = (int64_t)blockIdx.x * kThreads * kBreduceItems;
+  const uint32_t g0 = gid[first < n ? first : n - 1];
+  for (int i = threadIdx.x; i < kBreduceSlots * 3; i += kThreads) {
+    (&s_lo[0][0])[i] = 0u, (&s_hi[0][0])[i] = 0u, (&s_sum[0][0])[i] = 0.0;
+  }
+  __syncthreads();
+  for (int it = 0; it < kBreduceItems; ++it) {
+    const int64_t i = first + (int64_t)it * kThreads + threadIdx.x;
+    const bool ok = i < n;
+    const uint32_t g = ok ? gid[i] : 0xffffffffu;
+    float4 p = ok ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float lo[3] = {p.x, p.y, p.z}, hi[3] = {p.x, p.y, p.z}, sm[3] = {p.x, p.y, p.z};
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t go = __shfl_down_sync(FL_FULL, g, o);
-    const bool same = lane + o < 32 && go == g;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t go = __shfl_down_sync(FL_FULL, g, o);
+      const bool same = lane + o < 32 && go == g;
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const float a = __shfl_down_sync(FL_FULL, lo[k], o), b = __shfl_down_sync(FL_FULL, hi[k], o),
-                  c = __shfl_down_sync(FL_FULL, sm[k], o);
-      if (same) lo[k] = fminf(lo[k], a), hi[k] = fmaxf(hi[k], b), sm[k] += c;
+      for (int k = 0; k < 3; ++k) {
+        const float a = __shfl_down_sync(FL_FULL, lo[k], o), b = __shfl_down_sync(FL_FULL, hi[k], o),
+                    c = __shfl_down_sync(FL_FULL, sm[k], o);
+        if (same) lo[k] = fminf(lo[k], a), hi[k] = fmaxf(hi[k], b), sm[k] += c;
+      }
+    }
+    const uint32_t gp = __shfl_up_sync(FL_FULL, g, 1);
+    if (!ok || (lane > 0 && gp == g)) continue;  // not the first lane of its run
+    const uint32_t slot = g - g0;
+    if (slot < (uint32_t)kBreduceSlots) {
+      for (int k = 0; k < ndim; ++k) {
+        atomicMax(&s_lo[slot][k], ~fl::ordered(lo[k]));
+        atomicMax(&s_hi[slot][k], fl::ordered(hi[k]));
+        atomicAdd(&s_sum[slot][k], (double)sm[k]);
+      }
+    } else {
+      FlReduce* r = red + g;
+      for (int k = 0; k < ndim; ++k) {
+        atomicMax(&r->lo[k], ~fl::ordered(lo[k]));
+        atomicMax(&r->hi[k], fl::ordered(hi[k]));
+        atomicAdd(&r->sum[k], (double)sm[k]);
+      }
     }
   }
-  const uint32_t gp = __shfl_up_sync(FL_FULL, g, 1);
-  if (!ok || (lane > 0 && gp == g)) return;  // not the first lane of its run
-  FlReduce* r = red + g;
-  for (int k = 0; k < ndim; ++k) {
-    atomicMax(&r->lo[k], ~fl::ordered(lo[k]));
-    atomicMax(&r->hi[k], fl::ordered(hi[k]));
-    atomicAdd(&r->sum[k], (double)sm[k]);
+  __syncthreads();
+  // the table: one thread per graph and axis (a zero low word: no run of that graph here)
+  for (int t = threadIdx.x; t < kBreduceSlots * 3; t += kThreads) {
+    const int slot = t / 3, k = t % 3;
+    if (k >= ndim || s_lo[slot][k] == 0u) continue;
+    FlReduce* r = red + (g0 + slot);
+    atomicMax(&r->lo[k], s_lo[slot][k]);
+    atomicMax(&r->hi[k], s_hi[slot][k]);
+    atomicAdd(&r->sum[k], s_sum[slot][k]);
   }
 }
 
@@ -301,7 +334,8 @@ void fl_launch_center_apply(float4* pos, int n, int ndim, const FlReduce* red, d
 
 void fl_launch_breduce(const float4* pos, int n, int ndim, const uint32_t* gid, FlReduce* red,
                        cudaStream_t st) {
-  k_breduce<<<grid_for(n, kThreads), kThreads, 0, st>>>(pos, n, ndim, gid, red);
+  if (n <= 0) return;
+  k_breduce<<<grid_for(n, kThreads * kBreduceItems), kThreads, 0, st>>>(pos, n, ndim, gid, red);
 }
 
 void fl_launch_integrate(float4* pos, float4* vel, const float4* fix, const uint32_t* mask, int n,
