@@ -155,7 +155,8 @@ void encode_batch_tick(fl_batch* b, const double* alpha, const FlTick* tk) {
     int r = fl_sort_passes(&b->sb, n, lo_sort, err, st, &b->launches);
     r = fl_sort_runfix(&b->sb, n, lo_bit, lo_sort, r, st, &b->launches);
     fl_sort_reset(&b->sb2, n, 2, st);
-    fl_launch_bgidkey(n, b->sb.vals[r], gid, b->sb2.keys[0], b->sb2.vals[0], b->sb2.hist, st);
+    fl_launch_bgidkey(n, b->sb.vals[r], gid, b->off.as<int32_t>(), G, b->sb2.keys[0],
+                      b->sb2.vals[0], b->sb2.hist, st);
     const int r2 = fl_sort_passes(&b->sb2, n, 48, err, st, &b->launches);
     uint64_t* skeys = b->sb.keys[1 - r];
     uint32_t* perm = b->sb.vals[1 - r];

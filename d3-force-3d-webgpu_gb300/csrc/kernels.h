@@ -51,8 +51,8 @@ void fl_launch_bgraph(int graphs, int ndim, const int32_t* off, const FlReduce* 
                       const FlBatchParams* prm, const double* alpha, FlGraph* gr, cudaStream_t st);
 void fl_launch_bmorton(const float4* pos, int n, int ndim, const uint32_t* gid, const FlGraph* gr,
                        uint64_t* keys, uint32_t* vals, uint32_t* hist, int lo_bit, cudaStream_t st);
-void fl_launch_bgidkey(int n, const uint32_t* mperm, const uint32_t* gid, uint64_t* keys,
-                       uint32_t* vals, uint32_t* hist, cudaStream_t st);
+void fl_launch_bgidkey(int n, const uint32_t* mperm, const uint32_t* gid, const int32_t* off,
+                       int graphs, uint64_t* keys, uint32_t* vals, uint32_t* hist, cudaStream_t st);
 void fl_launch_bgather(int n, const uint32_t* order2, const uint64_t* mkeys, const uint32_t* mperm,
                        const uint32_t* gid, uint64_t* skeys, uint32_t* perm, uint32_t* gid_pos,
                        cudaStream_t st);

@@ -298,13 +298,30 @@ __global__ void __launch_bounds__(kThreads) k_bmorton(const float4* __restrict__
 
 // The second sort's input: the graph of each point in Morton order, in key bits [48, 64), and
 // the point's Morton-order position; with the histograms of those two digits.
+// The graph of node `node`: the last g with off[g] <= node (graph offsets in shared memory).
+__device__ __forceinline__ uint32_t graph_of(const int32_t* s_off, int graphs, uint32_t node) {
+  int lo = 0, hi = graphs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if ((uint32_t)s_off[mid] <= node) lo = mid;
+    else hi = mid - 1;
+  }
+  return (uint32_t)lo;
+}
+constexpr int kGidSearchMax = 8192;  // graphs whose offsets the key kernel searches in shared memory
+
 __global__ void __launch_bounds__(kThreads) k_bgidkey(int n, const uint32_t* __restrict__ mperm,
                                                       const uint32_t* __restrict__ gid,
+                                                      const int32_t* __restrict__ off, int graphs,
                                                       uint64_t* __restrict__ keys,
                                                       uint32_t* __restrict__ vals,
                                                       uint32_t* __restrict__ hist) {
   __shared__ uint32_t sh[2 * 256];
+  __shared__ int32_t s_off[kGidSearchMax];
+  const bool search = graphs <= kGidSearchMax;
   for (int i = threadIdx.x; i < 2 * 256; i += blockDim.x) sh[i] = 0;
+  if (search)
+    for (int i = threadIdx.x; i < graphs; i += blockDim.x) s_off[i] = off[i];
   __syncthreads();
   const int stride = gridDim.x * blockDim.x;
   for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
@@ -312,7 +329,9 @@ __global__ void __launch_bounds__(kThreads) k_bgidkey(int n, const uint32_t* __r
     const bool ok = i < n;
     uint64_t key = 0;
     if (ok) {
-      key = (uint64_t)gid[mperm[i]] << 48;
+      // a node's graph: from the offsets (a search in shared memory) rather than a random read
+      const uint32_t node = mperm[i];
+      key = (uint64_t)(search ? graph_of(s_off, graphs, node) : gid[node]) << 48;
       keys[i] = key;
       vals[i] = (uint32_t)i;
     }
@@ -338,7 +357,8 @@ __global__ void __launch_bounds__(kThreads) k_bgather(int n, const uint32_t* __r
   const uint32_t node = mperm[v];
   skeys[j] = mkeys[v];
   perm[j] = node;
-  gid_pos[j] = gid[node];
+  // graph g's points take sorted positions [off[g], off[g + 1]), the same range its nodes have
+  gid_pos[j] = gid[j];
 }
 
 // Common prefix of sorted keys i and j (index tie-break), -1 outside [lo, hi] (one graph's range)
@@ -1424,12 +1444,12 @@ void fl_launch_bmorton(const float4* pos, int n, int ndim, const uint32_t* gid, 
   k_bmorton<<<g, kThreads, 0, st>>>(pos, n, ndim, gid, gr, keys, vals, hist, lo_bit);
 }
 
-void fl_launch_bgidkey(int n, const uint32_t* mperm, const uint32_t* gid, uint64_t* keys,
-                       uint32_t* vals, uint32_t* hist, cudaStream_t st) {
+void fl_launch_bgidkey(int n, const uint32_t* mperm, const uint32_t* gid, const int32_t* off,
+                       int graphs, uint64_t* keys, uint32_t* vals, uint32_t* hist, cudaStream_t st) {
   int g = (n + kThreads - 1) / kThreads;
-  if (g > 2 * 152) g = 2 * 152;
+  if (g > 4 * fl_sms()) g = 4 * fl_sms();
   if (g < 1) g = 1;
-  k_bgidkey<<<g, kThreads, 0, st>>>(n, mperm, gid, keys, vals, hist);
+  k_bgidkey<<<g, kThreads, 0, st>>>(n, mperm, gid, off, graphs, keys, vals, hist);
 }
 
 void fl_launch_bgather(int n, const uint32_t* order2, const uint64_t* mkeys, const uint32_t* mperm,
