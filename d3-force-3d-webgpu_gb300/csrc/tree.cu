@@ -1055,7 +1055,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
       stest[gl] = make_uint4(0u, 0u, 0u, 0u);
     }
     __syncwarp();
-#pragma unroll 2
+#pragma unroll 4
     for (int j = 0; j < jmax; j += 2) {  // two children per round: independent work to overlap
       const float4 pa = spair[j], pb = spair[j + 1];
       const uint4 r0 = stest[j], r1 = stest[j + 1];
