@@ -102,6 +102,10 @@ struct fl_sim {
   // and so overlaps with the forces before it; joined before the walk
   cudaStream_t aux = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_tree = nullptr;
+  // a third stream for the tree's internal nodes and octant masks, which need only the sorted
+  // keys: they run beside the sorted points' records, joined before the cells
+  cudaStream_t aux2 = nullptr;
+  cudaEvent_t ev_fork2 = nullptr, ev_nodes = nullptr;
   std::string err;
   int32_t n = 0, ndim = 2;
   DevMem pos, vel[2], fix, mask, errw;
@@ -388,6 +392,22 @@ void encode_tree(fl_sim* s, Pass* p, const FlReduce* box, cudaStream_t st) {
   // the closed form (exact fixed-point sums) when the strengths share one sign, unless a
   // recursion was asked for
   const bool closed = !p->mixed && s->cell_sums == FL_CELLS_AUTO;
+  const int fp64_depth = s->cell_sums == FL_CELLS_FP32 ? 0 : kRecursionFp64Depth;
+  if (s->aux2 && !s->profiling) {
+    // the internal nodes and the heads' octant masks on the third stream, beside the points
+    cudaEventRecord(s->ev_fork2, st);
+    cudaStreamWaitEvent(s->aux2, s->ev_fork2, 0);
+    fl_launch_build_nodes(t, p->sb.keys[r], p->sb.vals[r], s->pos.as<float4>(), strength,
+                          p->cube.as<float>(), p->fx_exp, s->aux2, &s->launches);
+    fl_launch_frontier(t, p->sb.keys[r], s->errw.as<uint32_t>(), s->aux2, &s->launches);
+    cudaEventRecord(s->ev_nodes, s->aux2);
+    fl_launch_build_points(t, p->sb.keys[r], p->sb.vals[r], s->pos.as<float4>(), strength,
+                           closed, p->cube.as<float>(), p->fx_exp, st, &s->launches);
+    cudaStreamWaitEvent(st, s->ev_nodes, 0);
+    fl_launch_cells(t, closed, p->sign, p->cube.as<float>(), p->fx_exp, fp64_depth,
+                    s->errw.as<uint32_t>(), st, &s->launches);
+    return;
+  }
   {
     Scope sc(s, G_BUILD, st);
     fl_launch_build(t, p->sb.keys[r], p->sb.vals[r], s->pos.as<float4>(), strength, closed,
@@ -396,8 +416,7 @@ void encode_tree(fl_sim* s, Pass* p, const FlReduce* box, cudaStream_t st) {
   {
     Scope sc(s, G_AGGREGATE, st);
     fl_launch_aggregate(t, p->sb.keys[r], closed, p->sign, p->cube.as<float>(), p->fx_exp,
-                        s->cell_sums == FL_CELLS_FP32 ? 0 : kRecursionFp64Depth,
-                        s->errw.as<uint32_t>(), st, &s->launches);
+                        fp64_depth, s->errw.as<uint32_t>(), st, &s->launches);
   }
 }
 
@@ -645,6 +664,13 @@ int32_t fl_create(int32_t device, fl_sim** out) {
     if (s->aux) cudaStreamDestroy(s->aux);
     s->aux = nullptr;
   }
+  if (cudaStreamCreateWithFlags(&s->aux2, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&s->ev_fork2, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&s->ev_nodes, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();  // no third stream: the tree's halves run one after the other
+    if (s->aux2) cudaStreamDestroy(s->aux2);
+    s->aux2 = nullptr;
+  }
   for (auto& r : s->reds)
     if ((e = r.alloc(sizeof(FlReduce))) != cudaSuccess) return cuda_fail(nullptr, e, "cudaMalloc");
   if ((e = s->errw.alloc(256)) != cudaSuccess) return cuda_fail(nullptr, e, "cudaMalloc");
@@ -660,14 +686,18 @@ int32_t fl_destroy(fl_sim* s) {
   for (auto& r : s->prof_pending) cudaEventDestroy(r.a), cudaEventDestroy(r.b);
   for (auto e : s->ev_pool) cudaEventDestroy(e);
   if (s->aux) cudaStreamSynchronize(s->aux);
+  if (s->aux2) cudaStreamSynchronize(s->aux2);
   clear_blocks(s);
   s->plan.clear();
-  cudaStream_t st = s->st, aux = s->aux;
+  cudaStream_t st = s->st, aux = s->aux, aux2 = s->aux2;
   if (s->ev_fork) cudaEventDestroy(s->ev_fork);
   if (s->ev_tree) cudaEventDestroy(s->ev_tree);
+  if (s->ev_fork2) cudaEventDestroy(s->ev_fork2);
+  if (s->ev_nodes) cudaEventDestroy(s->ev_nodes);
   delete s;  // frees the device buffers
   if (st) cudaStreamDestroy(st);
   if (aux) cudaStreamDestroy(aux);
+  if (aux2) cudaStreamDestroy(aux2);
   return FL_OK;
 }
 

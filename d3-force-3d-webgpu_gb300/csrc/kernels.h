@@ -176,6 +176,22 @@ void fl_launch_morton(const float4* pos, int n, int ndim, const FlReduce* red, u
                       cudaStream_t st);
 // Karras build + sorted leaves (position, strength) gather; with `closed`, the FP64 point
 // records of the closed-form cell sums.
+// The two halves of fl_launch_build, for streams of their own: the sorted points with their
+// fixed-point records (and the records' top prefix), and the Karras internal nodes.
+void fl_launch_build_points(const FlTreeBufs* t, const uint64_t* skeys, const uint32_t* perm,
+                            const float4* pos, const float* strength, bool closed,
+                            const float* cube, int fx_exp, cudaStream_t st, int64_t* launches,
+                            FlSegs segs = {});
+void fl_launch_build_nodes(const FlTreeBufs* t, const uint64_t* skeys, const uint32_t* perm,
+                           const float4* pos, const float* strength, const float* cube,
+                           int fx_exp, cudaStream_t st, int64_t* launches, FlSegs segs = {});
+// The halves of fl_launch_aggregate: the heads' octant masks (after the nodes), then the cells,
+// counts and child slots (after the points and the masks).
+void fl_launch_frontier(const FlTreeBufs* t, const uint64_t* skeys, uint32_t* err,
+                        cudaStream_t st, int64_t* launches);
+void fl_launch_cells(const FlTreeBufs* t, bool closed, float sign, const float* cube, int fx_exp,
+                     int fp64_depth, uint32_t* err, cudaStream_t st, int64_t* launches,
+                     FlSegs segs = {});
 void fl_launch_build(const FlTreeBufs* t, const uint64_t* skeys, const uint32_t* perm,
                      const float4* pos, const float* strength, bool closed, const float* cube,
                      int fx_exp, cudaStream_t st, int64_t* launches, FlSegs segs = FlSegs{});

@@ -1297,36 +1297,59 @@ int fl_fixed_exponent(int64_t n, double wmax) {
   return e < 0 ? 0 : e > 100 ? 100 : e;
 }
 
-void fl_launch_build(const FlTreeBufs* t, const uint64_t* skeys, const uint32_t* perm,
-                     const float4* pos, const float* strength, bool closed, const float* cube,
-                     int fx_exp, cudaStream_t st, int64_t* launches, FlSegs segs) {
+void fl_launch_build_points(const FlTreeBufs* t, const uint64_t* skeys, const uint32_t* perm,
+                            const float4* pos, const float* strength, bool closed,
+                            const float* cube, int fx_exp, cudaStream_t st, int64_t* launches,
+                            FlSegs segs) {
   const int n = t->n;
   const int nb = (n + kThreads - 1) / kThreads;
-  // two kernels: the internal nodes' searches are latency chains that want every warp an SM
-  // can hold, which the points' fixed-point records and prefix (more registers) would limit
   k_build<1><<<nb, kThreads, 0, st>>>(skeys, perm, pos, strength, n, t->ndim, t->left, t->right,
                                       t->parent, t->leaf_parent, t->range, t->depth, t->leaf,
                                       closed ? reinterpret_cast<D4*>(t->wsum) : nullptr,
                                       reinterpret_cast<D4*>(t->wtiles), cube, fx_exp, segs);
-  k_build<2><<<nb, kThreads, 0, st>>>(skeys, perm, pos, strength, n, t->ndim, t->left, t->right,
-                                      t->parent, t->leaf_parent, t->range, t->depth, t->leaf,
-                                      nullptr, nullptr, cube, fx_exp, segs);
-  *launches += 2;
+  ++*launches;
   if (closed) {
     k_top4<<<1, kTopThreads, 0, st>>>(reinterpret_cast<D4*>(t->wtiles), nb);
     ++*launches;
   }
 }
 
-void fl_launch_aggregate(const FlTreeBufs* t, const uint64_t* skeys, bool closed, float sign,
-                         const float* cube, int fx_exp, int fp64_depth, uint32_t* err,
-                         cudaStream_t st, int64_t* launches, FlSegs segs) {
+void fl_launch_build_nodes(const FlTreeBufs* t, const uint64_t* skeys, const uint32_t* perm,
+                           const float4* pos, const float* strength, const float* cube,
+                           int fx_exp, cudaStream_t st, int64_t* launches, FlSegs segs) {
+  const int n = t->n;
+  const int nb = (n + kThreads - 1) / kThreads;
+  k_build<2><<<nb, kThreads, 0, st>>>(skeys, perm, pos, strength, n, t->ndim, t->left, t->right,
+                                      t->parent, t->leaf_parent, t->range, t->depth, t->leaf,
+                                      nullptr, nullptr, cube, fx_exp, segs);
+  ++*launches;
+}
+
+void fl_launch_build(const FlTreeBufs* t, const uint64_t* skeys, const uint32_t* perm,
+                     const float4* pos, const float* strength, bool closed, const float* cube,
+                     int fx_exp, cudaStream_t st, int64_t* launches, FlSegs segs) {
+  // two kernels: the internal nodes' searches are latency chains that want every warp an SM
+  // can hold, which the points' fixed-point records and prefix (more registers) would limit
+  fl_launch_build_points(t, skeys, perm, pos, strength, closed, cube, fx_exp, st, launches, segs);
+  fl_launch_build_nodes(t, skeys, perm, pos, strength, cube, fx_exp, st, launches, segs);
+}
+
+void fl_launch_frontier(const FlTreeBufs* t, const uint64_t* skeys, uint32_t* err,
+                        cudaStream_t st, int64_t* launches) {
   const int n = t->n, m = n - 1;
-  const int g = (m + kThreads - 1) / kThreads, g2 = (2 * n - 1 + kThreads - 1) / kThreads;
-  uint32_t* ctot = static_cast<uint32_t*>(t->scan_scratch);
+  const int g2 = (2 * n - 1 + kThreads - 1) / kThreads;
   cudaMemsetAsync(t->omask, 0, 4 * (size_t)m, st);
   k_frontier<<<g2, kThreads, 0, st>>>(n, t->ndim, skeys, t->parent, t->leaf_parent, t->range,
                                       t->depth, t->omask, t->head_of, err);
+  ++*launches;
+}
+
+void fl_launch_cells(const FlTreeBufs* t, bool closed, float sign, const float* cube, int fx_exp,
+                     int fp64_depth, uint32_t* err, cudaStream_t st, int64_t* launches,
+                     FlSegs segs) {
+  const int n = t->n, m = n - 1;
+  const int g = (m + kThreads - 1) / kThreads, g2 = (2 * n - 1 + kThreads - 1) / kThreads;
+  uint32_t* ctot = static_cast<uint32_t*>(t->scan_scratch);
   const D4* P = reinterpret_cast<const D4*>(t->wsum);
   const D4* Ptot = reinterpret_cast<const D4*>(t->wtiles);
   if (closed)
@@ -1338,7 +1361,7 @@ void fl_launch_aggregate(const FlTreeBufs* t, const uint64_t* skeys, bool closed
                                            t->count, t->first, ctot, sign, P, Ptot, t->leaf, cube,
                                            fx_exp, t->cell, segs);
   k_top_u32<<<1, kTopThreads, 0, st>>>(ctot, g);
-  *launches += 3;
+  *launches += 2;
   if (!closed) {
     cudaMemsetAsync(t->flag, 0, 4 * (size_t)m, st);
     k_cells_climb<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(
@@ -1350,6 +1373,13 @@ void fl_launch_aggregate(const FlTreeBufs* t, const uint64_t* skeys, bool closed
                                    t->depth, t->count, t->first, ctot, t->cell, t->leaf,
                                    t->child_data, t->child_meta, err, segs);
   ++*launches;
+}
+
+void fl_launch_aggregate(const FlTreeBufs* t, const uint64_t* skeys, bool closed, float sign,
+                         const float* cube, int fx_exp, int fp64_depth, uint32_t* err,
+                         cudaStream_t st, int64_t* launches, FlSegs segs) {
+  fl_launch_frontier(t, skeys, err, st, launches);
+  fl_launch_cells(t, closed, sign, cube, fx_exp, fp64_depth, err, st, launches, segs);
 }
 
 // Blocks of this walk variant resident on one SM (queried once), at most kWalkBlocksPerSm.
