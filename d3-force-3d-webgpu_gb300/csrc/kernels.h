@@ -66,7 +66,7 @@ struct FlSortBufs {
   uint32_t* vals[2];
   uint32_t* hist;      // [8][256] digit counts per pass
   uint32_t* status;    // [passes][tiles][256] look-back words (tiles of this sort's tile size)
-  uint32_t* counters;  // [kSortCounters]: tile tickets of the 8 passes, then the run fix-up's
+  uint32_t* counters;  // [kSortCounters]: tile tickets of up to 8 passes, then the run fix-up's
   uint32_t* longs;     // [longs_cap] first positions of the runs the fix-up sorts in one block
   uint32_t longs_cap;
   int64_t cap;         // pairs the buffers hold

@@ -7,7 +7,8 @@
 //   morton     the d3 cube from the bounding box, each point's cell at the finest level (exact),
 //              interleaved into a left-aligned Morton key in d3's child order; the sort's digit
 //              histograms are counted in the same pass
-//   sort       onesweep radix sort of (key, node) (sort.cu)
+//   sort       onesweep radix sort of (key, node) over the top 31 (3D) / 32 (2D) key bits, then
+//              the run fix-up that orders keys equal in those bits by the rest (sort.cu)
 //   build      Karras (2012) binary radix tree over the sorted keys; each internal node's d3
 //              depth = common prefix bits / DIMS; the sorted (position, strength) of the points,
 //              and each point's d3 leaf depth (from the deeper of its two neighbour prefixes)
