@@ -88,6 +88,9 @@ struct fl_batch {
   std::vector<Block> blocks;
   bool use_graphs = true;
   int sort_passes = 0, walk_blocks = 0;  // tuning (FL_TUNE_SORT_PASSES, FL_TUNE_WALK_BLOCKS)
+  // the side stream of the trees (overlapping the links), forked and joined by events
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_tree = nullptr;
 };
 
 namespace {
@@ -137,6 +140,42 @@ void encode_batch_tick(fl_batch* b, const double* alpha, const FlTick* tk) {
   fl_launch_bgraph(G, b->ndim, b->off.as<int32_t>(), b->red.as<FlReduce>(),
                    b->prm.as<FlBatchParams>(), alpha, gr, st);
   b->launches += 2;
+  // many-body trees: sort by Morton code, then (stably) by graph; one tree per graph. They
+  // depend on the positions and the graphs' cubes only, so they are built on the side stream
+  // while the links run on the main one
+  uint64_t* skeys = nullptr;
+  uint32_t* perm = nullptr;
+  uint32_t* gpos = b->gid_pos.as<uint32_t>();
+  FlSegs segs{G, b->off.as<int32_t>(), gid, gpos, gr};
+  const bool side = b->aux != nullptr;
+  if (n >= 2) {
+    cudaStream_t ts = st;
+    if (side) {
+      cudaEventRecord(b->ev_fork, st);
+      cudaStreamWaitEvent(b->aux, b->ev_fork, 0);
+      ts = b->aux;
+    }
+    const int bits = (b->ndim == 3 ? 21 : 24) * b->ndim, lo_bit = 64 - bits;
+    const int lo_sort = fl_sort_split(lo_bit, b->sort_passes);
+    fl_sort_reset(&b->sb, n, (64 - lo_sort + 7) / 8, ts);
+    fl_launch_bmorton(b->pos.as<float4>(), n, b->ndim, gid, gr, b->sb.keys[0], b->sb.vals[0],
+                      b->sb.hist, lo_sort, ts);
+    int r = fl_sort_passes(&b->sb, n, lo_sort, err, ts, &b->launches);
+    r = fl_sort_runfix(&b->sb, n, lo_bit, lo_sort, r, ts, &b->launches);
+    fl_sort_reset(&b->sb2, n, 2, ts);
+    fl_launch_bgidkey(n, b->sb.vals[r], gid, b->off.as<int32_t>(), G, b->sb2.keys[0],
+                      b->sb2.vals[0], b->sb2.hist, ts);
+    const int r2 = fl_sort_passes(&b->sb2, n, 48, err, ts, &b->launches);
+    skeys = b->sb.keys[1 - r];
+    perm = b->sb.vals[1 - r];
+    fl_launch_bgather(n, b->sb2.vals[r2], b->sb.keys[r], b->sb.vals[r], gid, skeys, perm, gpos, ts);
+    b->launches += 3;
+    fl_launch_build(&b->tb, skeys, perm, b->pos.as<float4>(), b->charge.as<float>(), b->closed,
+                    nullptr, b->fx_exp, ts, &b->launches, segs);
+    fl_launch_aggregate(&b->tb, skeys, b->closed, b->sign, nullptr, b->fx_exp, 6, err, ts,
+                        &b->launches, segs);
+    if (side) cudaEventRecord(b->ev_tree, ts);
+  }
   // links (a snapshot: read v, write the other velocity buffer)
   if (b->m > 0) {
     FlLinkCsr csr{b->row.as<int32_t>(), b->entry.as<float4>(), b->code.as<uint32_t>()};
@@ -145,29 +184,8 @@ void encode_batch_tick(fl_batch* b, const double* alpha, const FlTick* tk) {
     b->cur = 1 - b->cur;
     ++b->launches;
   }
-  // many-body: sort by Morton code, then (stably) by graph; one tree per graph
   if (n >= 2) {
-    const int bits = (b->ndim == 3 ? 21 : 24) * b->ndim, lo_bit = 64 - bits;
-    const int lo_sort = fl_sort_split(lo_bit, b->sort_passes);
-    fl_sort_reset(&b->sb, n, (64 - lo_sort + 7) / 8, st);
-    fl_launch_bmorton(b->pos.as<float4>(), n, b->ndim, gid, gr, b->sb.keys[0], b->sb.vals[0],
-                      b->sb.hist, lo_sort, st);
-    int r = fl_sort_passes(&b->sb, n, lo_sort, err, st, &b->launches);
-    r = fl_sort_runfix(&b->sb, n, lo_bit, lo_sort, r, st, &b->launches);
-    fl_sort_reset(&b->sb2, n, 2, st);
-    fl_launch_bgidkey(n, b->sb.vals[r], gid, b->off.as<int32_t>(), G, b->sb2.keys[0],
-                      b->sb2.vals[0], b->sb2.hist, st);
-    const int r2 = fl_sort_passes(&b->sb2, n, 48, err, st, &b->launches);
-    uint64_t* skeys = b->sb.keys[1 - r];
-    uint32_t* perm = b->sb.vals[1 - r];
-    uint32_t* gpos = b->gid_pos.as<uint32_t>();
-    fl_launch_bgather(n, b->sb2.vals[r2], b->sb.keys[r], b->sb.vals[r], gid, skeys, perm, gpos, st);
-    b->launches += 3;
-    FlSegs segs{G, b->off.as<int32_t>(), gid, gpos, gr};
-    fl_launch_build(&b->tb, skeys, perm, b->pos.as<float4>(), b->charge.as<float>(), b->closed,
-                    nullptr, b->fx_exp, st, &b->launches, segs);
-    fl_launch_aggregate(&b->tb, skeys, b->closed, b->sign, nullptr, b->fx_exp, 6, err, st,
-                        &b->launches, segs);
+    if (side) cudaStreamWaitEvent(st, b->ev_tree, 0);
     b->tb.walk_blocks = b->walk_blocks;
     fl_launch_walk(&b->tb, perm, nullptr, bvel(b), 0.f, 1.0, 0.0, b->dmax_any, b->step, b->seed,
                    err, nullptr, 32, st, segs, tk);
@@ -201,6 +219,13 @@ int32_t fl_batch_create(int32_t device, fl_batch** out) {
     delete b;
     return FL_E_DEVICE;
   }
+  if (cudaStreamCreateWithFlags(&b->aux, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->ev_tree, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();  // no side stream: the trees run on the main one
+    if (b->aux) cudaStreamDestroy(b->aux);
+    b->aux = nullptr;
+  }
   *out = b;
   return FL_OK;
 }
@@ -209,8 +234,12 @@ int32_t fl_batch_destroy(fl_batch* b) {
   if (!b) return FL_OK;
   cudaSetDevice(b->device);
   cudaStreamSynchronize(b->st);
+  if (b->aux) cudaStreamSynchronize(b->aux);
   clear_blocks(b);
   cudaStreamDestroy(b->st);
+  if (b->aux) cudaStreamDestroy(b->aux);
+  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+  if (b->ev_tree) cudaEventDestroy(b->ev_tree);
   delete b;
   return FL_OK;
 }

@@ -8,10 +8,18 @@
 The physics runs in libforcegpu.so (sm_103a CUDA, C ABI in include/forcegpu.h); this package is
 the host side: the simulation object, the force objects and the ctypes bindings.
 """
-from ._lib import Engine, FlError, load
-from .forces import (constant, forceCenter, forceCollide, forceLink, forceManyBody, forceRadial,
-                     forceX, forceY, forceZ)
-from .simulation import GPU_KEYS, SIMULATION_KEYS, Simulation, forceSimulationGPU, lcg
+import os as _os
+
+# Every simulation runs on three streams and a batch on two; a server runs many of them at
+# once. With the CUDA default of 8 hardware work queues, streams share queues and wait on each
+# other's unrelated work; 32 (the most) lets them run side by side. The setting is read when the
+# process's CUDA context is created, so it only takes effect if nothing created one before.
+_os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
+from ._lib import Engine, FlError, load  # noqa: E402
+from .forces import (constant, forceCenter, forceCollide, forceLink,  # noqa: E402
+                     forceManyBody, forceRadial, forceX, forceY, forceZ)
+from .simulation import GPU_KEYS, SIMULATION_KEYS, Simulation, forceSimulationGPU, lcg  # noqa: E402
 
 
 def isWebGPUAvailable():
