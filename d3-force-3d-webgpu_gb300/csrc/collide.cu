@@ -236,7 +236,7 @@ void fl_launch_grid_keys(const float4* pos, const float4* vel, int n, int ndim, 
                          int bits, uint64_t* keys, uint32_t* vals, uint32_t* hist, int lo_bit,
                          cudaStream_t st) {
   int g = (n + kThreads - 1) / kThreads;
-  if (g > 2 * 152) g = 2 * 152;  // few blocks: each flushes its histograms with global atomics
+  if (g > 2 * fl_sms()) g = 2 * fl_sms();  // few blocks: each flushes its histograms with global atomics
   if (g < 1) g = 1;
   k_grid_keys<<<g, kThreads, 0, st>>>(pos, vel, n, ndim, inv_cell, bits, keys, vals, hist, lo_bit);
 }

@@ -422,7 +422,7 @@ void fl_sort_histogram(const FlSortBufs* b, int64_t n, int lo_bit, cudaStream_t 
                        int64_t* launches) {
   int passes = (64 - lo_bit + 7) / 8;
   int64_t blocks = (n + 255) / 256;
-  if (blocks > 4 * 152) blocks = 4 * 152;
+  if (blocks > 4 * fl_sms()) blocks = 4 * fl_sms();
   if (blocks < 1) blocks = 1;
   k_hist<<<(int)blocks, 256, 0, st>>>(b->keys[0], n, lo_bit, passes, b->hist);
   ++*launches;

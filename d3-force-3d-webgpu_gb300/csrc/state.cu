@@ -323,7 +323,7 @@ __global__ void __launch_bounds__(kThreads) k_position(const float4* __restrict_
 void fl_launch_reduce(const float4* pos, int n, int ndim, int want_box, int want_sum,
                       FlReduce* red, cudaStream_t st) {
   int g = grid_for(n, kThreads * 4);
-  if (g > 2 * 152) g = 2 * 152;
+  if (g > 2 * fl_sms()) g = 2 * fl_sms();
   k_reduce<<<g, kThreads, 0, st>>>(pos, n, ndim, want_box, want_sum, red);
 }
 
