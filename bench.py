@@ -53,7 +53,7 @@ BYTES_PER_NODE_TICK = 64 + 4 + 140 + 4 + 48
 WALK_BYTES_PER_NODE = 16 + 4 + 48 + 32
 # DRAM bytes (read + write) of one walk launch at the default 1M-node workload, from ncu
 # (profiles/walk_1m_3d.md); reported as the roofline's measured traffic at that size only
-WALK_DRAM_BYTES_1M = 74.0e6
+WALK_DRAM_BYTES_1M = 73.5e6
 FLOPS_PER_INTERACTION = 20  # FP32 ops per accepted cell or point interaction
 FLOPS_PER_OPEN = 8          # per opened-cell test
 
