@@ -10,8 +10,10 @@ velocityDecay 0.4. A step is one tick. Synthetic, seeded data (no dataset is inv
 
   value     ms per tick, device-timed with CUDA events on the engine's stream, state resident
   e2e       ms per tick through the C ABI with host buffers: each step uploads every position
-            from pinned host memory (fl_update_positions), queues the tick (fl_enqueue) and reads
-            positions and velocities back into pinned host memory (fl_sync)
+            from pinned host memory (fl_update_positions_packed: x, y, z per node), queues the
+            tick (fl_enqueue) and reads positions and velocities back into pinned host memory
+            (fl_sync_packed: x, y, z each). The host link (~190-205 GB/s each way, measured)
+            carries 3/4 of the bytes of the float4 calls, fl_update_positions and fl_sync
   roofline  the dominant kernel (the tree walk) against measured HBM bandwidth, and its FP32
             pipe view from interaction counts
   cpu_baseline  the oracle (FP64 C restatement of the reference's CPU simulation, one core) on
@@ -686,26 +688,26 @@ def main():
     # e2e through the C ABI with pinned host buffers
     e2e = None
     if not args.no_e2e:
-        hp = torch.empty((n, 4), dtype=torch.float32, pin_memory=True)
-        hv = torch.empty((n, 4), dtype=torch.float32, pin_memory=True)
-        eng.sync_into(hp.data_ptr(), hv.data_ptr())
+        hp = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+        hv = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+        eng.sync_packed_into(hp.data_ptr(), hv.data_ptr())
         hpn = hp.numpy()
         k = args.steps
         a2 = al[total + 1:total + 1 + k]
         barrier()
         t0 = time.perf_counter()
         for i in range(k):
-            eng.update_positions(0, hpn)
+            eng.update_positions_packed(0, hpn)
             eng.enqueue(a2[i:i + 1], decay)
-            eng.sync_into(hp.data_ptr(), hv.data_ptr())
+            eng.sync_packed_into(hp.data_ptr(), hv.data_ptr())
         barrier()
         e2e_ms = (time.perf_counter() - t0) * 1e3 / k
         if world > 1:
             t = torch.tensor([e2e_ms], device="cuda")
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             e2e_ms = float(t.item())
-        e2e = {"value": e2e_ms / world, "unit": UNIT, "h2d_bytes_per_step": 16 * n + 8,
-               "d2h_bytes_per_step": 32 * n}
+        e2e = {"value": e2e_ms / world, "unit": UNIT, "h2d_bytes_per_step": 12 * n + 8,
+               "d2h_bytes_per_step": 24 * n}
 
     dev_bytes = eng.query(Q_DEVICE_BYTES)
     peaks, peak_kind = measured_peaks()

@@ -109,6 +109,7 @@ struct fl_sim {
   std::string err;
   int32_t n = 0, ndim = 2;
   DevMem pos, vel[2], fix, mask, errw;
+  DevMem pack;  // staging of the packed transfers: ndim floats of position, then of velocity
   int cur = 0;
   // the box and sums of the tick's starting positions: reds[red_cur]; the integrate of the tick
   // before fills it (pre_valid) unless the positions changed since
@@ -734,6 +735,7 @@ int32_t fl_set_nodes(fl_sim* s, int32_t n, int32_t ndim, const float* pos4, cons
   FL_CK(s, s->vel[1].alloc(v4));
   FL_CK(s, s->fix.alloc(v4));
   FL_CK(s, s->mask.alloc(4 * (size_t)std::max(n, 1)));
+  FL_CK(s, s->pack.alloc(8 * (size_t)s->ndim * (size_t)std::max(n, 1)));
   if (n) {
     FL_CK(s, cudaMemcpy(s->pos.p, pos4, 16 * (size_t)n, cudaMemcpyHostToDevice));
     if (vel4) FL_CK(s, cudaMemcpy(s->vel[0].p, vel4, 16 * (size_t)n, cudaMemcpyHostToDevice));
@@ -755,6 +757,22 @@ int32_t fl_update_positions(fl_sim* s, int32_t first, int32_t count, const float
     FL_CK(s, cudaMemcpyAsync(s->pos.as<float4>() + first, pos4, 16 * (size_t)count,
                              cudaMemcpyHostToDevice, s->st));
   s->pre_valid = false;  // the next tick reduces the positions afresh (count 0: written on the device)
+  FL_CK(s, cudaStreamSynchronize(s->st));
+  return FL_OK;
+}
+
+int32_t fl_update_positions_packed(fl_sim* s, int32_t first, int32_t count, const float* pos) {
+  int32_t rc = check_sim(s);
+  if (rc) return rc;
+  if (first < 0 || count < 0 || first + (int64_t)count > s->n || (count && !pos))
+    return fail(s, FL_E_ARG, "range out of bounds");
+  if (count) {
+    FL_CK(s, cudaMemcpyAsync(s->pack.p, pos, 4 * (size_t)s->ndim * count, cudaMemcpyHostToDevice,
+                             s->st));
+    fl_launch_unpack(s->pack.as<float>(), count, s->ndim, s->pos.as<float4>() + first, s->st);
+    ++s->launches;
+  }
+  s->pre_valid = false;
   FL_CK(s, cudaStreamSynchronize(s->st));
   return FL_OK;
 }
@@ -940,6 +958,25 @@ int32_t fl_sync(fl_sim* s, float* pos4_out, float* vel4_out) {
     FL_CK(s, cudaMemcpyAsync(pos4_out, s->pos.p, 16 * (size_t)s->n, cudaMemcpyDeviceToHost, s->st));
   if (s->n && vel4_out)
     FL_CK(s, cudaMemcpyAsync(vel4_out, vel_cur(s), 16 * (size_t)s->n, cudaMemcpyDeviceToHost, s->st));
+  FL_CK(s, cudaStreamSynchronize(s->st));
+  if (s->profiling) drain_profile(s);
+  return collect_errors(s);
+}
+
+int32_t fl_sync_packed(fl_sim* s, float* pos_out, float* vel_out) {
+  int32_t rc = check_sim(s);
+  if (rc) return rc;
+  if (s->n && (pos_out || vel_out)) {
+    const size_t m = (size_t)s->n * s->ndim;
+    fl_launch_pack(pos_out ? s->pos.as<float4>() : nullptr, vel_out ? vel_cur(s) : nullptr, s->n,
+                   s->ndim, s->pack.as<float>(), s->st);
+    ++s->launches;
+    if (pos_out)
+      FL_CK(s, cudaMemcpyAsync(pos_out, s->pack.p, 4 * m, cudaMemcpyDeviceToHost, s->st));
+    if (vel_out)
+      FL_CK(s, cudaMemcpyAsync(vel_out, s->pack.as<float>() + m, 4 * m, cudaMemcpyDeviceToHost,
+                               s->st));
+  }
   FL_CK(s, cudaStreamSynchronize(s->st));
   if (s->profiling) drain_profile(s);
   return collect_errors(s);

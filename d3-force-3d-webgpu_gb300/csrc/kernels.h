@@ -113,6 +113,12 @@ void fl_launch_integrate(float4* pos, float4* vel, const float4* fix, const uint
                          double cz, double strength, cudaStream_t st, const FlGraph* gr = nullptr,
                          const uint32_t* gid = nullptr, const FlTick* tk = nullptr,
                          FlReduce* out = nullptr, int want_box = 0, int want_sum = 0);
+// Positions and velocities (either may be NULL) to `ndim` floats per node in out: positions at
+// [0, n ndim), velocities at [n ndim, 2 n ndim). And back: ndim floats per node to float4 (the
+// rest 0) at dst[0, count).
+void fl_launch_pack(const float4* pos, const float4* vel, int n, int ndim, float* out,
+                    cudaStream_t st);
+void fl_launch_unpack(const float* src, int count, int ndim, float4* dst, cudaStream_t st);
 void fl_launch_radial(const float4* pos, float4* vel, const float* radius, const float* strength,
                       int n, int ndim, float cx, float cy, float cz, float alpha, cudaStream_t st,
                       const FlTick* tk = nullptr);

@@ -318,7 +318,45 @@ __global__ void __launch_bounds__(kThreads) k_position(const float4* __restrict_
   vel[i] = v;
 }
 
+// Positions and velocities to `ndim` floats per node: out[0, n ndim) and out[n ndim, 2 n ndim),
+// one thread per output float (coalesced writes).
+__global__ void __launch_bounds__(kThreads) k_pack(const float* __restrict__ pos,
+                                                   const float* __restrict__ vel, int64_t n,
+                                                   int ndim, float* __restrict__ out) {
+  const int64_t m = n * ndim;
+  for (int64_t i = blockIdx.x * (int64_t)kThreads + threadIdx.x; i < m;
+       i += (int64_t)gridDim.x * kThreads) {
+    const int64_t node = i / ndim, at = node * 4 + (i - node * ndim);
+    if (pos) out[i] = pos[at];
+    if (vel) out[m + i] = vel[at];
+  }
+}
+
+// `ndim` floats per node back to float4 state: the components past ndim and w are 0, as the
+// integrate leaves them.
+__global__ void __launch_bounds__(kThreads) k_unpack(const float* __restrict__ src, int count,
+                                                     int ndim, float4* __restrict__ dst) {
+  const int i = blockIdx.x * kThreads + threadIdx.x;
+  if (i >= count) return;
+  const float* s = src + (int64_t)i * ndim;
+  dst[i] = make_float4(s[0], ndim > 1 ? s[1] : 0.f, ndim > 2 ? s[2] : 0.f, 0.f);
+}
+
 }  // namespace
+
+void fl_launch_pack(const float4* pos, const float4* vel, int n, int ndim, float* out,
+                    cudaStream_t st) {
+  if (n <= 0) return;
+  int g = grid_for(n * ndim, kThreads * 4);
+  if (g > 8 * fl_sms()) g = 8 * fl_sms();
+  k_pack<<<g, kThreads, 0, st>>>(reinterpret_cast<const float*>(pos),
+                                 reinterpret_cast<const float*>(vel), n, ndim, out);
+}
+
+void fl_launch_unpack(const float* src, int count, int ndim, float4* dst, cudaStream_t st) {
+  if (count <= 0) return;
+  k_unpack<<<grid_for(count, kThreads), kThreads, 0, st>>>(src, count, ndim, dst);
+}
 
 void fl_launch_reduce(const float4* pos, int n, int ndim, int want_box, int want_sum,
                       FlReduce* red, cudaStream_t st) {

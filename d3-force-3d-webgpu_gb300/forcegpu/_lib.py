@@ -28,7 +28,8 @@ EXPORTS = ["fl_create", "fl_destroy", "fl_last_error", "fl_fits", "fl_set_nodes"
            "fl_debug_tree", "fl_set_tuning", "fl_radix_sort_noalloc", "fl_batch_create",
            "fl_batch_destroy", "fl_batch_last_error", "fl_batch_set_graphs", "fl_batch_set_seed",
            "fl_batch_enqueue", "fl_batch_sync", "fl_batch_query", "fl_batch_stream",
-           "fl_autotune", "fl_batch_set_tuning", "fl_batch_autotune", "fl_batch_read"]
+           "fl_autotune", "fl_batch_set_tuning", "fl_batch_autotune", "fl_batch_read",
+           "fl_update_positions_packed", "fl_sync_packed"]
 SORT_NOALLOC_MAX_PAIRS = 262144  # FL_SORT_NOALLOC_MAX_PAIRS
 TUNE_WALK_GROUP, TUNE_CELL_SUMS, TUNE_GRAPHS = 1, 2, 3
 TUNE_SORT_PASSES, TUNE_WALK_BLOCKS, TUNE_COLLIDE_CELL = 4, 5, 6
@@ -113,6 +114,8 @@ def load():
         "fl_set_seed": (I32, [P, U32]),
         "fl_enqueue": (I32, [P, P, I32, D]),
         "fl_sync": (I32, [P, P, P]),
+        "fl_sync_packed": (I32, [P, P, P]),
+        "fl_update_positions_packed": (I32, [P, I32, I32, P]),
         "fl_idle": (I32, [P]),
         "fl_busy": (I32, [P, ctypes.POINTER(I32)]),
         "fl_buffers": (I32, [P, ctypes.POINTER(BufferInfo)]),
@@ -197,6 +200,11 @@ class Engine:
         pos4 = np.ascontiguousarray(pos4, dtype=np.float32).reshape(-1, 4)
         self._check(self.L.fl_update_positions(self.h, int(first), len(pos4), _ptr(pos4)))
 
+    def update_positions_packed(self, first, pos):
+        """fl_update_positions with ndim floats per node: a (count, ndim) array."""
+        pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, self.ndim)
+        self._check(self.L.fl_update_positions_packed(self.h, int(first), len(pos), _ptr(pos)))
+
     def update_velocities(self, first, vel4):
         vel4 = np.ascontiguousarray(vel4, dtype=np.float32).reshape(-1, 4)
         self._check(self.L.fl_update_velocities(self.h, int(first), len(vel4), _ptr(vel4)))
@@ -232,6 +240,22 @@ class Engine:
     def sync_into(self, pos_ptr, vel_ptr):
         """Wait, then read back into caller-owned host memory given by address (e.g. pinned)."""
         self._check(self.L.fl_sync(self.h, pos_ptr, vel_ptr))
+
+    def sync_packed(self, pos_out=None, vel_out=None):
+        """fl_sync into float32 (n, ndim) arrays: ndim floats per node cross the host link."""
+        if pos_out is None:
+            pos_out = np.empty((self.n, self.ndim), np.float32)
+        if vel_out is None:
+            vel_out = np.empty((self.n, self.ndim), np.float32)
+        for a in (pos_out, vel_out):
+            if a.dtype != np.float32 or not a.flags.c_contiguous or a.size != self.n * self.ndim:
+                raise ValueError("sync_packed wants C-contiguous float32 arrays of n * ndim floats")
+        self._check(self.L.fl_sync_packed(self.h, _ptr(pos_out), _ptr(vel_out)))
+        return pos_out, vel_out
+
+    def sync_packed_into(self, pos_ptr, vel_ptr):
+        """fl_sync_packed into caller-owned host memory given by address (e.g. pinned)."""
+        self._check(self.L.fl_sync_packed(self.h, pos_ptr, vel_ptr))
 
     def idle(self):
         self._check(self.L.fl_idle(self.h))

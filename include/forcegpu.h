@@ -105,6 +105,10 @@ int32_t fl_set_nodes(fl_sim* sim, int32_t n, int32_t ndim, const float* pos4, co
 /* Upload nodes [first, first + count) that the caller moved (uploadPositions,
  * src/gpu/engine.js:147-156): 4*count floats. */
 int32_t fl_update_positions(fl_sim* sim, int32_t first, int32_t count, const float* pos4);
+/* fl_update_positions with `ndim` floats per node (x[, y[, z]]: ndim*count floats), unpacked on
+ * the device, so the host link carries ndim/4 of the bytes. No counterpart in the reference,
+ * whose uploadPositions writes vec4s (src/gpu/engine.js:147-156). */
+int32_t fl_update_positions_packed(fl_sim* sim, int32_t first, int32_t count, const float* pos);
 /* Upload changed pins of nodes [first, first + count) (uploadPinned, src/gpu/engine.js:158-169). */
 int32_t fl_update_pins(fl_sim* sim, int32_t first, int32_t count, const float* fix4,
                        const uint32_t* mask);
@@ -126,6 +130,11 @@ int32_t fl_enqueue(fl_sim* sim, const double* alphas, int32_t count, double deca
  * be NULL) into the caller's arrays (engine.sync + readback, src/gpu/engine.js:218-239,
  * :406-414). Reports a device-side error raised by any tick since the previous sync. */
 int32_t fl_sync(fl_sim* sim, float* pos4_out, float* vel4_out);
+/* fl_sync with positions and velocities packed to `ndim` floats per node (ndim*n floats each;
+ * either may be NULL), packed on the device first so that the host link carries ndim/4 of
+ * fl_sync's bytes. No counterpart in the reference, whose readback maps the two vec4 buffers
+ * (src/gpu/engine.js:218-239). */
+int32_t fl_sync_packed(fl_sim* sim, float* pos_out, float* vel_out);
 /* Wait for every queued tick, no readback (engine.idle, src/gpu/engine.js:401-404). */
 int32_t fl_idle(fl_sim* sim);
 /* Whether queued work is still running (engine.busy, src/gpu/engine.js:393-396). */
