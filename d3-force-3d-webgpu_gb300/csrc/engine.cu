@@ -376,18 +376,26 @@ void encode_tree(fl_sim* s, Pass* p, const FlReduce* box, cudaStream_t st) {
     ++s->launches;
     box = p->red.as<FlReduce>();
   }
+  // a small layout's keys are sorted in one launch (unless digit passes were asked for), so
+  // the keys need no digit histograms (lo_bit 64: none)
+  const bool by_rank = n <= kSortRankMax && s->sort_passes == 0;
   {
     Scope sc(s, G_MORTON, st);
-    fl_sort_reset(&p->sb, n, (64 - lo_sort + 7) / 8, st);
+    if (!by_rank) fl_sort_reset(&p->sb, n, (64 - lo_sort + 7) / 8, st);
     fl_launch_morton(s->pos.as<float4>(), n, s->ndim, box, p->sb.keys[0], p->sb.vals[0],
-                     p->sb.hist, lo_sort, p->cube.as<float>(), st);
+                     by_rank ? nullptr : p->sb.hist, by_rank ? 64 : lo_sort, p->cube.as<float>(),
+                     st);
     ++s->launches;
   }
   int r;
   {
     Scope sc(s, G_SORT, st);
-    r = fl_sort_passes(&p->sb, n, lo_sort, s->errw.as<uint32_t>(), st, &s->launches);
-    r = fl_sort_runfix(&p->sb, n, lo_bit, lo_sort, r, st, &s->launches);
+    if (by_rank) {
+      r = fl_sort_rank(&p->sb, n, st, &s->launches);
+    } else {
+      r = fl_sort_passes(&p->sb, n, lo_sort, s->errw.as<uint32_t>(), st, &s->launches);
+      r = fl_sort_runfix(&p->sb, n, lo_bit, lo_sort, r, st, &s->launches);
+    }
     p->sorted_in = r;
   }
   // the closed form (exact fixed-point sums) when the strengths share one sign, unless a

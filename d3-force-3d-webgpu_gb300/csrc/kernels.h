@@ -97,6 +97,12 @@ int fl_sort_passes(const FlSortBufs* b, int64_t n, int lo_bit, uint32_t* err, cu
 int fl_sort_split(int lo_bit, int passes = 0);
 int fl_sort_runfix(const FlSortBufs* b, int64_t n, int lo_bit, int lo_sort, int cur,
                    cudaStream_t st, int64_t* launches);
+// Up to this many pairs, the tree sorts its keys in one launch (fl_sort_rank): each pair's place
+// counted against every key, the stable order of the digit passes and the run fix-up.
+constexpr int64_t kSortRankMax = 6144;
+// The stable sort of 1 <= n <= kSortRankMax pairs, keys[0]/vals[0] -> keys[1]/vals[1]; returns
+// the buffer holding the result (1), or 0 without a launch for other n.
+int fl_sort_rank(const FlSortBufs* b, int64_t n, cudaStream_t st, int64_t* launches);
 
 // ---------------------------------------------------------------- state kernels (state.cu)
 void fl_launch_reduce(const float4* pos, int n, int ndim, int want_box, int want_sum,

@@ -375,6 +375,41 @@ void launch_pass(const uint64_t* kin, const uint32_t* vin, uint64_t* kout, uint3
 }
 uint32_t longs_cap_for(int64_t n) { return (uint32_t)(n / (kRunShort + 1) + 1); }
 
+constexpr int kRankWarps = 8;
+
+// The stable sort of up to kSortRankMax pairs in one launch, for the tree of a small layout,
+// where the digit passes and the run fix-up are five launches over a few thousand keys. A pair's
+// place is the number of smaller keys plus the number of equal keys before it in the input.
+// Block b places pairs 32 b .. 32 b + 31: lane l of every warp holds pair 32 b + l and counts
+// over one kRankWarps-th of the keys (the same key in every lane: one broadcast load); the
+// warps' counts are summed in shared memory.
+__global__ void __launch_bounds__(kRankWarps * 32) k_ranksort(const uint64_t* __restrict__ keys,
+                                                              const uint32_t* __restrict__ vals,
+                                                              int n, uint64_t* __restrict__ okeys,
+                                                              uint32_t* __restrict__ ovals) {
+  __shared__ uint32_t s_rank[kRankWarps][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i = blockIdx.x * 32 + lane;
+  const uint64_t k = i < n ? keys[i] : ~0ull;
+  const int per = (n + kRankWarps - 1) / kRankWarps;
+  const int j0 = min(n, w * per), j1 = min(n, j0 + per);
+  uint32_t rank = 0;
+#pragma unroll 8
+  for (int j = j0; j < j1; ++j) {
+    const uint64_t kj = keys[j];
+    rank += (uint32_t)((kj < k) | ((kj == k) & (j < i)));
+  }
+  s_rank[w][lane] = rank;
+  __syncthreads();
+  if (w == 0 && i < n) {
+    uint32_t r = 0;
+#pragma unroll
+    for (int q = 0; q < kRankWarps; ++q) r += s_rank[q][lane];
+    okeys[r] = k;
+    ovals[r] = vals[i];
+  }
+}
+
 }  // namespace
 
 int fl_sort_tile(int64_t n) { return n <= kSortSmallMax ? kSortTileSmall : kSortTile; }
@@ -447,6 +482,14 @@ int fl_sort_passes(const FlSortBufs* b, int64_t n, int lo_bit, uint32_t* err, cu
     cur = 1 - cur;
   }
   return cur;
+}
+
+int fl_sort_rank(const FlSortBufs* b, int64_t n, cudaStream_t st, int64_t* launches) {
+  if (n <= 0 || n > kSortRankMax) return 0;
+  k_ranksort<<<(int)((n + 31) / 32), kRankWarps * 32, 0, st>>>(b->keys[0], b->vals[0], (int)n,
+                                                                b->keys[1], b->vals[1]);
+  ++*launches;
+  return 1;
 }
 
 int fl_sort_split(int lo_bit, int passes) {

@@ -126,7 +126,7 @@ class _NodeMirror:
         if first:
             self.eng.set_nodes(pos, self.nDim, vel, fix, mask)
         elif n:
-            self.eng.update_positions(0, pos)
+            self.eng.update_positions_packed(0, pos[:, :self.nDim])
             self.eng.update_velocities(0, vel)
             self.eng.update_pins(0, fix, mask)
         self.stale = False
@@ -150,7 +150,7 @@ class _NodeMirror:
             for a, b in zip(starts, ends):
                 if upload == "pos":
                     self.shadow[a:b] = pos[a:b, :3]
-                    self.eng.update_positions(int(a), pos[a:b])
+                    self.eng.update_positions_packed(int(a), pos[a:b, :self.nDim])
                 else:
                     self.pinned[a:b] = mask[a:b]
                     self.pinnedAt[a:b] = fix[a:b, :3]
@@ -207,7 +207,7 @@ class _NodeMirror:
         if not self.n or self.landed == self.enqueued:
             self.eng.idle()
             return
-        pos, vel = self.eng.sync()
+        pos, vel = self.eng.sync_packed()  # nDim floats per node across the host link
         self.land(pos, vel)
         self.landed = self.enqueued
 

@@ -8,7 +8,7 @@ import pytest
 
 import oracle
 from forcegpu import forceManyBody, forceSimulationGPU
-from forcegpu._lib import radix_sort
+from forcegpu._lib import TUNE_SORT_PASSES, radix_sort
 from gpu_helpers import make_nodes
 
 pytestmark = pytest.mark.gpu
@@ -62,8 +62,10 @@ def test_sort_full_64bit_keys():
     assert np.array_equal(vo, order.astype(np.uint32))
 
 
-def _tree_of(nodes, dims):
+def _tree_of(nodes, dims, sort_passes=0):
     sim = forceSimulationGPU(nodes, dims).stop()
+    if sort_passes:  # digit passes and the run fix-up even for a small layout
+        sim._engine.eng.set_tuning(TUNE_SORT_PASSES, sort_passes)
     sim.force("charge", forceManyBody())
     asyncio.run(sim.tickAsync(1))
     # positions the tree was built from: the state before the tick
@@ -89,7 +91,8 @@ def clustered_nodes(dims, clusters, per, spread, tight, seed, loose=0):
 
 # the tree's sort orders the top 32 key bits by digit passes and then the runs of equal top
 # bits by a fix-up: runs of a few points, of up to 1024 (ranked in place) and longer ones (sorted
-# by the last block of the fix-up)
+# by the last block of the fix-up); up to 6144 points it ranks every pair in one launch instead,
+# unless digit passes are asked for (sort_passes 4: both paths are checked at every size)
 CLUSTERED = {
     "short runs 3d": (3, 200, 30, 200.0, 1e-3, 1, 0),
     "long run 3d": (3, 1, 3000, 200.0, 1e-3, 2, 2000),
@@ -100,9 +103,11 @@ CLUSTERED = {
 
 
 @pytest.mark.parametrize("dims,n,size", [(1, 500, 200), (2, 2000, 200), (3, 5000, 200),
-                                         (3, 3000, 2), (3, 1000, 2e5), (2, 257, 1)]
+                                         (3, 3000, 2), (3, 1000, 2e5), (2, 257, 1),
+                                         (3, 6144, 300), (3, 6145, 300), (2, 4, 1)]
                          + [pytest.param(v[0], None, k, id=k) for k, v in CLUSTERED.items()])
-def test_tree_matches_cpu_rebuild(dims, n, size):
+@pytest.mark.parametrize("sort_passes", [0, 4])
+def test_tree_matches_cpu_rebuild(dims, n, size, sort_passes):
     if n is None:
         nodes = clustered_nodes(*CLUSTERED[size])
         n = len(nodes)
@@ -115,7 +120,7 @@ def test_tree_matches_cpu_rebuild(dims, n, size):
     for i, d in enumerate(nodes):
         for a, k in enumerate("xyz"[:dims]):
             start[i, a] = d[k]
-    sim = _tree_of(nodes, dims)
+    sim = _tree_of(nodes, dims, sort_passes)
     keys, perm, left, right, depth, cube = sim._engine.eng.debug_tree(0)
     sim.destroy()
     codes = oracle.morton(start, dims)
