@@ -113,7 +113,9 @@ __device__ __forceinline__ int cell_coord(float s, float inv) {
   return (int)fminf(fmaxf(floorf(s * inv), -1073741824.f), 1073741824.f);
 }
 
-__global__ void __launch_bounds__(kThreads) k_grid_keys(const float4* __restrict__ pos,
+constexpr int kKeyThreads = 1024;
+
+__global__ void __launch_bounds__(kKeyThreads) k_grid_keys(const float4* __restrict__ pos,
                                                         const float4* __restrict__ vel, int n,
                                                         int ndim, float inv, int bits,
                                                         uint64_t* __restrict__ keys,
@@ -235,10 +237,11 @@ void fl_grid_carve(FlGridBufs* g, void* base, int64_t n) {
 void fl_launch_grid_keys(const float4* pos, const float4* vel, int n, int ndim, float inv_cell,
                          int bits, uint64_t* keys, uint32_t* vals, uint32_t* hist, int lo_bit,
                          cudaStream_t st) {
-  int g = (n + kThreads - 1) / kThreads;
-  if (g > 2 * fl_sms()) g = 2 * fl_sms();  // few blocks: each flushes its histograms with global atomics
+  // few, large blocks: each flushes its histograms with global atomics
+  int g = (n + kKeyThreads - 1) / kKeyThreads;
+  if (g > 2 * fl_sms()) g = 2 * fl_sms();
   if (g < 1) g = 1;
-  k_grid_keys<<<g, kThreads, 0, st>>>(pos, vel, n, ndim, inv_cell, bits, keys, vals, hist, lo_bit);
+  k_grid_keys<<<g, kKeyThreads, 0, st>>>(pos, vel, n, ndim, inv_cell, bits, keys, vals, hist, lo_bit);
 }
 
 void fl_launch_grid_query(const FlGridBufs* g, const uint64_t* skeys, const uint32_t* perm,

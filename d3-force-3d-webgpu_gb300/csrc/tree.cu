@@ -196,7 +196,9 @@ __device__ __forceinline__ uint64_t morton_key(float4 p, const float* origin, in
 }
 
 // Bounding box -> d3 cube -> keys; digit histograms of the sort passes in the same read.
-__global__ void __launch_bounds__(kThreads) k_morton(const float4* __restrict__ pos, int n,
+constexpr int kMortonThreads = 1024;
+
+__global__ void __launch_bounds__(kMortonThreads) k_morton(const float4* __restrict__ pos, int n,
                                                      int ndim, const FlReduce* red,
                                                      uint64_t* __restrict__ keys,
                                                      uint32_t* __restrict__ vals,
@@ -268,7 +270,7 @@ __global__ void __launch_bounds__(kThreads) k_bgraph(int graphs, int ndim, const
 }
 
 // Morton keys of a batch, each point in its own graph's cube; histograms as k_morton.
-__global__ void __launch_bounds__(kThreads) k_bmorton(const float4* __restrict__ pos, int n,
+__global__ void __launch_bounds__(kMortonThreads) k_bmorton(const float4* __restrict__ pos, int n,
                                                       int ndim, const uint32_t* __restrict__ gid,
                                                       const FlGraph* __restrict__ gr,
                                                       uint64_t* __restrict__ keys,
@@ -1284,12 +1286,14 @@ void fl_tree_carve(FlTreeBufs* t, void* base, int64_t n, int ndim) {
 void fl_launch_morton(const float4* pos, int n, int ndim, const FlReduce* red, uint64_t* keys,
                       uint32_t* vals, uint32_t* hist, int lo_bit, float* cube_out,
                       cudaStream_t st) {
-  // one full wave (8 blocks of 256 per SM, so that enough loads are in flight); each block
-  // flushes its digit histograms with up to 1024 global atomics (4 passes)
-  int g = (n + kThreads - 1) / kThreads;
-  if (g > 8 * fl_sms()) g = 8 * fl_sms();
+  // one full wave of large blocks (2 of 1024 threads per SM, so that enough loads are in
+  // flight): each block flushes its digit histograms with up to 1024 global atomics (4
+  // passes), so fewer blocks contend less for the same counters (8 blocks of 256 per SM took
+  // 9.5 us more per 1M keys; 1 block of 1024, 4 us more)
+  int g = (n + kMortonThreads - 1) / kMortonThreads;
+  if (g > 2 * fl_sms()) g = 2 * fl_sms();
   if (g < 1) g = 1;
-  k_morton<<<g, kThreads, 0, st>>>(pos, n, ndim, red, keys, vals, hist, lo_bit, cube_out);
+  k_morton<<<g, kMortonThreads, 0, st>>>(pos, n, ndim, red, keys, vals, hist, lo_bit, cube_out);
 }
 
 int fl_fixed_exponent(int64_t n, double wmax) {
@@ -1469,10 +1473,10 @@ void fl_launch_bgraph(int graphs, int ndim, const int32_t* off, const FlReduce* 
 
 void fl_launch_bmorton(const float4* pos, int n, int ndim, const uint32_t* gid, const FlGraph* gr,
                        uint64_t* keys, uint32_t* vals, uint32_t* hist, int lo_bit, cudaStream_t st) {
-  int g = (n + kThreads - 1) / kThreads;
-  if (g > 8 * fl_sms()) g = 8 * fl_sms();
+  int g = (n + kMortonThreads - 1) / kMortonThreads;  // as fl_launch_morton
+  if (g > 2 * fl_sms()) g = 2 * fl_sms();
   if (g < 1) g = 1;
-  k_bmorton<<<g, kThreads, 0, st>>>(pos, n, ndim, gid, gr, keys, vals, hist, lo_bit);
+  k_bmorton<<<g, kMortonThreads, 0, st>>>(pos, n, ndim, gid, gr, keys, vals, hist, lo_bit);
 }
 
 void fl_launch_bgidkey(int n, const uint32_t* mperm, const uint32_t* gid, const int32_t* off,
