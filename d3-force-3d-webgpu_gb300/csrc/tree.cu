@@ -313,7 +313,7 @@ __device__ __forceinline__ uint32_t graph_of(const int32_t* s_off, int graphs, u
 }
 constexpr int kGidSearchMax = 8192;  // graphs whose offsets the key kernel searches in shared memory
 
-__global__ void __launch_bounds__(kThreads) k_bgidkey(int n, const uint32_t* __restrict__ mperm,
+__global__ void __launch_bounds__(kMortonThreads) k_bgidkey(int n, const uint32_t* __restrict__ mperm,
                                                       const uint32_t* __restrict__ gid,
                                                       const int32_t* __restrict__ off, int graphs,
                                                       uint64_t* __restrict__ keys,
@@ -1481,10 +1481,12 @@ void fl_launch_bmorton(const float4* pos, int n, int ndim, const uint32_t* gid, 
 
 void fl_launch_bgidkey(int n, const uint32_t* mperm, const uint32_t* gid, const int32_t* off,
                        int graphs, uint64_t* keys, uint32_t* vals, uint32_t* hist, cudaStream_t st) {
-  int g = (n + kThreads - 1) / kThreads;
-  if (g > 4 * fl_sms()) g = 4 * fl_sms();
+  // as fl_launch_morton: few, large blocks (each flushes its histograms with global atomics
+  // and loads the graph offsets once)
+  int g = (n + kMortonThreads - 1) / kMortonThreads;
+  if (g > 2 * fl_sms()) g = 2 * fl_sms();
   if (g < 1) g = 1;
-  k_bgidkey<<<g, kThreads, 0, st>>>(n, mperm, gid, off, graphs, keys, vals, hist);
+  k_bgidkey<<<g, kMortonThreads, 0, st>>>(n, mperm, gid, off, graphs, keys, vals, hist);
 }
 
 void fl_launch_bgather(int n, const uint32_t* order2, const uint64_t* mkeys, const uint32_t* mperm,
