@@ -9,6 +9,8 @@
 // preceding tiles (bounded: a wait gives up after FL_SPIN_LIMIT polls and raises an error bit
 // instead of hanging); keys are then staged in shared memory in digit order and written out in
 // coalesced runs. Stable: keys of equal digit keep their input order.
+#include <atomic>
+
 #include "kernels.h"
 
 namespace {
@@ -360,16 +362,24 @@ int64_t tiles_for(int64_t n) {
 }
 int64_t tiles_cap_for(int64_t cap) { return (cap + kSortTileSmall - 1) / kSortTileSmall; }
 
+// True the first time it is called on the current device for `done` (a kernel's shared-memory
+// limit is raised once per device, and on the first launch, which is never inside a capture).
+static bool first_on_device(std::atomic<uint64_t>& done) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return true;
+  const uint64_t bit = 1ull << dev;
+  return !(done.fetch_or(bit) & bit);
+}
+
 template <int T>
 void launch_pass(const uint64_t* kin, const uint32_t* vin, uint64_t* kout, uint32_t* vout,
                  int64_t n, int shift, const uint32_t* ghist, uint32_t* status, uint32_t* ticket,
                  uint32_t* err, cudaStream_t st) {
-  static bool configured = false;
+  static std::atomic<uint64_t> configured{0};
   const size_t dyn = (size_t)T * kItems * 12;
-  if (!configured) {
+  if (first_on_device(configured))
     cudaFuncSetAttribute(k_onesweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
-    configured = true;
-  }
   const int64_t tiles = (n + T * kItems - 1) / (T * kItems);
   k_onesweep<T><<<(int)tiles, T, dyn, st>>>(kin, vin, kout, vout, n, shift, ghist, status, ticket, err);
 }
@@ -380,23 +390,27 @@ constexpr int kRankWarps = 8;
 // The stable sort of up to kSortRankMax pairs in one launch, for the tree of a small layout,
 // where the digit passes and the run fix-up are five launches over a few thousand keys. A pair's
 // place is the number of smaller keys plus the number of equal keys before it in the input.
-// Block b places pairs 32 b .. 32 b + 31: lane l of every warp holds pair 32 b + l and counts
-// over one kRankWarps-th of the keys (the same key in every lane: one broadcast load); the
-// warps' counts are summed in shared memory.
+// Block b places pairs 32 b .. 32 b + 31: the block copies every key to shared memory
+// (coalesced), then lane l of every warp holds pair 32 b + l and counts over one kRankWarps-th
+// of the keys (the same key in every lane: a broadcast read); the warps' counts are summed in
+// shared memory.
 __global__ void __launch_bounds__(kRankWarps * 32) k_ranksort(const uint64_t* __restrict__ keys,
                                                               const uint32_t* __restrict__ vals,
                                                               int n, uint64_t* __restrict__ okeys,
                                                               uint32_t* __restrict__ ovals) {
+  extern __shared__ uint64_t s_keys[];  // [n]
   __shared__ uint32_t s_rank[kRankWarps][32];
+  for (int j = threadIdx.x; j < n; j += kRankWarps * 32) s_keys[j] = keys[j];
+  __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int i = blockIdx.x * 32 + lane;
-  const uint64_t k = i < n ? keys[i] : ~0ull;
+  const uint64_t k = i < n ? s_keys[i] : ~0ull;
   const int per = (n + kRankWarps - 1) / kRankWarps;
   const int j0 = min(n, w * per), j1 = min(n, j0 + per);
   uint32_t rank = 0;
 #pragma unroll 8
   for (int j = j0; j < j1; ++j) {
-    const uint64_t kj = keys[j];
+    const uint64_t kj = s_keys[j];
     rank += (uint32_t)((kj < k) | ((kj == k) & (j < i)));
   }
   s_rank[w][lane] = rank;
@@ -486,8 +500,12 @@ int fl_sort_passes(const FlSortBufs* b, int64_t n, int lo_bit, uint32_t* err, cu
 
 int fl_sort_rank(const FlSortBufs* b, int64_t n, cudaStream_t st, int64_t* launches) {
   if (n <= 0 || n > kSortRankMax) return 0;
-  k_ranksort<<<(int)((n + 31) / 32), kRankWarps * 32, 0, st>>>(b->keys[0], b->vals[0], (int)n,
-                                                                b->keys[1], b->vals[1]);
+  static std::atomic<uint64_t> configured{0};
+  if (first_on_device(configured))
+    cudaFuncSetAttribute(k_ranksort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(kSortRankMax * sizeof(uint64_t)));
+  k_ranksort<<<(int)((n + 31) / 32), kRankWarps * 32, (size_t)n * sizeof(uint64_t), st>>>(
+      b->keys[0], b->vals[0], (int)n, b->keys[1], b->vals[1]);
   ++*launches;
   return 1;
 }
