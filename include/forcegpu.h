@@ -159,7 +159,8 @@ int32_t fl_buffers(fl_sim* sim, fl_buffer_info* out);
  * seen, or 0 to launch every kernel of every block directly; FL_TUNE_SORT_PASSES, the 8-bit digit
  * passes of the tree's radix sort, from the top of the Morton key (0 = 4, the default: the top
  * 31 bits in 3D, 32 in 2D; 8 = every bit in 3D), the bits below ordered within runs of equal top
- * bits by a fix-up pass: fewer passes, longer runs; FL_TUNE_WALK_BLOCKS, blocks per SM of the
+ * bits by a fix-up pass: fewer passes, longer runs (with 0, a layout of up to 6,144 nodes sorts
+ * in one launch instead, each key ranked against all others: the same order); FL_TUNE_WALK_BLOCKS, blocks per SM of the
  * persistent tree-walk grid (0 = as many as fit, the default); FL_TUNE_COLLIDE_CELL, the collide
  * grid's cell side in percent of the largest diameter (>= 100; 100 = the default).
  * fl_autotune picks these by timing. */
