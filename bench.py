@@ -14,6 +14,7 @@ velocityDecay 0.4. A step is one tick. Synthetic, seeded data (no dataset is inv
             tick (fl_enqueue) and reads positions and velocities back into pinned host memory
             (fl_sync_packed: x, y, z each). The host link (~190-205 GB/s each way, measured)
             carries 3/4 of the bytes of the float4 calls, fl_update_positions and fl_sync
+  e2e_float4  the same through those float4 calls (the reference's vec4 layout)
   roofline  the dominant kernel (the tree walk) against measured HBM bandwidth, and its FP32
             pipe view from interaction counts
   cpu_baseline  the oracle (FP64 C restatement of the reference's CPU simulation, one core) on
@@ -707,7 +708,28 @@ def main():
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             e2e_ms = float(t.item())
         e2e = {"value": e2e_ms / world, "unit": UNIT, "h2d_bytes_per_step": 12 * n + 8,
-               "d2h_bytes_per_step": 24 * n}
+               "d2h_bytes_per_step": 24 * n,
+               "calls": "fl_update_positions_packed + fl_enqueue + fl_sync_packed"}
+        # the same through the float4 calls: the reference's vec4 layout, 16 B per node each way
+        hp4 = torch.empty((n, 4), dtype=torch.float32, pin_memory=True)
+        hv4 = torch.empty((n, 4), dtype=torch.float32, pin_memory=True)
+        eng.sync_into(hp4.data_ptr(), hv4.data_ptr())
+        hp4n = hp4.numpy()
+        a3 = al[total + 1 + k:total + 1 + 2 * k]
+        barrier()
+        t0 = time.perf_counter()
+        for i in range(k):
+            eng.update_positions(0, hp4n)
+            eng.enqueue(a3[i:i + 1], decay)
+            eng.sync_into(hp4.data_ptr(), hv4.data_ptr())
+        barrier()
+        ms4 = (time.perf_counter() - t0) * 1e3 / k
+        if world > 1:
+            t = torch.tensor([ms4], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms4 = float(t.item())
+        e2e_float4 = {"value": ms4 / world, "unit": UNIT, "h2d_bytes_per_step": 16 * n + 8,
+                      "d2h_bytes_per_step": 32 * n, "calls": "fl_update_positions + fl_enqueue + fl_sync"}
 
     dev_bytes = eng.query(Q_DEVICE_BYTES)
     peaks, peak_kind = measured_peaks()
@@ -743,6 +765,7 @@ def main():
             "gpu_launches": int(launches), "clocks": clk, "roofline": roof, "kernels": kernels}
     if e2e:
         line["e2e"] = e2e
+        line["e2e_float4"] = e2e_float4
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         ms_cpu, t = cpu_baseline(xyz, src, dst, n)
         line["cpu_baseline"] = {"value": ms_cpu, "unit": UNIT, "cores": 1, "kind": "port",
