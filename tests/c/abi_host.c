@@ -76,9 +76,18 @@ int main(int argc, char** argv) {
   CHECK(fl_enqueue(sim, alphas, ticks, 0.6));
   float* out = malloc(sizeof(float) * 4 * (size_t)n);
   CHECK(fl_sync(sim, out, NULL));
+  /* the packed readback carries the same x, y, z */
+  float* packed = malloc(sizeof(float) * 3 * (size_t)n);
+  CHECK(fl_sync_packed(sim, packed, NULL));
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < 3; ++k)
+      if (packed[3 * i + k] != out[4 * i + k]) {
+        fprintf(stderr, "fl_sync_packed differs from fl_sync at node %d\n", i);
+        return 3;
+      }
   for (int i = 0; i < n; ++i) printf("%.9g %.9g %.9g\n", out[4 * i], out[4 * i + 1], out[4 * i + 2]);
   fl_destroy(sim);
   free(pos4), free(src), free(dst), free(dist), free(strength), free(bias), free(deg);
-  free(charge), free(alphas), free(out);
+  free(charge), free(alphas), free(out), free(packed);
   return 0;
 }

@@ -1,6 +1,7 @@
 """A host written in plain C (tests/c/abi_host.c) against include/forcegpu.h alone: built with
-gcc, linked to libforcegpu.so, it steps a layout through the C ABI; the same layout stepped
-through the Python binding gives the same positions (one library, the same inputs)."""
+gcc, linked to libforcegpu.so, it steps a layout through the C ABI (and checks that
+fl_sync_packed reads back the same x, y, z as fl_sync); the same layout stepped through the
+Python binding gives the same positions (one library, the same inputs)."""
 import os
 import shutil
 import subprocess
