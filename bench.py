@@ -19,10 +19,19 @@ velocityDecay 0.4. A step is one tick. Synthetic, seeded data (no dataset is inv
             pipe view from interaction counts
   cpu_baseline  the oracle (FP64 C restatement of the reference's CPU simulation, one core) on
             a bounded sample: ticks of the same 1M-node layout
+  batched, served  compact runs of the batched engine (256 graphs x 100 ticks against the plain
+            engine one graph at a time) and of the layout server (40 jobs arriving at 2,000/s,
+            continuous batching, against serial plain solves): layouts/s, p50/p99 latency
 
-With --impl reference, the same workload runs on the CPU implementation (the oracle; the
-reference's own CPU code is JavaScript, and there is no Node.js on this machine).
-Multi-GPU: the single simulation does not shard; N ranks run N independent replicas.
+Timing: a pre-roll runs the warm-up and timed ticks twice from the start state and puts that
+state back (fl_upload_all), so that every block of ticks has been captured as a CUDA graph;
+then W warm-up ticks, then ticks W+1..W+K timed. The clock samples cover the pre-roll, the
+warm-up and the timed region.
+
+With --impl reference, the same workload and tick window run on the CPU implementation (the
+oracle; the reference's own CPU code is JavaScript, and there is no Node.js on this machine).
+Multi-GPU: the single simulation does not shard; N ranks run N independent replicas, and
+`value` stays the ms per tick of one simulation (the slowest replica).
 """
 from __future__ import annotations
 
@@ -54,9 +63,11 @@ BYTES_PER_NODE_TICK = 64 + 4 + 140 + 4 + 48
 # the walk's compulsory traffic per point: its sorted point (16) and permutation entry (4),
 # the child slots of the tree read once (24 B x ~2 per point), the velocity read + write (32)
 WALK_BYTES_PER_NODE = 16 + 4 + 48 + 32
-# DRAM bytes (read + write) of one walk launch at the default 1M-node workload, from ncu
-# (profiles/walk_1m_3d.md); reported as the roofline's measured traffic at that size only
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one walk launch of the default
+# 1M-node workload, from an ncu capture of that launch: a profiler figure, not something this
+# run can measure, so it is reported at that size only, with where it came from
 WALK_DRAM_BYTES_1M = 73.5e6
+WALK_DRAM_SOURCE = "ncu --set full capture of one k_walk launch, 1M-node workload"
 FLOPS_PER_INTERACTION = 20  # FP32 ops per accepted cell or point interaction
 FLOPS_PER_OPEN = 8          # per opened-cell test
 
@@ -64,12 +75,14 @@ FLOPS_PER_OPEN = 8          # per opened-cell test
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=300)
-    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--nodes", type=int, default=1_000_000)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-modes", action="store_true",
+                   help="leave the compact batched and served measurements out of the line")
     p.add_argument("--block", type=int, default=50,
                    help="ticks queued per enqueue call (a block seen twice runs as a CUDA graph)")
     p.add_argument("--no-autotune", action="store_true",
@@ -173,31 +186,50 @@ def cpu_baseline(xyz, src, dst, n, ticks=2):
     return dt / ticks * 1e3, ticks
 
 
+def plain_config(n, m):
+    """The workload of the headline line, the same in both arms."""
+    return {"workload": "3D layout, %d nodes, %d links, link+charge(theta 0.9)+center, "
+                        "phyllotaxis start" % (n, m), "nodes": n, "links": m}
+
+
+# seconds of timed CPU ticks the reference arm may spend (one 1M-node tick takes ~10 s on one core)
+REFERENCE_BUDGET_S = 240.0
+
+
 def run_reference(args):
-    """--impl reference: the CPU implementation of the path (the oracle port), rank 0 only."""
+    """--impl reference: the CPU implementation of the path (the oracle port of the reference's
+    CPU simulation; the reference's own is JavaScript and there is no Node.js), rank 0 only.
+    The same workload and tick window as the GPU arm: W untimed warm-up ticks, then ticks
+    W+1..W+K timed one by one, stopping early only if they exceed REFERENCE_BUDGET_S. One thread:
+    the reference's CPU force draws its jiggle from one sequential LCG stream, so its node loop
+    cannot be split across threads without changing its results."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     n = args.nodes
+    W, K = args.warmup, args.steps
     xyz, src, dst, _, _ = workload(n)
     import oracle
     o = oracle.OracleSim(n, 3, xyz=xyz)
     o.link(src, dst, distance=30.0)
     o.manybody(theta=0.9)
     o.center()
-    warm = max(1, min(args.warmup, 1))
-    steps = max(1, min(args.steps, 5))
-    o.tick(warm)
-    t0 = time.perf_counter()
-    o.tick(steps)
-    ms = (time.perf_counter() - t0) / steps * 1e3
+    if W:
+        o.tick(W)
+    times = []
+    while len(times) < K and sum(times) < REFERENCE_BUDGET_S:
+        t0 = time.perf_counter()
+        o.tick(1)
+        times.append(time.perf_counter() - t0)
+    ms = sum(times) / len(times) * 1e3
+    window = [W + 1, W + len(times)]
     line = {"metric": METRIC, "value": ms, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
-            "steps": steps, "warmup": warm, "ms_per_step": ms, "higher_is_better": False,
+            "steps": len(times), "warmup": W, "ms_per_step": ms, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "3D layout, %d nodes, %d links, link+charge(theta 0.9)+center"
-                                   % (n, len(src)), "nodes": n, "links": int(len(src))},
+            "config": plain_config(n, int(len(src))), "ticks_timed": window,
             "cpu_baseline": {"value": ms, "unit": UNIT, "cores": 1, "kind": "port",
-                             "sample": "ticks %d-%d of the layout, full size" % (warm + 1, warm + steps)},
+                             "sample": "ticks %d-%d of the layout, full size, one thread" % tuple(window),
+                             "host_cores": os.cpu_count()},
             "e2e": {"value": ms, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -312,33 +344,33 @@ def batch_workload(graphs, seed=2024):
     return specs
 
 
-def run_batched(args):
-    """--batched: layouts per second of the batched engine on a batch of many graphs, 300 ticks
-    each (every graph's own d3 alpha schedule), against the plain engine laying out a sample of
-    the same graphs one at a time (the same work per graph; layouts/s of the sample)."""
+def batched_measure(graphs, ticks, serial_sample, warmup, autotune, local=0):
+    """Layouts per second of the batched engine on `graphs` graphs of the batched workload,
+    `ticks` ticks each (every graph's own d3 alpha schedule), against the plain engine laying out
+    a sample of the same graphs one at a time (the same work per graph). The batched figure is
+    taken twice: device time of the queued ticks, and wall time from the graphs' upload to the
+    positions read back (the like of the serial figure, which is wall time per graph)."""
     import torch
     from forcegpu import Engine
-    from forcegpu._lib import desc_from_gpu
     from forcegpu.batch import Batch
     from forcegpu.graphs import link_defaults
-    ticks = 300
-    specs = batch_workload(args.graphs)
+    specs = batch_workload(graphs)
     nodes = int(sum(len(s.xyz) for s in specs))
-    b = Batch(0)
+    b = Batch(local)
     b.set_graphs(specs, ndim=3, seed=12345)
-    tuning = None if args.no_autotune else b.autotune(ticks=3)
-    stream = torch.cuda.ExternalStream(b.stream(), device=0)
-    # warm-up on a copy of the schedule, then the timed full layout from the start
-    b.run(args.warmup)
+    tuning = b.autotune(ticks=3) if autotune else None
+    stream = torch.cuda.ExternalStream(b.stream(), device=local)
+    # warm-up on the schedule's first ticks, then the timed full layout from the start
+    b.run(warmup)
     b.sync()
-    b.set_graphs(specs, ndim=3, seed=12345)
-    sched = b.alpha_schedule(ticks)
     clocks = Clocks()
     clocks.start()
     torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.set_graphs(specs, ndim=3, seed=12345)
+    sched = b.alpha_schedule(ticks)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     launches0 = b.launches()
-    t0 = time.perf_counter()
     e0.record(stream)
     b.enqueue(sched)
     e1.record(stream)
@@ -348,52 +380,67 @@ def run_batched(args):
     dev_ms = e0.elapsed_time(e1)
     launches = b.launches() - launches0
     assert np.isfinite(pos).all()
-    batched = len(specs) / (dev_ms / 1e3)
-    # the plain engine, one graph after another (a sample; each a full 300-tick layout)
+    dev_bytes = b.device_bytes()
+    b.close()
+    # the plain engine, one graph after another (a sample, each a full layout of `ticks` ticks)
     rng = np.random.default_rng(99)
-    sample = rng.choice(len(specs), min(args.serial_sample, len(specs)), replace=False)
-    eng = Engine(0)
+    sample = rng.choice(len(specs), min(serial_sample, len(specs)), replace=False)
+    eng = Engine(local)
     sample_nodes = 0
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     for gi in sample:
-        s = specs[gi]
-        n = len(s.xyz)
+        sp = specs[gi]
+        n = len(sp.xyz)
         sample_nodes += n
         pos4 = np.zeros((n, 4), np.float32)
-        pos4[:, :3] = s.xyz
+        pos4[:, :3] = sp.xyz
         eng.set_nodes(pos4, 3)
-        bias, strength = link_defaults(n, s.source, s.target)
-        ld = desc_from_gpu({"type": "link", "version": 1, "source": s.source, "target": s.target,
-                            "iterations": 1, "strengths": strength,
-                            "distances": np.full(len(s.source), 30.0), "bias": bias}, 1, n)
-        cd = desc_from_gpu({"type": "manyBody", "version": 1, "strengths": np.full(n, -30.0),
-                            "distanceMin2": 1.0, "distanceMax2": math.inf, "theta2": 0.81}, 2, n)
-        xd = desc_from_gpu({"type": "center", "x": 0, "y": 0, "z": 0, "strength": 1.0}, 3, n)
-        eng.set_forces([ld, cd, xd])
+        bias, strength = link_defaults(n, sp.source, sp.target)
+        eng.set_forces(plain_forces(n, sp.source, sp.target, bias, strength))
         al, _ = alphas(ticks)
         eng.enqueue(al, 0.6)
         eng.sync()
     serial_s = time.perf_counter() - t1
     eng.close()
     serial = len(sample) / serial_s
-    line = {"metric": "layouts/s, 2048 graphs x 300 ticks (batched)", "value": batched,
-            "unit": "layouts/s", "n_gpus": 1, "steps": ticks, "warmup": args.warmup,
-            "ms_per_step": dev_ms / ticks, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "%d 3D graphs, sizes log-uniform in [100, 20000] (seed 2024), "
-                                   "1.5 links/node, link+charge(theta 0.9)+center, 300 ticks each"
-                                   % len(specs), "graphs": len(specs), "nodes": nodes,
-                       "tuning": tuning},
-            "e2e": {"value": len(specs) / wall, "unit": "layouts/s",
-                    "h2d_bytes_per_step": 8 * len(specs), "d2h_bytes_per_step": 32 * nodes / ticks},
-            "serial_plain": {"value": serial, "unit": "layouts/s", "sample_graphs": len(sample),
-                             "sample_nodes": sample_nodes, "seconds": serial_s},
-            "speedup_vs_serial_plain": batched / serial,
-            "gpu_launches": int(launches), "clocks": clk,
-            "device_bytes": b.device_bytes()}
+    return {"graphs": len(specs), "nodes": nodes, "ticks": ticks,
+            "layouts_per_s": len(specs) / (dev_ms / 1e3),
+            "layouts_per_s_wall": len(specs) / wall,
+            "ms_per_tick": dev_ms / ticks,
+            "serial_plain_layouts_per_s": serial, "serial_sample_graphs": len(sample),
+            "serial_sample_nodes": sample_nodes,
+            "speedup_vs_serial_plain": len(specs) / wall / serial,
+            "gpu_launches": int(launches), "tuning": tuning, "clocks": clk,
+            "device_bytes": dev_bytes,
+            "workload": "%d 3D graphs, sizes log-uniform in [100, 20000] (seed 2024), 1.5 links/node, "
+                        "link+charge(theta 0.9)+center, %d ticks each" % (len(specs), ticks)}
+
+
+def batched_summary(args, local):
+    """The compact batched measurement of the default line: 256 graphs x 100 ticks."""
+    return batched_measure(256, 100, 16, 3, autotune=False, local=local)
+
+
+def run_batched(args):
+    """--batched: the batched configuration, 2,048 graphs x 300 ticks."""
+    m = batched_measure(args.graphs, 300, args.serial_sample, args.warmup, not args.no_autotune)
+    line = {"metric": "layouts/s, %d graphs x 300 ticks (batched)" % m["graphs"],
+            "value": m["layouts_per_s"], "unit": "layouts/s", "n_gpus": 1, "steps": 300,
+            "warmup": args.warmup, "ms_per_step": m["ms_per_tick"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": m["workload"], "graphs": m["graphs"], "nodes": m["nodes"],
+                       "tuning": m["tuning"]},
+            "e2e": {"value": m["layouts_per_s_wall"], "unit": "layouts/s",
+                    "h2d_bytes_per_step": 8 * m["graphs"],
+                    "d2h_bytes_per_step": 32 * m["nodes"] / 300},
+            "serial_plain": {"value": m["serial_plain_layouts_per_s"], "unit": "layouts/s",
+                             "sample_graphs": m["serial_sample_graphs"],
+                             "sample_nodes": m["serial_sample_nodes"]},
+            "speedup_vs_serial_plain": m["speedup_vs_serial_plain"],
+            "gpu_launches": m["gpu_launches"], "clocks": m["clocks"],
+            "device_bytes": m["device_bytes"]}
     print(json.dumps(line), flush=True)
-    b.close()
 
 
 def served_jobs(count, rate, seed=77):
@@ -417,15 +464,16 @@ def served_jobs(count, rate, seed=77):
     return jobs
 
 
-def run_served(args):
-    """--served: the layout server under Poisson arrivals (continuous batching), and the same
-    jobs solved one at a time on the plain engine, first come first served."""
+def served_measure(count, rate, local=0):
+    """The layout server under Poisson arrivals (continuous batching), and the same jobs solved
+    one at a time on the plain engine, first come first served (each job's service time
+    measured alone, the queue replayed against the same arrivals)."""
     import copy
     from forcegpu.serve import LayoutServer, latency_summary
-    jobs = served_jobs(args.jobs, args.rate)
+    jobs = served_jobs(count, rate)
     work = copy.deepcopy(jobs)
     # the server, in real time: arrivals are offsets from the start
-    srv = LayoutServer(hbm_budget=96 << 30, block=50).warmup()
+    srv = LayoutServer(device=local, hbm_budget=96 << 30, block=50).warmup()
     clocks = Clocks()
     clocks.start()
     t0 = time.perf_counter()
@@ -438,9 +486,9 @@ def run_served(args):
     srv.close()
     assert all(j.result is not None and np.isfinite(j.result).all() for j in work)
     served = latency_summary(work)
-    # serial plain solves, FIFO under the same arrivals: each job's service time measured alone
     serial = copy.deepcopy(jobs)
-    one = LayoutServer(hbm_budget=96 << 30, block=50, batching=False, plain_graphs=True).warmup()
+    one = LayoutServer(device=local, hbm_budget=96 << 30, block=50, batching=False,
+                       plain_graphs=True).warmup()
     service = []
     for j in serial:
         j.arrival = None
@@ -455,21 +503,35 @@ def run_served(args):
         lat.append(finish - j.arrival)
     lat = np.array(lat)
     node_ticks = sum(j.n * j.ticks for j in jobs)
-    line = {"metric": "served layouts/s and p99 latency (continuous batching)",
-            "value": len(jobs) / makespan, "unit": "layouts/s", "n_gpus": 1, "steps": len(jobs),
-            "warmup": 0, "ms_per_step": 1e3 * makespan / len(jobs), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "%d jobs, Poisson arrivals at %g/s, 2D/3D 50/50, sizes "
-                                   "log-uniform [500, 200000], 1-3 links/node, 30%% collide, "
-                                   "ticks uniform [100, 500]" % (len(jobs), args.rate),
-                       "node_ticks": int(node_ticks)},
-            "latency": served,
-            "serial_plain": {"layouts_per_s": len(jobs) / max(finish - jobs[0].arrival, 1e-9),
+    serial_lps = len(jobs) / max(finish - jobs[0].arrival, 1e-9)
+    return {"jobs": len(jobs), "rate_per_s": rate, "layouts_per_s": len(jobs) / makespan,
+            "makespan_s": makespan, "latency": served,
+            "serial_plain": {"layouts_per_s": serial_lps,
                              "p50_s": float(np.percentile(lat, 50)),
                              "p99_s": float(np.percentile(lat, 99)),
                              "busy_seconds": float(sum(service))},
-            "clocks": clk}
-    line["speedup_vs_serial_plain"] = line["value"] / line["serial_plain"]["layouts_per_s"]
+            "speedup_vs_serial_plain": len(jobs) / makespan / serial_lps,
+            "node_ticks": int(node_ticks), "clocks": clk,
+            "workload": "%d jobs, Poisson arrivals at %g/s, 2D/3D 50/50, sizes log-uniform "
+                        "[500, 200000], 1-3 links/node, 30%% collide, ticks uniform [100, 500]"
+                        % (len(jobs), rate)}
+
+
+def served_summary(args, local):
+    """The compact served measurement of the default line: 40 jobs arriving at 2,000/s."""
+    return served_measure(40, 2000.0, local)
+
+
+def run_served(args):
+    """--served: the served configuration."""
+    m = served_measure(args.jobs, args.rate)
+    line = {"metric": "served layouts/s and p99 latency (continuous batching)",
+            "value": m["layouts_per_s"], "unit": "layouts/s", "n_gpus": 1, "steps": m["jobs"],
+            "warmup": 0, "ms_per_step": 1e3 * m["makespan_s"] / m["jobs"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": m["workload"], "node_ticks": m["node_ticks"]},
+            "latency": m["latency"], "serial_plain": m["serial_plain"],
+            "speedup_vs_serial_plain": m["speedup_vs_serial_plain"], "clocks": m["clocks"]}
     print(json.dumps(line), flush=True)
 
 
@@ -573,6 +635,18 @@ def run_config2(args):
     print(json.dumps(line), flush=True)
 
 
+def plain_forces(n, src, dst, bias, strength):
+    """The benchmark's force list: link (distance 30, d3's default strength and bias), many-body
+    (-30, theta 0.9), center."""
+    from forcegpu._lib import desc_from_gpu
+    links = {"type": "link", "version": 1, "source": src, "target": dst, "iterations": 1,
+             "strengths": strength, "distances": np.full(len(src), 30.0), "bias": bias}
+    charge = {"type": "manyBody", "version": 1, "strengths": np.full(n, -30.0), "distanceMin2": 1.0,
+              "distanceMax2": math.inf, "theta2": 0.81}
+    center = {"type": "center", "x": 0, "y": 0, "z": 0, "strength": 1.0}
+    return [desc_from_gpu(links, 1, n), desc_from_gpu(charge, 2, n), desc_from_gpu(center, 3, n)]
+
+
 def main():
     args = parse()
     if args.config2:
@@ -598,39 +672,28 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
-    import forcegpu
     from forcegpu import Engine
     from forcegpu._lib import (Q_DEVICE_BYTES, Q_LAUNCHES, Q_WALK_APPLIES, Q_WALK_OPENS,
-                               Q_WALK_RARE, Q_WALK_TESTS, Q_WALK_USEFUL, TUNE_WALK_GROUP,
-                               desc_from_gpu)
+                               Q_WALK_RARE, Q_WALK_TESTS, Q_WALK_USEFUL, TUNE_WALK_GROUP)
 
     n = args.nodes
+    W, K = args.warmup, args.steps
     xyz, src, dst, bias, strength = workload(n)
     pos4 = np.zeros((n, 4), np.float32)
     pos4[:, :3] = xyz
     eng = Engine(local)
     eng.set_nodes(pos4, 3)
-    links = {"type": "link", "version": 1, "source": src, "target": dst, "iterations": 1,
-             "strengths": strength, "distances": np.full(len(src), 30.0), "bias": bias}
-    d_link, keep_l = desc_from_gpu(links, 1, n)
-    charge = {"type": "manyBody", "version": 1, "strengths": np.full(n, -30.0), "distanceMin2": 1.0,
-              "distanceMax2": math.inf, "theta2": 0.81}
-    d_charge, keep_c = desc_from_gpu(charge, 2, n)
-    d_center, keep_x = desc_from_gpu({"type": "center", "x": 0, "y": 0, "z": 0, "strength": 1.0}, 3, n)
-    descs = [(d_link, keep_l), (d_charge, keep_c), (d_center, keep_x)]
-    eng.set_forces(descs)
+    eng.set_forces(plain_forces(n, src, dst, bias, strength))
     eng.set_seed(12345)
     eng.set_tuning(TUNE_WALK_GROUP, args.walk_group)
     decay = 0.6
     tuning = None
-    if not args.no_autotune:  # outside the timed region, from the same start
+    if not args.no_autotune:  # outside the timed region, from the same start (state restored)
         tuning = eng.autotune(ticks=10, alpha=0.5, decay=decay)
     # ticks are queued in blocks of B, as an application queues a frame's or a batch's worth:
     # the engine runs a block it has seen before as one CUDA graph
-    B = max(1, min(args.block, args.steps))
-    warm = max(args.warmup, 2 * B)
-    total = warm + args.steps
-    al, _ = alphas(total + 2 * args.steps + B + 9)
+    B = max(1, min(args.block, K))
+    al, _ = alphas(W + K + 2 * K + B + 9)
 
     def run(first, count):
         k = first
@@ -640,28 +703,37 @@ def main():
             k += c
 
     stream = torch.cuda.ExternalStream(eng.stream(), device=local)
-    run(0, warm)  # warm-up
+    clocks = Clocks()
+    clocks.start()
+    # pre-roll, outside the count of warm-up ticks: the same W + K ticks twice from the start
+    # (fl_upload_all puts the start state back and keeps the captured blocks), so that every
+    # block the warm-up and the timed region queue has been seen twice and runs as a CUDA graph
+    for _ in range(2):
+        run(0, W)
+        run(W, K)
+        eng.idle()
+        eng.upload_all(pos4)
+    run(0, W)  # the warm-up: ticks 1..W
     eng.idle()
 
-    # timed region: K ticks, state resident, CUDA events on the engine's stream
+    # timed region: ticks W+1..W+K, state resident, CUDA events on the engine's stream
     def barrier():
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
     launches0 = eng.query(Q_LAUNCHES)
-    clocks = Clocks()
-    clocks.start()
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    run(warm, args.steps)
+    run(W, K)
     e1.record(stream)
     eng.idle()
     barrier()
     clk = clocks.stop()
     ms_total = e0.elapsed_time(e1)
     launches = eng.query(Q_LAUNCHES) - launches0
+    total = W + K
     # the per-kernel times: one more block, with the kernels timed one group at a time
     eng.profile(True)
     eng.enqueue(al[total:total + B], decay)
@@ -669,12 +741,11 @@ def main():
     prof = eng.profile_read()
     eng.profile(False)
     total += B
-    if world > 1:
+    if world > 1:  # the slowest replica
         t = torch.tensor([ms_total], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms_total = float(t.item())
-    ms_tick = ms_total / args.steps
-    value = ms_total / (args.steps * world)
+    ms_tick = ms_total / K
 
     # the walk's counted work, from one more tick with the walk's counters on (outside the
     # timed region): FP32 operations per launch for the FP32-pipe view of the roofline
@@ -686,28 +757,30 @@ def main():
                                               ("rare_rounds", Q_WALK_RARE))}
     eng.profile(False)
 
-    # e2e through the C ABI with pinned host buffers
-    e2e = None
+    def max_over_ranks(v):
+        if world > 1:
+            t = torch.tensor([v], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            v = float(t.item())
+        return v
+
+    # e2e through the C ABI with pinned host buffers, K ticks from the state reached
+    e2e = e2e_float4 = None
     if not args.no_e2e:
         hp = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
         hv = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
         eng.sync_packed_into(hp.data_ptr(), hv.data_ptr())
         hpn = hp.numpy()
-        k = args.steps
-        a2 = al[total + 1:total + 1 + k]
+        a2 = al[total + 1:total + 1 + K]
         barrier()
         t0 = time.perf_counter()
-        for i in range(k):
+        for i in range(K):
             eng.update_positions_packed(0, hpn)
             eng.enqueue(a2[i:i + 1], decay)
             eng.sync_packed_into(hp.data_ptr(), hv.data_ptr())
         barrier()
-        e2e_ms = (time.perf_counter() - t0) * 1e3 / k
-        if world > 1:
-            t = torch.tensor([e2e_ms], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            e2e_ms = float(t.item())
-        e2e = {"value": e2e_ms / world, "unit": UNIT, "h2d_bytes_per_step": 12 * n + 8,
+        e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / K)
+        e2e = {"value": e2e_ms, "unit": UNIT, "h2d_bytes_per_step": 12 * n + 8,
                "d2h_bytes_per_step": 24 * n,
                "calls": "fl_update_positions_packed + fl_enqueue + fl_sync_packed"}
         # the same through the float4 calls: the reference's vec4 layout, 16 B per node each way
@@ -715,20 +788,16 @@ def main():
         hv4 = torch.empty((n, 4), dtype=torch.float32, pin_memory=True)
         eng.sync_into(hp4.data_ptr(), hv4.data_ptr())
         hp4n = hp4.numpy()
-        a3 = al[total + 1 + k:total + 1 + 2 * k]
+        a3 = al[total + 1 + K:total + 1 + 2 * K]
         barrier()
         t0 = time.perf_counter()
-        for i in range(k):
+        for i in range(K):
             eng.update_positions(0, hp4n)
             eng.enqueue(a3[i:i + 1], decay)
             eng.sync_into(hp4.data_ptr(), hv4.data_ptr())
         barrier()
-        ms4 = (time.perf_counter() - t0) * 1e3 / k
-        if world > 1:
-            t = torch.tensor([ms4], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms4 = float(t.item())
-        e2e_float4 = {"value": ms4 / world, "unit": UNIT, "h2d_bytes_per_step": 16 * n + 8,
+        ms4 = max_over_ranks((time.perf_counter() - t0) * 1e3 / K)
+        e2e_float4 = {"value": ms4, "unit": UNIT, "h2d_bytes_per_step": 16 * n + 8,
                       "d2h_bytes_per_step": 32 * n, "calls": "fl_update_positions + fl_enqueue + fl_sync"}
 
     dev_bytes = eng.query(Q_DEVICE_BYTES)
@@ -739,7 +808,8 @@ def main():
     achieved = walk_bytes / (walk_avg * 1e-3) / 1e9 if walk_avg else None
     roof = {"bound": "hbm", "kernel": "k_walk", "achieved": achieved, "peak": peaks["hbm_gbs"],
             "unit": "GB/s", "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
-            "traffic": WALK_DRAM_BYTES_1M if n == 1_000_000 else None, "peak_kind": peak_kind,
+            "traffic": WALK_DRAM_BYTES_1M if n == 1_000_000 else None,
+            "traffic_source": WALK_DRAM_SOURCE if n == 1_000_000 else None, "peak_kind": peak_kind,
             "algorithmic_bytes_per_launch": walk_bytes, "avg_launch_ms": walk_avg,
             "tick_bytes": BYTES_PER_NODE_TICK * n,
             "tick_hbm_frac": BYTES_PER_NODE_TICK * n / (ms_tick * 1e-3) / 1e9 / peaks["hbm_gbs"]}
@@ -754,18 +824,27 @@ def main():
                     "per_point": {k: v / n for k, v in walk_count.items()}}
     kernels = {k: {"ms_per_tick": v[0] / B, "launches": v[1]} for k, v in prof.items()}
 
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": warm, "ms_per_step": ms_tick, "higher_is_better": False,
+    line = {"metric": METRIC, "value": ms_tick, "unit": UNIT, "n_gpus": world, "steps": K,
+            "warmup": W, "ms_per_step": ms_tick, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "3D layout, %d nodes, %d links, link+charge(theta 0.9)+center, "
-                                   "ticks %d-%d from the phyllotaxis start" % (n, len(src), warm + 1, warm + args.steps),
-                       "tick_block": B, "tuning": tuning,
-                       "nodes": n, "links": int(len(src)), "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "working set %.0f MB > 126 MB L2 (no flush)" % (dev_bytes / 1e6)},
+            "config": plain_config(n, len(src)),
+            "ticks_timed": [W + 1, W + K],
+            "preroll": "the same %d ticks twice before the warm-up, from the start state "
+                       "(fl_upload_all), so that every tick block runs as a CUDA graph" % (W + K),
+            "tick_block": B, "tuning": tuning,
+            "l2": "working set %.0f MB > 126 MB L2 (no flush)" % (dev_bytes / 1e6),
             "gpu_launches": int(launches), "clocks": clk, "roofline": roof, "kernels": kernels}
+    if world > 1:
+        line["replicas"] = world
+        line["aggregate_ticks_per_s"] = world * K / (ms_total * 1e-3)
+        line["value_note"] = "ms per tick of one simulation (the slowest of %d independent replicas)" % world
     if e2e:
         line["e2e"] = e2e
         line["e2e_float4"] = e2e_float4
+    eng.close()
+    if not args.no_modes:
+        line["batched"] = batched_summary(args, local)
+        line["served"] = served_summary(args, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         ms_cpu, t = cpu_baseline(xyz, src, dst, n)
         line["cpu_baseline"] = {"value": ms_cpu, "unit": UNIT, "cores": 1, "kind": "port",
@@ -773,7 +852,6 @@ def main():
                                 "host_cores": os.cpu_count()}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    eng.close()
     if world > 1:
         torch.distributed.destroy_process_group()
 

@@ -62,7 +62,8 @@ struct fl_batch {
   std::string err;
   int32_t ndim = 3, graphs = 0, n = 0, m = 0;
   Buf pos, vel[2], fix, mask, gid, off, prm, red, gr, alphas, charge, row, entry, code, errw;
-  Buf sort1, sort2, tree, gid_pos;
+  Buf sort1, sort2, tree, gid_pos, groups;
+  int32_t ngroups = 0;
   FlSortBufs sb{}, sb2{};
   FlTreeBufs tb{};
   int cur = 0;
@@ -146,7 +147,7 @@ void encode_batch_tick(fl_batch* b, const double* alpha, const FlTick* tk) {
   uint64_t* skeys = nullptr;
   uint32_t* perm = nullptr;
   uint32_t* gpos = b->gid_pos.as<uint32_t>();
-  FlSegs segs{G, b->off.as<int32_t>(), gid, gpos, gr};
+  FlSegs segs{G, b->off.as<int32_t>(), gid, gpos, gr, b->groups.as<uint2>(), b->ngroups};
   const bool side = b->aux != nullptr;
   if (n >= 2) {
     cudaStream_t ts = st;
@@ -272,9 +273,16 @@ int32_t fl_batch_set_graphs(fl_batch* b, int32_t ndim, int32_t graphs, const fl_
   std::vector<FlBatchParams> prm(graphs);
   bool neg = false, posv = false;
   double smax = 0, dmax_any = INFINITY;
+  // the walk's point groups: each graph's sorted positions in runs of 32 from its first one (a
+  // graph of one point has no tree and no group)
+  std::vector<uint2> groups;
   for (int32_t g = 0, at = 0; g < graphs; ++g) {
     off[g] = at;
     const fl_graph_desc& x = d[g];
+    double gmax = x.charge ? 0.0 : 30.0;
+    if (x.n >= 2)
+      for (int32_t j = 0; j < x.n; j += 32)
+        groups.push_back(make_uint2((uint32_t)(at + j), (uint32_t)(at + std::min(j + 32, x.n))));
     for (int32_t i = 0; i < x.n; ++i) {
       for (int k = 0; k < 4; ++k) {
         const float p = k < ndim ? x.pos4[4 * (size_t)i + k] : 0.f;
@@ -286,9 +294,13 @@ int32_t fl_batch_set_graphs(fl_batch* b, int32_t ndim, int32_t graphs, const fl_
       charge[at + i] = std::isfinite(c) ? c : 0.f;
       neg = neg || charge[at + i] < 0.f, posv = posv || charge[at + i] > 0.f;
       smax = std::max(smax, (double)std::fabs(charge[at + i]));
+      gmax = std::max(gmax, (double)std::fabs(charge[at + i]));
     }
+    // the graph's own fixed-point scale, as a lone simulation of it chooses it: its cells come
+    // out the same bit for bit, alone or in any batch
     prm[g] = FlBatchParams{x.theta2, x.distance_min2, x.distance_max2, x.center_x, x.center_y,
-                           x.center_z, x.center_strength, 1.0 - x.velocity_decay};
+                           x.center_z, x.center_strength, 1.0 - x.velocity_decay,
+                           fl_fixed_exponent(x.n, gmax * (ndim == 1 ? 8192.0 : 1.0)), x.tick0};
     if (x.distance_max2 < 3e38) dmax_any = 1.0;  // some graph has a finite distanceMax
     at += x.n;
     off[g + 1] = at;
@@ -301,6 +313,8 @@ int32_t fl_batch_set_graphs(fl_batch* b, int32_t ndim, int32_t graphs, const fl_
   std::vector<int32_t> row((size_t)n + 1, 0);
   std::vector<int32_t> src((size_t)std::max<int64_t>(m, 1)), dst(src.size());
   std::vector<float> dist(src.size()), str(src.size()), bias(src.size());
+  // each link's index within its own graph: the jiggle of a link is the graph's own
+  std::vector<uint32_t> local((size_t)std::max<int64_t>(m, 1));
   {
     int64_t k = 0;
     for (int32_t g = 0; g < graphs; ++g) {
@@ -315,6 +329,7 @@ int32_t fl_batch_set_graphs(fl_batch* b, int32_t ndim, int32_t graphs, const fl_
       for (int32_t j = 0; j < x.m; ++j, ++k) {
         const int32_t a = x.source[j], c = x.target[j];
         src[k] = off[g] + a, dst[k] = off[g] + c;
+        local[k] = (uint32_t)j;
         dist[k] = x.link_distance ? x.link_distance[j] : 30.f;
         // src/link.js:73-75, :36-38: bias = count(source) / (count(source) + count(target)),
         // strength = 1 / min(count(source), count(target))
@@ -334,12 +349,12 @@ int32_t fl_batch_set_graphs(fl_batch* b, int32_t ndim, int32_t graphs, const fl_
     std::memcpy(&entry[4 * (size_t)e], &c, 4);
     entry[4 * (size_t)e + 1] = dist[k], entry[4 * (size_t)e + 2] = str[k];
     entry[4 * (size_t)e + 3] = (float)(1.0 - (double)bias[k]);
-    code[e] = 2u * (uint32_t)k;
+    code[e] = 2u * local[k];
     e = cur[c]++;
     std::memcpy(&entry[4 * (size_t)e], &a, 4);
     entry[4 * (size_t)e + 1] = dist[k], entry[4 * (size_t)e + 2] = str[k];
     entry[4 * (size_t)e + 3] = bias[k];
-    code[e] = 2u * (uint32_t)k + 1u;
+    code[e] = 2u * local[k] + 1u;
   }
   // device buffers
   const size_t N = (size_t)std::max<int64_t>(n, 1);
@@ -362,6 +377,8 @@ int32_t fl_batch_set_graphs(fl_batch* b, int32_t ndim, int32_t graphs, const fl_
   FB_CK(b, b->sort1.reserve(fl_sort_bytes(n)));
   FB_CK(b, b->sort2.reserve(fl_sort_bytes(n)));
   FB_CK(b, b->tree.reserve(fl_tree_bytes(n)));
+  b->ngroups = (int32_t)groups.size();
+  FB_CK(b, b->groups.reserve(8 * std::max<size_t>(groups.size(), 1)));
   fl_sort_carve(&b->sb, b->sort1.p, n);
   fl_sort_carve(&b->sb2, b->sort2.p, n);
   fl_tree_carve(&b->tb, b->tree.p, n, ndim);
@@ -378,6 +395,8 @@ int32_t fl_batch_set_graphs(fl_batch* b, int32_t ndim, int32_t graphs, const fl_
   FB_CK(b, cudaMemcpyAsync(b->prm.p, prm.data(), sizeof(FlBatchParams) * (size_t)graphs,
                            cudaMemcpyHostToDevice, st));
   FB_CK(b, cudaMemcpyAsync(b->row.p, row.data(), 4 * ((size_t)n + 1), cudaMemcpyHostToDevice, st));
+  if (!groups.empty())
+    FB_CK(b, cudaMemcpyAsync(b->groups.p, groups.data(), 8 * groups.size(), cudaMemcpyHostToDevice, st));
   if (m) {
     FB_CK(b, cudaMemcpyAsync(b->entry.p, entry.data(), 32 * (size_t)m, cudaMemcpyHostToDevice, st));
     FB_CK(b, cudaMemcpyAsync(b->code.p, code.data(), 8 * (size_t)m, cudaMemcpyHostToDevice, st));

@@ -89,11 +89,75 @@ __device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
 }  // namespace fl
 
 // Reduction record shared by the bounding-box and centre passes (device memory, reset before
-// each use): ordered-uint min/max of positions and their FP64 sum.
+// each use): ordered-uint min/max of positions, and their exact sum.
+//
+// The sums are exact integers: every position x contributes x * 2^kSumFracBits truncated toward
+// zero, as a 128-bit two's-complement integer (sum_hi:sum_lo), and integer addition does not
+// depend on its order. So the centre force's mean is the same whatever the grid, the blocks'
+// order or the graph's place in a batch: a layout is bit-reproducible, alone or among others.
+// The range covers |x| < 2^50 at a resolution of 2^-40 (sums of up to 2^28 positions cannot
+// overflow); a position outside it (or not finite) is counted in `bad`, and the mean is NaN.
+constexpr int kSumFracBits = 40;
 struct FlReduce {
   uint32_t lo[3];
   uint32_t hi[3];
-  uint32_t pad[2];
-  double sum[3];
-  double pad2;
+  uint32_t bad;
+  uint32_t pad;
+  unsigned long long sum_lo[3];
+  unsigned long long sum_hi[3];
 };
+
+namespace fl {
+
+// x * 2^kSumFracBits, truncated toward zero, as an exact 128-bit integer, from x's bits alone
+// (no floating-point rounding); counts x in `bad` when it is outside the range.
+__device__ __forceinline__ __int128 fx128(float x, uint32_t& bad) {
+  const uint32_t b = __float_as_uint(x);
+  const int e = (int)((b >> 23) & 255u);
+  if (e == 0) return 0;  // zero or subnormal: below the resolution
+  if (e >= 127 + 50) {   // |x| >= 2^50, inf or NaN
+    ++bad;
+    return 0;
+  }
+  const unsigned __int128 m = (unsigned __int128)((b & 0x7fffffu) | 0x800000u);  // x = m 2^(e-150)
+  const int sh = e - 150 + kSumFracBits;
+  const unsigned __int128 v = sh >= 0 ? m << sh : (sh > -24 ? m >> -sh : (unsigned __int128)0);
+  return (b >> 31) ? -(__int128)v : (__int128)v;
+}
+
+__device__ __forceinline__ __int128 shfl_xor128(__int128 v, int o) {
+  unsigned long long lo = (unsigned long long)v;
+  unsigned long long hi = (unsigned long long)((unsigned __int128)v >> 64);
+  lo = __shfl_xor_sync(FL_FULL, lo, o);
+  hi = __shfl_xor_sync(FL_FULL, hi, o);
+  return (__int128)(((unsigned __int128)hi << 64) | lo);
+}
+
+__device__ __forceinline__ __int128 shfl_down128(__int128 v, int o) {
+  unsigned long long lo = (unsigned long long)v;
+  unsigned long long hi = (unsigned long long)((unsigned __int128)v >> 64);
+  lo = __shfl_down_sync(FL_FULL, lo, o);
+  hi = __shfl_down_sync(FL_FULL, hi, o);
+  return (__int128)(((unsigned __int128)hi << 64) | lo);
+}
+
+// Adds v to the 128-bit accumulator (hi:lo) in global or shared memory. The carry out of the
+// low word is taken from the value the low atomic replaced, so the total number of carries is
+// that of the whole sum, in any order: the result is exact and order-independent.
+__device__ __forceinline__ void atomic_add128(unsigned long long* lo, unsigned long long* hi,
+                                              __int128 v) {
+  const unsigned long long a = (unsigned long long)v;
+  const unsigned long long b = (unsigned long long)((unsigned __int128)v >> 64);
+  const unsigned long long old = atomicAdd(lo, a);
+  const unsigned long long c = b + (old + a < old ? 1ull : 0ull);
+  if (c) atomicAdd(hi, c);
+}
+
+// The sum of axis k of a reduction record as a double (NaN when a position was out of range).
+__device__ __forceinline__ double sum_of(const FlReduce& r, int k) {
+  if (r.bad) return __longlong_as_double(0x7ff8000000000000ll);
+  const double v = (double)(long long)r.sum_hi[k] * 18446744073709551616.0 + (double)r.sum_lo[k];
+  return v * 9.094947017729282379150390625e-13;  // 2^-40
+}
+
+}  // namespace fl

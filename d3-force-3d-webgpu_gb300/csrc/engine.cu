@@ -140,6 +140,7 @@ struct fl_sim {
   int sort_passes = 0;  // tuning FL_TUNE_SORT_PASSES (0: the default)
   int walk_blocks = 0;  // tuning FL_TUNE_WALK_BLOCKS (0: as many as fit)
   int collide_cell = 100;  // tuning FL_TUNE_COLLIDE_CELL (percent of the largest diameter)
+  uint32_t test_lookback = 0;  // tuning FL_TUNE_TEST_LOOKBACK (0: off)
   bool profiling = false;
   int prof_level = 0;
   DevMem wstats;  // walk counters (profiling level 2)
@@ -151,7 +152,9 @@ struct fl_sim {
 
 namespace {
 
-std::string g_create_error;
+// the message of the last failed call that takes no simulation (fl_create, the sorts), one per
+// host thread: two threads failing at once do not race on it
+thread_local std::string g_create_error;
 
 int32_t fail(fl_sim* s, int32_t code, const std::string& msg) {
   if (s) s->err = msg;
@@ -393,6 +396,7 @@ void encode_tree(fl_sim* s, Pass* p, const FlReduce* box, cudaStream_t st) {
     if (by_rank) {
       r = fl_sort_rank(&p->sb, n, st, &s->launches);
     } else {
+      p->sb.test_spins = s->test_lookback;
       r = fl_sort_passes(&p->sb, n, lo_sort, s->errw.as<uint32_t>(), st, &s->launches);
       r = fl_sort_runfix(&p->sb, n, lo_bit, lo_sort, r, st, &s->launches);
     }
@@ -756,6 +760,32 @@ int32_t fl_set_nodes(fl_sim* s, int32_t n, int32_t ndim, const float* pos4, cons
   return FL_OK;
 }
 
+int32_t fl_upload_all(fl_sim* s, const float* pos4, const float* vel4, const float* fix4,
+                      const uint32_t* mask) {
+  int32_t rc = check_sim(s);
+  if (rc) return rc;
+  if (s->n > 0 && !pos4) return fail(s, FL_E_ARG, "positions are NULL");
+  FL_CK(s, cudaStreamSynchronize(s->st));
+  // the state starts over in the first velocity and reduction buffers, as after fl_set_nodes,
+  // so that a tick block captured from that start replays from this one
+  s->cur = 0;
+  s->red_cur = 0;
+  s->pre_valid = false;
+  const size_t b4 = 16 * (size_t)s->n;
+  if (s->n) {
+    FL_CK(s, cudaMemcpyAsync(s->pos.p, pos4, b4, cudaMemcpyHostToDevice, s->st));
+    if (vel4) FL_CK(s, cudaMemcpyAsync(s->vel[0].p, vel4, b4, cudaMemcpyHostToDevice, s->st));
+    else FL_CK(s, cudaMemsetAsync(s->vel[0].p, 0, b4, s->st));
+    if (fix4) FL_CK(s, cudaMemcpyAsync(s->fix.p, fix4, b4, cudaMemcpyHostToDevice, s->st));
+    else FL_CK(s, cudaMemsetAsync(s->fix.p, 0, b4, s->st));
+    if (mask)
+      FL_CK(s, cudaMemcpyAsync(s->mask.p, mask, 4 * (size_t)s->n, cudaMemcpyHostToDevice, s->st));
+    else FL_CK(s, cudaMemsetAsync(s->mask.p, 0, 4 * (size_t)s->n, s->st));
+  }
+  FL_CK(s, cudaStreamSynchronize(s->st));
+  return FL_OK;
+}
+
 int32_t fl_update_positions(fl_sim* s, int32_t first, int32_t count, const float* pos4) {
   int32_t rc = check_sim(s);
   if (rc) return rc;
@@ -1041,6 +1071,10 @@ int32_t fl_set_tuning(fl_sim* s, int32_t key, int32_t value) {
       if (value < 100 || value > 1000) return fail(s, FL_E_ARG, "collide cell must be 100..1000 percent");
       s->collide_cell = value;
       return FL_OK;
+    case FL_TUNE_TEST_LOOKBACK:
+      if (value < 0 || value > 65536) return fail(s, FL_E_ARG, "test look-back polls must be 0..65536");
+      s->test_lookback = (uint32_t)value;
+      return FL_OK;
     default:
       return fail(s, FL_E_ARG, "unknown tuning key");
   }
@@ -1270,6 +1304,21 @@ int32_t fl_debug_tree(fl_sim* s, int32_t index, uint64_t* keys, uint32_t* perm, 
   if (right) FL_CK(s, cudaMemcpy(right, p->tb.right, 4 * m, cudaMemcpyDeviceToHost));
   if (depth) FL_CK(s, cudaMemcpy(depth, p->tb.depth, m, cudaMemcpyDeviceToHost));
   if (cube5) FL_CK(s, cudaMemcpy(cube5, p->cube.p, 20, cudaMemcpyDeviceToHost));
+  return FL_OK;
+}
+
+int32_t fl_debug_links(fl_sim* s, int32_t index, int32_t* row, int32_t* other, uint32_t* code) {
+  int32_t rc = check_sim(s);
+  if (rc) return rc;
+  if (index < 0 || index >= (int32_t)s->plan.size()) return fail(s, FL_E_ARG, "no such force");
+  const Pass* p = s->plan[index].get();
+  if (p->type != FL_FORCE_LINK || !p->row.p) return fail(s, FL_E_STATE, "force is not a link force");
+  FL_CK(s, cudaStreamSynchronize(s->st));
+  const size_t e = 2 * (size_t)p->m;
+  if (row) FL_CK(s, cudaMemcpy(row, p->row.p, 4 * ((size_t)s->n + 1), cudaMemcpyDeviceToHost));
+  if (code && e) FL_CK(s, cudaMemcpy(code, p->code.p, 4 * e, cudaMemcpyDeviceToHost));
+  if (other && e)  // the other end's index is the first word of each float4 entry
+    FL_CK(s, cudaMemcpy2D(other, 4, p->entry.p, 16, 4, e, cudaMemcpyDeviceToHost));
   return FL_OK;
 }
 

@@ -25,7 +25,9 @@ struct FlGraph {
   float2 shift[3];        // the centre force's shift per axis (hi + lo), 0 without one
   int32_t first, count;   // nodes [first, first + count)
   int32_t frozen;         // 1: the graph sits this tick out (its alpha was given as negative)
-  float pad;
+  int32_t fx;             // scale exponent of the graph's fixed-point cell sums
+  uint32_t tick0;         // the graph's own tick count when the batch started (jiggle steps)
+  uint32_t pad;
 };
 // A batch of independent graphs, concatenated: graph g owns nodes [off[g], off[g+1]) and, after
 // the tree's sort (by graph, then Morton code), the same range of sorted positions. Kernels
@@ -36,6 +38,10 @@ struct FlSegs {
   const uint32_t* gid_node;  // [n] graph of each node
   const uint32_t* gid_pos;   // [n] graph of each sorted position
   const FlGraph* g;          // [graphs]
+  // the tree walk's point groups: sorted positions [x, y), up to 32 of one graph each, so that a
+  // graph's groups (and so every sum of its walk) are the same whatever else is in the batch
+  const uint2* groups;       // [ngroups]
+  int ngroups;
 };
 
 // A graph's fixed parameters in a batch: many-body theta^2, distanceMin^2, distanceMax^2; the
@@ -44,6 +50,9 @@ struct FlBatchParams {
   double theta2, dmin2, dmax2;
   double cx, cy, cz, cstrength;
   double decay;
+  int32_t fx;      // scale exponent of the fixed-point cell sums, from the graph's own size and
+                   // strengths (as a lone simulation of that graph chooses it)
+  uint32_t tick0;  // the graph's tick count when the batch started
 };
 void fl_launch_breduce(const float4* pos, int n, int ndim, const uint32_t* gid, FlReduce* red,
                        cudaStream_t st);
@@ -71,6 +80,10 @@ struct FlSortBufs {
   uint32_t longs_cap;
   int64_t cap;         // pairs the buffers hold
   int64_t tiles_cap;   // tiles of kSortTileSmall pairs the look-back words have room for
+  // 0, or a test of the bounded look-back: every wait gives up after this many polls, and the
+  // first digit pass withholds tile 0's counts, so that the waits run out (the tiles that gave
+  // up count their predecessors' keys themselves: the result stays exact, FL_ERR_LOOKBACK is set)
+  uint32_t test_spins;
 };
 constexpr int kSortCounters = 16;
 // A onesweep tile: kSortItems pairs per thread; 1024 threads, or 256 for up to kSortSmallMax

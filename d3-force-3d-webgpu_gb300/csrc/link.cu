@@ -23,10 +23,12 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kLong = 64;
 
+// One entry's term. The entry's code word (link * 2 + end) is read only for a zero component,
+// which is rare: the common case streams the float4 entries alone.
 __device__ __forceinline__ void link_term(const float4* __restrict__ pos,
                                           const float4* __restrict__ vel, float3 me, float4 e,
-                                          uint32_t code, int ndim, float alpha, uint32_t step,
-                                          uint32_t seed, float3& acc) {
+                                          const uint32_t* __restrict__ codep, int ndim,
+                                          float alpha, uint32_t step, uint32_t seed, float3& acc) {
   const int j = __float_as_int(e.x);
   const float4 pj = __ldg(pos + j), vj = __ldg(vel + j);
   float dx = (pj.x + vj.x) - me.x;
@@ -34,6 +36,7 @@ __device__ __forceinline__ void link_term(const float4* __restrict__ pos,
   float dz = ndim > 2 ? (pj.z + vj.z) - me.z : 0.f;
   if (dx == 0.f || (ndim > 1 && dy == 0.f) || (ndim > 2 && dz == 0.f)) {
     // jiggle(link): the same value at both ends, negated at the target
+    const uint32_t code = __ldg(codep);
     const uint32_t link = code >> 1;
     const float sgn = (code & 1u) ? -1.f : 1.f;
     if (dx == 0.f) dx = sgn * fl::jiggle(link, 0x7fffffffu, 0, step, seed);
@@ -65,6 +68,7 @@ __global__ void __launch_bounds__(kThreads) k_link(const float4* __restrict__ po
   if (gr && live) {  // a batch: the node's graph's alpha; a graph sitting the tick out keeps v
     const FlGraph& g = gr[gid[i]];
     alpha = g.alpha, frozen = g.frozen != 0;
+    step += g.tick0;  // the graph's own step (its jiggles do not depend on the batch)
   }
   int r0 = 0, r1 = 0;
   float4 p = make_float4(0, 0, 0, 0), v = p;
@@ -76,7 +80,7 @@ __global__ void __launch_bounds__(kThreads) k_link(const float4* __restrict__ po
   float3 acc = make_float3(0.f, 0.f, 0.f);
   const bool longrow = !frozen && (r1 - r0) > kLong;
   if (!longrow && !frozen)
-    for (int e = r0; e < r1; ++e) link_term(pos, vel_in, me, __ldg(entry + e), __ldg(code + e), ndim, alpha, step, seed, acc);
+    for (int e = r0; e < r1; ++e) link_term(pos, vel_in, me, __ldg(entry + e), code + e, ndim, alpha, step, seed, acc);
   // long rows: the warp takes them one at a time
   uint32_t longs = __ballot_sync(FL_FULL, longrow);
   while (longs) {
@@ -86,9 +90,10 @@ __global__ void __launch_bounds__(kThreads) k_link(const float4* __restrict__ po
     const float3 m = make_float3(__shfl_sync(FL_FULL, me.x, src), __shfl_sync(FL_FULL, me.y, src),
                                  __shfl_sync(FL_FULL, me.z, src));
     const float am = __shfl_sync(FL_FULL, alpha, src);
+    const uint32_t sm = __shfl_sync(FL_FULL, step, src);
     float3 part = make_float3(0.f, 0.f, 0.f);
     for (int e = a + lane; e < b; e += 32)
-      link_term(pos, vel_in, m, __ldg(entry + e), __ldg(code + e), ndim, am, step, seed, part);
+      link_term(pos, vel_in, m, __ldg(entry + e), code + e, ndim, am, sm, seed, part);
     part.x = fl::warp_sum(part.x), part.y = fl::warp_sum(part.y), part.z = fl::warp_sum(part.z);
     if (lane == src) acc = part;
   }

@@ -84,7 +84,7 @@ template <int kThreads>
 __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_onesweep(
     const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
     uint32_t* __restrict__ vout, int64_t n, int shift, const uint32_t* __restrict__ ghist,
-    uint32_t* status, uint32_t* ticket, uint32_t* err) {
+    uint32_t* status, uint32_t* ticket, uint32_t* err, uint32_t spin_limit, int hold) {
   constexpr int kWarps = kThreads / 32, kTile = kThreads * kItems;
   extern __shared__ __align__(16) unsigned char smem[];
   uint64_t* sk = reinterpret_cast<uint64_t*>(smem);
@@ -94,6 +94,7 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_onesweep(
   __shared__ uint32_t s_texcl[256];
   __shared__ uint32_t s_base[256];
   __shared__ uint32_t s_warp[kWarps];
+  __shared__ uint32_t s_fall[256];
   __shared__ uint32_t s_tile;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -150,12 +151,14 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_onesweep(
       s_whist[w][d] = run;
       run += t;
     }
-    fl::st_relaxed(mine, (tile == 0 ? kFlagPre : kFlagAgg) | run);
+    // `hold` (a test of the bounded wait): tile 0 keeps its counts to itself in this pass
+    if (!(hold && tile == 0)) fl::st_relaxed(mine, (tile == 0 ? kFlagPre : kFlagAgg) | run);
   }
   const uint32_t tx = block_excl_scan<kThreads>(run, s_warp, &total);
   if (dt) s_texcl[d] = tx;
 
   uint32_t prefix = 0;
+  bool gave_up = false;
   if (dt && tile > 0) {
     // look back kLook tiles per round (independent loads), up to the nearest inclusive prefix:
     // all tiles of a pass start at once and publish their counts together, so the inclusive
@@ -181,8 +184,8 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_onesweep(
       }
       if (done) break;
       if (used == 0) {
-        if (++spins > FL_SPIN_LIMIT) {
-          atomicOr(err, FL_ERR_LOOKBACK);
+        if (++spins > spin_limit) {
+          gave_up = true;
           break;
         }
         if (spins > 64) __nanosleep(100);
@@ -190,10 +193,25 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_onesweep(
       }
       p -= used;
     }
-    fl::st_relaxed(mine, kFlagPre | (prefix + run));
+    if (!gave_up) fl::st_relaxed(mine, kFlagPre | (prefix + run));
   }
   if (dt) s_base[d] = s_gexcl[d] + prefix - s_texcl[d];
-  __syncthreads();
+  if (__syncthreads_or(gave_up)) {
+    // a wait gave up (a predecessor tile never published): the block counts the digits of every
+    // key before its tile itself, reading the pass's input, which is complete. Slower, still
+    // exact; the error bit reports that the wait gave up.
+    if (tid < 256) s_fall[tid] = 0u;
+    __syncthreads();
+    for (int64_t i = tid; i < tbase; i += kThreads) atomicAdd(&s_fall[(uint32_t)(kin[i] >> shift) & 255u], 1u);
+    __syncthreads();
+    if (dt) {
+      prefix = s_fall[d];
+      s_base[d] = s_gexcl[d] + prefix - s_texcl[d];
+      fl::st_relaxed(mine, kFlagPre | (prefix + run));
+    }
+    if (tid == 0) atomicOr(err, FL_ERR_LOOKBACK);
+    __syncthreads();
+  }
 
 #pragma unroll
   for (int j = 0; j < kItems; ++j) {
@@ -208,7 +226,7 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_onesweep(
   for (int i = tid; i < valid; i += kThreads) {
     uint64_t k = sk[i];
     uint32_t g = s_base[(uint32_t)(k >> shift) & 255u] + (uint32_t)i;
-    if (g < (uint64_t)n) {  // always true unless a look-back gave up (reported in err)
+    if (g < (uint64_t)n) {  // always true: a guard against a corrupted histogram
       kout[g] = k;
       vout[g] = sv[i];
     }
@@ -375,13 +393,14 @@ static bool first_on_device(std::atomic<uint64_t>& done) {
 template <int T>
 void launch_pass(const uint64_t* kin, const uint32_t* vin, uint64_t* kout, uint32_t* vout,
                  int64_t n, int shift, const uint32_t* ghist, uint32_t* status, uint32_t* ticket,
-                 uint32_t* err, cudaStream_t st) {
+                 uint32_t* err, uint32_t spin_limit, int hold, cudaStream_t st) {
   static std::atomic<uint64_t> configured{0};
   const size_t dyn = (size_t)T * kItems * 12;
   if (first_on_device(configured))
     cudaFuncSetAttribute(k_onesweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
   const int64_t tiles = (n + T * kItems - 1) / (T * kItems);
-  k_onesweep<T><<<(int)tiles, T, dyn, st>>>(kin, vin, kout, vout, n, shift, ghist, status, ticket, err);
+  k_onesweep<T><<<(int)tiles, T, dyn, st>>>(kin, vin, kout, vout, n, shift, ghist, status, ticket,
+                                            err, spin_limit, hold);
 }
 uint32_t longs_cap_for(int64_t n) { return (uint32_t)(n / (kRunShort + 1) + 1); }
 
@@ -428,13 +447,23 @@ __global__ void __launch_bounds__(kRankWarps * 32) k_ranksort(const uint64_t* __
 
 int fl_sort_tile(int64_t n) { return n <= kSortSmallMax ? kSortTileSmall : kSortTile; }
 
+// The SM count of the current device, queried once per device index. The cache entries are
+// atomics: threads that race on a device's first query store the same value.
 int fl_sms() {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0, v = 0;
-    cudaGetDevice(&dev);
-    sms = cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0 ? v : 1;
+  constexpr int kMaxDevices = 64;
+  static std::atomic<int> cache[kMaxDevices];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    dev = -1;
   }
+  if (dev >= 0 && dev < kMaxDevices) {
+    const int c = cache[dev].load(std::memory_order_relaxed);
+    if (c > 0) return c;
+  }
+  int v = 0;
+  const int sms = dev >= 0 && cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0 ? v : 1;
+  if (dev >= 0 && dev < kMaxDevices && v > 0) cache[dev].store(sms, std::memory_order_relaxed);
   return sms;
 }
 
@@ -458,6 +487,7 @@ void fl_sort_carve(FlSortBufs* b, void* base, int64_t n) {
   b->longs_cap = longs_cap_for(cap);
   b->cap = cap;
   b->tiles_cap = tiles;
+  b->test_spins = 0;
 }
 
 void fl_sort_reset(const FlSortBufs* b, int64_t n, int passes, cudaStream_t st) {
@@ -483,15 +513,19 @@ int fl_sort_passes(const FlSortBufs* b, int64_t n, int lo_bit, uint32_t* err, cu
   int cur = 0;
   if (n <= 0) return 0;
   const int64_t tiles = tiles_for(n);
+  // the test of the bounded wait (b->test_spins > 0): the first pass withholds tile 0's counts
+  const uint32_t limit = b->test_spins ? b->test_spins : FL_SPIN_LIMIT;
   for (int p = 0; p < passes; ++p) {
     uint32_t* status = b->status + (size_t)p * tiles * 256;
+    const int hold = b->test_spins && p == 0;
     if (fl_sort_tile(n) == kSortTileSmall)
       launch_pass<kSortThreadsSmall>(b->keys[cur], b->vals[cur], b->keys[1 - cur], b->vals[1 - cur],
                                      n, lo_bit + 8 * p, b->hist + p * 256, status, b->counters + p,
-                                     err, st);
+                                     err, limit, hold, st);
     else
       launch_pass<kSortThreads>(b->keys[cur], b->vals[cur], b->keys[1 - cur], b->vals[1 - cur], n,
-                                lo_bit + 8 * p, b->hist + p * 256, status, b->counters + p, err, st);
+                                lo_bit + 8 * p, b->hist + p * 256, status, b->counters + p, err,
+                                limit, hold, st);
     ++*launches;
     cur = 1 - cur;
   }

@@ -10,11 +10,13 @@
 // words, the tile tickets and an error word) lives in one file-scope __device__ array of
 // kScratchBytes, which the CUDA runtime places on every device that loads this library and
 // keeps until the process exits. Its host-side name is only a stand-in for the device symbol,
-// so the device address is looked up once per device with cudaGetSymbolAddress and cached.
-// The caller's output buffers are the other half of the ping-pong.
+// so every call looks the device address up with cudaGetSymbolAddress, with the caller's device
+// (and context) current. The address belongs to the context that loaded the module, so it is
+// not cached: after cudaDeviceReset, or under a host that makes its own driver-API context
+// current, a cached address would point into memory the current context does not map. The
+// lookup allocates nothing. The caller's output buffers are the other half of the ping-pong.
 #include <cuda_runtime.h>
 
-#include <mutex>
 #include <string>
 
 #include "../../include/forcegpu.h"
@@ -38,10 +40,6 @@ constexpr size_t kScratchBytes = kCountersOff + 256;  // 3.6 MB for 262,144 pair
 
 static __device__ __align__(256) unsigned char g_sort_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_lock;
-void* g_scratch_ptr[kMaxDevices] = {};
-
 int32_t fail(int32_t code, const std::string& msg) {
   fl_set_sim_free_error("fl_radix_sort_noalloc: " + msg);
   return code;
@@ -52,22 +50,14 @@ int32_t cuda_fail(cudaError_t e, const char* what) {
   return fail(FL_E_DEVICE, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-// The device address of the scratch array on the current device; looked up on the first call
-// made with that device current.
-int32_t scratch_of_current_device(char** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
-  if (dev < 0 || dev >= kMaxDevices) return fail(FL_E_DEVICE, "device index out of range");
-  std::lock_guard<std::mutex> g(g_setup_lock);
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_sort_scratch);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress");
-    if (!p) return fail(FL_E_DEVICE, "cudaGetSymbolAddress returned no address");
-    g_scratch_ptr[dev] = p;
-  }
-  *out = static_cast<char*>(g_scratch_ptr[dev]);
+// The device address of the scratch array in the current context (the current device's,
+// unless the host made another context current). Looked up on every call, never cached.
+int32_t scratch_of_current_context(char** out) {
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_sort_scratch);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress");
+  if (!p) return fail(FL_E_DEVICE, "cudaGetSymbolAddress returned no address");
+  *out = static_cast<char*>(p);
   return FL_OK;
 }
 
@@ -88,15 +78,19 @@ extern "C" int32_t fl_radix_sort_noalloc(const uint64_t* keys, const uint32_t* v
   if (n == 0) return FL_OK;
   if (!keys || !vals || !keys_out || !vals_out) return fail(FL_E_ARG, "null buffer");
   const size_t kb = 8 * (size_t)n, vb = 4 * (size_t)n;
+  // the keys are copied to keys_out before the values to vals_out, so keys_out may not overlap
+  // vals (nor, for the same reason the other way round, vals_out the keys); only identical
+  // buffers may coincide: a sort in place
   if ((keys != keys_out && overlap(keys, kb, keys_out, kb)) ||
-      (vals != vals_out && overlap(vals, vb, vals_out, vb)) || overlap(keys_out, kb, vals_out, vb))
+      (vals != vals_out && overlap(vals, vb, vals_out, vb)) || overlap(keys_out, kb, vals_out, vb) ||
+      overlap(keys_out, kb, vals, vb) || overlap(vals_out, vb, keys, kb))
     return fail(FL_E_ARG, "input and output buffers overlap (only identical, in-place buffers may)");
   char* base = nullptr;
-  int32_t rc = scratch_of_current_device(&base);
+  int32_t rc = scratch_of_current_context(&base);
   if (rc) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   uint32_t* err = reinterpret_cast<uint32_t*>(base + kErrOff);
-  FlSortBufs sb;
+  FlSortBufs sb{};
   sb.keys[0] = keys_out;
   sb.vals[0] = vals_out;
   sb.keys[1] = reinterpret_cast<uint64_t*>(base + kKeysOff);

@@ -21,25 +21,21 @@ __device__ __forceinline__ void two_sum(float s, float x, float& t, float& e) {
 
 // Bounding box (ordered-uint atomics) and sum of the positions, one pass.
 // d3 computes the cube from the extent of the points (d3-octree cover) and the centre force
-// sums positions in FP64 (src/center.js:8-26); both come from this one read. Each thread sums
-// its positions as an FP32 value plus an FP32 compensation (TwoSum: every rounding error is
-// kept), about 48 bits, and only the per-thread totals are added in FP64, which runs at a
-// small fraction of the FP32 rate on this part.
-// One thread's share of the reduction: box and compensated sums of the positions it saw.
+// sums positions in FP64 (src/center.js:8-26); both come from this one read. The sums are exact
+// fixed-point integers (fl::fx128: 128 bits, 2^-40 resolution), so they do not depend on the
+// order of the additions: the same positions give the same mean bit for bit, whatever the grid.
+// One thread's share of the reduction: box and exact sums of the positions it saw.
 struct Partial {
   float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-  float fs[3] = {0.f, 0.f, 0.f}, fc[3] = {0.f, 0.f, 0.f};
-  __device__ __forceinline__ void add(float4 p, int want_sum) {
+  __int128 s[3] = {0, 0, 0};
+  uint32_t bad = 0;
+  __device__ __forceinline__ void add(float4 p, int ndim, int want_sum) {
     const float c[3] = {p.x, p.y, p.z};
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       lo[k] = fminf(lo[k], c[k]);
       hi[k] = fmaxf(hi[k], c[k]);
-      if (want_sum) {
-        float t, e;
-        two_sum(fs[k], c[k], t, e);
-        fs[k] = t, fc[k] += e;
-      }
+      if (want_sum && k < ndim) s[k] += fl::fx128(c[k], bad);
     }
   }
 };
@@ -55,44 +51,51 @@ __global__ void __launch_bounds__(kThreads) k_reduce(const float4* __restrict__ 
   // a few blocks, many positions per thread: the warp shuffles and atomics of the reduction
   // are paid once per warp, not per handful of positions
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    q.add(pos[i], want_sum);
+    q.add(pos[i], ndim, want_sum);
   flush_partial(q, ndim, want_box, want_sum, red);
 }
 
 __device__ void flush_partial(const Partial& q, int ndim, int want_box, int want_sum,
                               FlReduce* red) {
   float lo[3] = {q.lo[0], q.lo[1], q.lo[2]}, hi[3] = {q.hi[0], q.hi[1], q.hi[2]};
-  const float* fs = q.fs;
-  const float* fc = q.fc;
-  double sum[3] = {(double)fs[0] + (double)fc[0], (double)fs[1] + (double)fc[1],
-                   (double)fs[2] + (double)fc[2]};
+  __int128 sum[3] = {q.s[0], q.s[1], q.s[2]};
+  uint32_t bad = q.bad;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       lo[k] = fminf(lo[k], __shfl_xor_sync(FL_FULL, lo[k], o));
       hi[k] = fmaxf(hi[k], __shfl_xor_sync(FL_FULL, hi[k], o));
-      if (want_sum) sum[k] += __shfl_xor_sync(FL_FULL, sum[k], o);
+      if (want_sum) sum[k] += fl::shfl_xor128(sum[k], o);
     }
   }
+  if (want_sum) bad = __reduce_add_sync(FL_FULL, bad);
   __shared__ float s_lo[3][kThreads / 32], s_hi[3][kThreads / 32];
-  __shared__ double s_sum[3][kThreads / 32];
+  __shared__ __int128 s_sum[3][kThreads / 32];
+  __shared__ uint32_t s_bad[kThreads / 32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (lane == 0)
+  if (lane == 0) {
     for (int k = 0; k < 3; ++k) s_lo[k][warp] = lo[k], s_hi[k][warp] = hi[k], s_sum[k][warp] = sum[k];
+    s_bad[warp] = bad;
+  }
   __syncthreads();
   if (threadIdx.x < 3) {
     int k = threadIdx.x;
     float a = INFINITY, b = -INFINITY;
-    double s = 0;
-    for (int w = 0; w < kThreads / 32; ++w) a = fminf(a, s_lo[k][w]), b = fmaxf(b, s_hi[k][w]), s += s_sum[k][w];
+    __int128 s = 0;
+    uint32_t nb = 0;
+    for (int w = 0; w < kThreads / 32; ++w) {
+      a = fminf(a, s_lo[k][w]), b = fmaxf(b, s_hi[k][w]), s += s_sum[k][w];
+      nb += s_bad[w];
+    }
     if (k < ndim) {
       if (want_box) {  // lo holds ~ordered(min), so a zeroed record is an empty box
         atomicMax(&red->lo[k], ~fl::ordered(a));
         atomicMax(&red->hi[k], fl::ordered(b));
       }
-      if (want_sum) atomicAdd(&red->sum[k], s);
+      if (want_sum) fl::atomic_add128(&red->sum_lo[k], &red->sum_hi[k], s);
     }
+    if (want_sum && k == 0 && nb) atomicAdd(&red->bad, nb);
   }
 }
 
@@ -108,28 +111,35 @@ __global__ void __launch_bounds__(kThreads) k_breduce(const float4* __restrict__
                                                       int ndim, const uint32_t* __restrict__ gid,
                                                       FlReduce* red) {
   __shared__ uint32_t s_lo[kBreduceSlots][3], s_hi[kBreduceSlots][3];
-  __shared__ double s_sum[kBreduceSlots][3];
+  __shared__ unsigned long long s_slo[kBreduceSlots][3], s_shi[kBreduceSlots][3];
+  __shared__ uint32_t s_bad[kBreduceSlots];
   const int lane = threadIdx.x & 31;
   const int64_t first = (int64_t)blockIdx.x * kThreads * kBreduceItems;
   const uint32_t g0 = gid[first < n ? first : n - 1];
   for (int i = threadIdx.x; i < kBreduceSlots * 3; i += kThreads) {
-    (&s_lo[0][0])[i] = 0u, (&s_hi[0][0])[i] = 0u, (&s_sum[0][0])[i] = 0.0;
+    (&s_lo[0][0])[i] = 0u, (&s_hi[0][0])[i] = 0u, (&s_slo[0][0])[i] = 0ull, (&s_shi[0][0])[i] = 0ull;
   }
+  for (int i = threadIdx.x; i < kBreduceSlots; i += kThreads) s_bad[i] = 0u;
   __syncthreads();
   for (int it = 0; it < kBreduceItems; ++it) {
     const int64_t i = first + (int64_t)it * kThreads + threadIdx.x;
     const bool ok = i < n;
     const uint32_t g = ok ? gid[i] : 0xffffffffu;
     float4 p = ok ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    float lo[3] = {p.x, p.y, p.z}, hi[3] = {p.x, p.y, p.z}, sm[3] = {p.x, p.y, p.z};
+    uint32_t bad = 0;
+    float lo[3] = {p.x, p.y, p.z}, hi[3] = {p.x, p.y, p.z};
+    __int128 sm[3] = {fl::fx128(p.x, bad), ndim > 1 ? fl::fx128(p.y, bad) : 0,
+                      ndim > 2 ? fl::fx128(p.z, bad) : 0};
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const uint32_t go = __shfl_down_sync(FL_FULL, g, o);
       const bool same = lane + o < 32 && go == g;
+      const uint32_t bo = __shfl_down_sync(FL_FULL, bad, o);
+      if (same) bad += bo;
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        const float a = __shfl_down_sync(FL_FULL, lo[k], o), b = __shfl_down_sync(FL_FULL, hi[k], o),
-                    c = __shfl_down_sync(FL_FULL, sm[k], o);
+        const float a = __shfl_down_sync(FL_FULL, lo[k], o), b = __shfl_down_sync(FL_FULL, hi[k], o);
+        const __int128 c = fl::shfl_down128(sm[k], o);
         if (same) lo[k] = fminf(lo[k], a), hi[k] = fmaxf(hi[k], b), sm[k] += c;
       }
     }
@@ -140,15 +150,17 @@ __global__ void __launch_bounds__(kThreads) k_breduce(const float4* __restrict__
       for (int k = 0; k < ndim; ++k) {
         atomicMax(&s_lo[slot][k], ~fl::ordered(lo[k]));
         atomicMax(&s_hi[slot][k], fl::ordered(hi[k]));
-        atomicAdd(&s_sum[slot][k], (double)sm[k]);
+        fl::atomic_add128(&s_slo[slot][k], &s_shi[slot][k], sm[k]);
       }
+      if (bad) atomicAdd(&s_bad[slot], bad);
     } else {
       FlReduce* r = red + g;
       for (int k = 0; k < ndim; ++k) {
         atomicMax(&r->lo[k], ~fl::ordered(lo[k]));
         atomicMax(&r->hi[k], fl::ordered(hi[k]));
-        atomicAdd(&r->sum[k], (double)sm[k]);
+        fl::atomic_add128(&r->sum_lo[k], &r->sum_hi[k], sm[k]);
       }
+      if (bad) atomicAdd(&r->bad, bad);
     }
   }
   __syncthreads();
@@ -159,7 +171,9 @@ __global__ void __launch_bounds__(kThreads) k_breduce(const float4* __restrict__
     FlReduce* r = red + (g0 + slot);
     atomicMax(&r->lo[k], s_lo[slot][k]);
     atomicMax(&r->hi[k], s_hi[slot][k]);
-    atomicAdd(&r->sum[k], s_sum[slot][k]);
+    const __int128 v = (__int128)(((unsigned __int128)s_shi[slot][k] << 64) | s_slo[slot][k]);
+    fl::atomic_add128(&r->sum_lo[k], &r->sum_hi[k], v);
+    if (k == 0 && s_bad[slot]) atomicAdd(&r->bad, s_bad[slot]);
   }
 }
 
@@ -171,7 +185,7 @@ __device__ __forceinline__ void center_shift(const FlReduce* red, int n, int ndi
   if (threadIdx.x < 3) {
     const int k = threadIdx.x;
     const double c = k == 0 ? cx : k == 1 ? cy : cz;
-    const double d = k < ndim ? (red->sum[k] / n - c) * strength : 0.0;
+    const double d = k < ndim ? (fl::sum_of(*red, k) / n - c) * strength : 0.0;
     const float h = (float)d;
     s_shift[k] = make_float2(h, (float)(d - (double)h));
   }
@@ -241,7 +255,7 @@ __global__ void __launch_bounds__(kThreads) k_integrate_reduce(
     integrate_node(p, v, fix, mask[i], i, ndim, decay, red != nullptr, sh);
     pos[i] = p;
     vel[i] = v;
-    q.add(p, want_sum);
+    q.add(p, ndim, want_sum);
   }
   flush_partial(q, ndim, want_box, want_sum, out);
 }

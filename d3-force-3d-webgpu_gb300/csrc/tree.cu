@@ -37,6 +37,7 @@
 // Points with the same code at the finest level share the deepest cell as its children.
 #include <math.h>
 
+#include <atomic>
 #include <cmath>
 
 #include "kernels.h"
@@ -259,13 +260,15 @@ __global__ void __launch_bounds__(kThreads) k_bgraph(int graphs, int ndim, const
   o.decay = (float)p.decay;
   const double c[3] = {p.cx, p.cy, p.cz};
   for (int k = 0; k < 3; ++k) {
-    const double d = k < ndim && count > 0 && p.cstrength != 0 ? (red[g].sum[k] / count - c[k]) * p.cstrength : 0.0;
+    const double d = k < ndim && count > 0 && p.cstrength != 0 ? (fl::sum_of(red[g], k) / count - c[k]) * p.cstrength : 0.0;
     const float h = (float)d;
     o.shift[k] = make_float2(h, (float)(d - (double)h));
   }
   o.first = first, o.count = count;
   o.frozen = alpha[g] < 0.0 ? 1 : 0;
-  o.pad = 0.f;
+  o.fx = p.fx;
+  o.tick0 = p.tick0;
+  o.pad = 0u;
   gr[g] = o;
 }
 
@@ -372,7 +375,18 @@ __device__ __forceinline__ int kdelta(const uint64_t* __restrict__ k, int lo, in
   return ki != kj ? __clzll(ki ^ kj) : 64 + __clz(i ^ j);
 }
 
-__device__ __forceinline__ D4 add4(D4 a, D4 b) { return mk4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+// Modular (wrapping) 64-bit arithmetic: in a batch, the prefix over all graphs' records may pass
+// 2^63 (each graph has its own scale); the difference of two prefix values within one graph is
+// still its exact sum, which that graph's scale keeps below 2^62.
+__device__ __forceinline__ long long wadd(long long a, long long b) {
+  return (long long)((unsigned long long)a + (unsigned long long)b);
+}
+__device__ __forceinline__ long long wsub(long long a, long long b) {
+  return (long long)((unsigned long long)a - (unsigned long long)b);
+}
+__device__ __forceinline__ D4 add4(D4 a, D4 b) {
+  return mk4(wadd(a.x, b.x), wadd(a.y, b.y), wadd(a.z, b.z), wadd(a.w, b.w));
+}
 __device__ __forceinline__ D4 shfl_up4(D4 v, int o) {
   return mk4(__shfl_up_sync(FL_FULL, v.x, o), __shfl_up_sync(FL_FULL, v.y, o),
              __shfl_up_sync(FL_FULL, v.z, o), __shfl_up_sync(FL_FULL, v.w, o));
@@ -421,10 +435,12 @@ __global__ void __launch_bounds__(kThreads) k_build(
   // the sorted range of this point's graph (a batch), and that graph's cube
   int lo = 0, hi = n - 1;
   const float* cb = cube;
+  int fe = fx_exp;
   if (seg.graphs && i < n) {
     const uint32_t g = seg.gid_pos[i];
     lo = seg.off[g], hi = seg.off[g + 1] - 1;
     cb = seg.g[g].origin;
+    fe = seg.g[g].fx;
   }
   const uint64_t ki = i < n ? k[i] : 0;
   const int up = i < n ? kdelta(k, lo, hi, ki, i, i + 1) : -1;
@@ -441,7 +457,7 @@ __global__ void __launch_bounds__(kThreads) k_build(
       const int lD = (dmx >= bits ? L : dmx / ndim) + 1;  // the point's d3 leaf depth
       const float sF = offset_scale(cb);
       const long long W =
-          f2ll_rn(fabsf(p.w * damp(ndim, lD)) * __int_as_float((fx_exp + 127) << 23));
+          f2ll_rn(fabsf(p.w * damp(ndim, lD)) * __int_as_float((fe + 127) << 23));
       wrec = mk4(W, mulhi62(W, fx_offset(p.x, cb[0], sF)),
                  ndim > 1 ? mulhi62(W, fx_offset(p.y, cb[1], sF)) : 0,
                  ndim > 2 ? mulhi62(W, fx_offset(p.z, cb[2], sF)) : 0);
@@ -634,10 +650,11 @@ __device__ __forceinline__ float4 closed_cell(uint32_t i, int ndim, float sign,
                                               const FlSegs& seg) {
   const uint32_t a = range[2 * i], b = range[2 * i + 1];
   const float* cube = seg.graphs ? seg.g[seg.gid_pos[a]].origin : cube1;
+  const int fe = seg.graphs ? seg.g[seg.gid_pos[a]].fx : fx_exp;
   // prefix sums: within the 256-point block, plus the blocks before it; exact in fixed point
   const D4 hi = add4(P[b], Ptot[b >> 8]);
   const D4 lo = a ? add4(P[a - 1], Ptot[(a - 1) >> 8]) : mk4(0, 0, 0, 0);
-  const long long W = hi.x - lo.x;
+  const long long W = wsub(hi.x, lo.x);
   const int D = depth[i];
   float4 out;
   if (W > 0) {
@@ -646,10 +663,10 @@ __device__ __forceinline__ float4 closed_cell(uint32_t i, int ndim, float sign,
     const float4 p0 = leaf[a];
     const float fW = ll2f_rn(W);
     const float sF = offset_scale(cube), r = cube[3] / fW;
-    out.x = p0.x + ll2f_rn(hi.y - lo.y - mulhi62(W, fx_offset(p0.x, cube[0], sF))) * r;
-    out.y = ndim > 1 ? p0.y + ll2f_rn(hi.z - lo.z - mulhi62(W, fx_offset(p0.y, cube[1], sF))) * r : 0.f;
-    out.z = ndim > 2 ? p0.z + ll2f_rn(hi.w - lo.w - mulhi62(W, fx_offset(p0.z, cube[2], sF))) * r : 0.f;
-    out.w = sign * fW * __int_as_float((127 - fx_exp) << 23) * damp(ndim, -D);
+    out.x = p0.x + ll2f_rn(wsub(wsub(hi.y, lo.y), mulhi62(W, fx_offset(p0.x, cube[0], sF)))) * r;
+    out.y = ndim > 1 ? p0.y + ll2f_rn(wsub(wsub(hi.z, lo.z), mulhi62(W, fx_offset(p0.y, cube[1], sF)))) * r : 0.f;
+    out.z = ndim > 2 ? p0.z + ll2f_rn(wsub(wsub(hi.w, lo.w), mulhi62(W, fx_offset(p0.z, cube[2], sF)))) * r : 0.f;
+    out.w = sign * fW * __int_as_float((127 - fe) << 23) * damp(ndim, -D);
   } else {
     out = leaf[a];
     out.w = 0.f;
@@ -866,12 +883,16 @@ struct WalkShared {
 // whose widest cell is too close (the child is approximated at the first, widest, depth of the
 // chain that passes the theta test), a zero component of the displacement (d3 replaces it with
 // a jiggle) and distanceMin. `va` arrives as the value at the chain's top depth.
+// The jiggle's ids of a pair are the graph's own: a point's node index less its graph's first
+// node (`first`: 0 outside a batch), and for a cell a hash of its centroid's bits (a point's ids
+// are below 2^26, a cell's have the top bit set), so that a layout draws the same jiggles alone
+// or in any batch.
 template <int NDIM>
 __device__ __forceinline__ void rare_case(uint32_t meta, uint32_t top, uint32_t idx, float T0,
-                                          float dmin2, uint32_t myid,
+                                          float dmin2, uint32_t myid, uint32_t first,
                                           const uint32_t* __restrict__ perm, int n, uint32_t step,
-                                          uint32_t seed, float& va, float& dx, float& dy,
-                                          float& dz, float& l) {
+                                          uint32_t seed, float cx, float cy, float cz, float& va,
+                                          float& dx, float& dy, float& dz, float& l) {
   if (meta != kLeafMark) {
     const uint32_t D = (meta >> 26) & 31u;
     if (top < D && T0 * pow4neg(top) >= l) {
@@ -881,7 +902,12 @@ __device__ __forceinline__ void rare_case(uint32_t meta, uint32_t top, uint32_t 
     }
   }
   if (dx == 0.f || (NDIM > 1 && dy == 0.f) || (NDIM > 2 && dz == 0.f)) {
-    const uint32_t other = meta == kLeafMark ? perm[idx < (uint32_t)n ? idx : 0] : (uint32_t)n + idx;
+    const uint32_t other =
+        meta == kLeafMark
+            ? perm[idx < (uint32_t)n ? idx : 0] - first
+            : 0x80000000u | fl::mix32(__float_as_uint(cx) ^
+                                      fl::mix32(__float_as_uint(cy) ^ fl::mix32(__float_as_uint(cz))));
+    myid -= first;
     if (dx == 0.f) dx = fl::jiggle(myid, other, 0, step, seed), l += dx * dx;
     if (NDIM > 1 && dy == 0.f) dy = fl::jiggle(myid, other, 1, step, seed), l += dy * dy;
     if (NDIM > 2 && dz == 0.f) dz = fl::jiggle(myid, other, 2, step, seed), l += dz * dz;
@@ -951,9 +977,11 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
   int wi = lane == 0 ? (int)atomicAdd(work, 1u) : 0;
   wi = __shfl_sync(FL_FULL, wi, 0);
   while (wi < nwarps) {
-  const int base = wi * 32;
+  // a group: 32 consecutive sorted points, or in a batch one graph's points [x, y), at most 32
+  const uint2 grp_range = BATCH ? segs.groups[wi] : make_uint2((uint32_t)wi * 32u, (uint32_t)n);
+  const int base = (int)grp_range.x;
   const int t = base + lane;
-  const bool live = t < n;
+  const bool live = t < (int)grp_range.y;
   const uint32_t act = __ballot_sync(FL_FULL, live) & gmask;
   const float4 me = live ? leaf[t] : make_float4(0, 0, 0, 0);
   const uint32_t myid = live ? perm[t] : 0;
@@ -961,6 +989,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
   const uint64_t MX = pk2(me.x, me.x), MY = pk2(me.y, me.y), MZ = pk2(me.z, me.z);
   // the lane's own graph: what its uncommon cases and distanceMax use
   float myT0 = T0, mydmin2 = dmin2, mydmax2 = dmax2;
+  uint32_t myfirst = 0, mystep = step;
   int sp;
   if (!BATCH) {
     if (gl == 0 && act) sset(0, make_uint4(0u, 1u, 0u, act));  // the root: slot 0, top depth 0
@@ -973,6 +1002,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
     if (live) {
       const FlGraph& gr = segs.g[g];
       myT0 = gr.T0, mydmin2 = gr.dmin2, mydmax2 = gr.dmax2;
+      myfirst = (uint32_t)gr.first, mystep = step + gr.tick0;
       tree = gr.count > 1 && !gr.frozen;
     }
     const uint32_t peers = __match_any_sync(FL_FULL, tree ? g : 0xffffffffu) & gmask;
@@ -1086,11 +1116,13 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
           float2 dx = up2(DX), dy = up2(DY), dz = up2(DZ);
           if (c0) {
             const uint2 k0 = scold[j];
-            rare_case<NDIM>(k0.x, k0.y & 0xffu, r0.w, myT0, mydmin2, myid, perm, n, step, seed, v0, dx.x, dy.x, dz.x, l.x);
+            rare_case<NDIM>(k0.x, k0.y & 0xffu, r0.w, myT0, mydmin2, myid, myfirst, perm, n, mystep,
+                            seed, pa.x, pa.z, pb.x, v0, dx.x, dy.x, dz.x, l.x);
           }
           if (c1) {
             const uint2 k1 = scold[j + 1];
-            rare_case<NDIM>(k1.x, k1.y & 0xffu, r1.w, myT0, mydmin2, myid, perm, n, step, seed, v1, dx.y, dy.y, dz.y, l.y);
+            rare_case<NDIM>(k1.x, k1.y & 0xffu, r1.w, myT0, mydmin2, myid, myfirst, perm, n, mystep,
+                            seed, pa.y, pa.w, pb.y, v1, dx.y, dy.y, dz.y, l.y);
           }
           DX = pk2(dx.x, dx.y), DY = pk2(dy.x, dy.y), DZ = pk2(dz.x, dz.y);
         }
@@ -1390,15 +1422,20 @@ void fl_launch_aggregate(const FlTreeBufs* t, const uint64_t* skeys, bool closed
 // Blocks of this walk variant resident on one SM (queried once), at most kWalkBlocksPerSm.
 template <int NDIM, int G, bool STATS, bool DMAX, bool BATCH>
 int walk_blocks_per_sm() {
-  static int blocks = 0;
-  if (!blocks) {
+  // an atomic: host threads racing on the first query store the same value
+  static std::atomic<int> blocks{0};
+  int c = blocks.load(std::memory_order_relaxed);
+  if (!c) {
     int b = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_walk<NDIM, G, STATS, DMAX, BATCH>,
-                                                      kWalkThreads, 0) != cudaSuccess || b < 1)
+                                                      kWalkThreads, 0) != cudaSuccess || b < 1) {
+      cudaGetLastError();
       b = 1;
-    blocks = b < kWalkBlocksPerSm ? b : kWalkBlocksPerSm;
+    }
+    c = b < kWalkBlocksPerSm ? b : kWalkBlocksPerSm;
+    blocks.store(c, std::memory_order_relaxed);
   }
-  return blocks;
+  return c;
 }
 
 void fl_launch_walk(const FlTreeBufs* t, const uint32_t* perm, const float* cube, float4* vel,
@@ -1406,7 +1443,7 @@ void fl_launch_walk(const FlTreeBufs* t, const uint32_t* perm, const float* cube
                     uint32_t seed, uint32_t* err, unsigned long long* stats, int group,
                     cudaStream_t st, FlSegs segs, const FlTick* tk) {
   const int n = t->n;
-  const int warps = (n + 31) / 32;
+  const int warps = segs.graphs ? segs.ngroups : (n + 31) / 32;
   // a persistent grid of the blocks that fit on the device at once (and that the spill buffer
   // has regions for), each warp walking every (grid)-th group of 32 points
   const int cap = t->walk_slots / kWalkWarps;

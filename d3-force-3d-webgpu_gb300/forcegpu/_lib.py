@@ -29,10 +29,10 @@ EXPORTS = ["fl_create", "fl_destroy", "fl_last_error", "fl_fits", "fl_set_nodes"
            "fl_batch_destroy", "fl_batch_last_error", "fl_batch_set_graphs", "fl_batch_set_seed",
            "fl_batch_enqueue", "fl_batch_sync", "fl_batch_query", "fl_batch_stream",
            "fl_autotune", "fl_batch_set_tuning", "fl_batch_autotune", "fl_batch_read",
-           "fl_update_positions_packed", "fl_sync_packed"]
+           "fl_update_positions_packed", "fl_sync_packed", "fl_upload_all", "fl_debug_links"]
 SORT_NOALLOC_MAX_PAIRS = 262144  # FL_SORT_NOALLOC_MAX_PAIRS
 TUNE_WALK_GROUP, TUNE_CELL_SUMS, TUNE_GRAPHS = 1, 2, 3
-TUNE_SORT_PASSES, TUNE_WALK_BLOCKS, TUNE_COLLIDE_CELL = 4, 5, 6
+TUNE_SORT_PASSES, TUNE_WALK_BLOCKS, TUNE_COLLIDE_CELL, TUNE_TEST_LOOKBACK = 4, 5, 6, 7
 CELLS_AUTO, CELLS_FP64_TOP, CELLS_FP32 = 0, 1, 2
 
 
@@ -71,6 +71,7 @@ class GraphDesc(ctypes.Structure):
         ("distance_max2", ctypes.c_double),
         ("center_x", ctypes.c_double), ("center_y", ctypes.c_double), ("center_z", ctypes.c_double),
         ("center_strength", ctypes.c_double), ("velocity_decay", ctypes.c_double),
+        ("tick0", ctypes.c_uint32),
     ]
 
 
@@ -108,6 +109,8 @@ def load():
         "fl_fits": (I32, [P, I64, ctypes.POINTER(I32)]),
         "fl_set_nodes": (I32, [P, I32, I32, P, P, P, P]),
         "fl_update_positions": (I32, [P, I32, I32, P]),
+        "fl_upload_all": (I32, [P, P, P, P, P]),
+        "fl_debug_links": (I32, [P, I32, P, P, P]),
         "fl_update_pins": (I32, [P, I32, I32, P, P]),
         "fl_update_velocities": (I32, [P, I32, I32, P]),
         "fl_set_forces": (I32, [P, I32, ctypes.POINTER(ForceDesc)]),
@@ -195,6 +198,15 @@ class Engine:
         mask = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint32).reshape(n)
         self._check(self.L.fl_set_nodes(self.h, n, int(ndim), _ptr(pos4), _ptr(vel4), _ptr(fix4), _ptr(mask)))
         self.n, self.ndim = n, min(3, max(1, int(ndim)))
+
+    def upload_all(self, pos4, vel4=None, fix4=None, mask=None):
+        """fl_upload_all: replace the state of the current n nodes, keeping the forces."""
+        n = self.n
+        pos4 = np.ascontiguousarray(pos4, dtype=np.float32).reshape(n, 4)
+        vel4 = None if vel4 is None else np.ascontiguousarray(vel4, dtype=np.float32).reshape(n, 4)
+        fix4 = None if fix4 is None else np.ascontiguousarray(fix4, dtype=np.float32).reshape(n, 4)
+        mask = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint32).reshape(n)
+        self._check(self.L.fl_upload_all(self.h, _ptr(pos4), _ptr(vel4), _ptr(fix4), _ptr(mask)))
 
     def update_positions(self, first, pos4):
         pos4 = np.ascontiguousarray(pos4, dtype=np.float32).reshape(-1, 4)
@@ -309,6 +321,14 @@ class Engine:
         self._check(self.L.fl_debug_tree(self.h, int(index), _ptr(keys), _ptr(perm), _ptr(left),
                                          _ptr(right), _ptr(depth), _ptr(cube)))
         return keys, perm, left[:n - 1], right[:n - 1], depth[:n - 1], cube
+
+    def debug_links(self, index, m):
+        """The link CSR of force `index` (m links): (row[n + 1], other[2m], code[2m])."""
+        row = np.zeros(self.n + 1, np.int32)
+        other = np.zeros(max(2 * m, 1), np.int32)
+        code = np.zeros(max(2 * m, 1), np.uint32)
+        self._check(self.L.fl_debug_links(self.h, int(index), _ptr(row), _ptr(other), _ptr(code)))
+        return row, other[:2 * m], code[:2 * m]
 
     def profile_read(self):
         cap = 32

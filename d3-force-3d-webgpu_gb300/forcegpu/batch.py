@@ -45,6 +45,7 @@ class GraphSpec:
     alpha_decay: float = 1 - 0.001 ** (1 / 300)
     alpha_target: float = 0.0
     vel: np.ndarray = None
+    tick0: int = 0  # ticks the layout ran before (a job moved between batches keeps its count)
     _keep: list = field(default_factory=list, repr=False)
 
 
@@ -113,6 +114,7 @@ class Batch:
             d.center_x, d.center_y, d.center_z = (list(s.center) + [0.0, 0.0, 0.0])[:3]
             d.center_strength = s.center_strength
             d.velocity_decay = s.velocity_decay
+            d.tick0 = int(s.tick0) & 0xffffffff
             s._keep = keep
         self._check(self.L.fl_batch_set_graphs(self.h, self.ndim, len(self.specs), descs))
         if seed is not None:

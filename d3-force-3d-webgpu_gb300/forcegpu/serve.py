@@ -113,7 +113,8 @@ class _Lane:
     def spec(self, j):
         return GraphSpec(xyz=j.pos[:, :self.ndim], source=j.source, target=j.target,
                          theta=j.theta, velocity_decay=j.velocity_decay,
-                         vel=j.vel[:, :self.ndim] if j.vel is not None else None)
+                         vel=j.vel[:, :self.ndim] if j.vel is not None else None,
+                         tick0=j.done_ticks)
 
     def _rebuild(self, seed):
         live = self.live()

@@ -90,8 +90,10 @@ typedef struct fl_buffer_info {
 int32_t fl_create(int32_t device, fl_sim** out);
 /* Release every device buffer (engine.destroy, src/gpu/engine.js:422-427). NULL is allowed. */
 int32_t fl_destroy(fl_sim* sim);
-/* Message of the last failed call on this simulation (or of the last fl_create failure when
- * sim is NULL). The string lives until the next call on the same simulation. */
+/* Message of the last failed call on this simulation. With sim NULL: the message of the last
+ * failed call on the calling thread that takes no simulation (fl_create, fl_radix_sort,
+ * fl_radix_sort_noalloc), kept per host thread. The string lives until the next call on the same
+ * simulation (or, with NULL, the next such failure on the same thread). */
 const char* fl_last_error(const fl_sim* sim);
 
 /* Whether `count` nodes fit this device (engine.fits, src/gpu/engine.js:332-338). */
@@ -102,6 +104,14 @@ int32_t fl_fits(fl_sim* sim, int64_t count, int32_t* fits);
  * forces must be set again afterwards, as in the reference. n may be 0. */
 int32_t fl_set_nodes(fl_sim* sim, int32_t n, int32_t ndim, const float* pos4, const float* vel4,
                      const float* fix4, const uint32_t* mask);
+/* Replace the whole node state of the current node set, keeping the forces (engine.markStale +
+ * uploadAll, src/gpu/engine.js:115-145, :346-349, :355): pos4/vel4/fix4 are 4*n floats of the n
+ * nodes fl_set_nodes gave; vel4, fix4 and mask may be NULL (zeros). The tick counter runs on, as
+ * the reference's does. A block of ticks that ran before from the state fl_set_nodes left (or
+ * from an earlier fl_upload_all) runs again as the same CUDA graph after this call, so a caller
+ * can restart from a saved state without recapturing. */
+int32_t fl_upload_all(fl_sim* sim, const float* pos4, const float* vel4, const float* fix4,
+                      const uint32_t* mask);
 /* Upload nodes [first, first + count) that the caller moved (uploadPositions,
  * src/gpu/engine.js:147-156): 4*count floats. */
 int32_t fl_update_positions(fl_sim* sim, int32_t first, int32_t count, const float* pos4);
@@ -170,7 +180,13 @@ enum {
   FL_TUNE_GRAPHS = 3,
   FL_TUNE_SORT_PASSES = 4,
   FL_TUNE_WALK_BLOCKS = 5,
-  FL_TUNE_COLLIDE_CELL = 6
+  FL_TUNE_COLLIDE_CELL = 6,
+  /* A test of the bounded device-side waits, not a tuning: with value v > 0 every look-back wait
+   * of the many-body tree's sort gives up after v polls, and the first digit pass of each tick
+   * withholds the first tile's counts, so that the waits do run out. A tile whose wait gave up
+   * counts its predecessors' keys itself (the sort stays exact, only slower) and the next
+   * fl_sync / fl_idle reports FL_E_TIMEOUT. 0 (the default) turns it off. */
+  FL_TUNE_TEST_LOOKBACK = 7
 };
 enum { FL_CELLS_AUTO = 0, FL_CELLS_FP64_TOP = 1, FL_CELLS_FP32 = 2 };
 int32_t fl_set_tuning(fl_sim* sim, int32_t key, int32_t value);
@@ -235,6 +251,10 @@ typedef struct fl_graph_desc {
   double theta2, distance_min2, distance_max2;  /* many-body (d3 defaults 0.81, 1, inf) */
   double center_x, center_y, center_z, center_strength; /* centre force; strength 0: none */
   double velocity_decay;     /* d3's velocityDecay (0.4 default) */
+  uint32_t tick0;            /* ticks the graph has run before (0 for a new layout): a layout
+                                moved from batch to batch keeps its own tick count, which seeds
+                                its coincident-node jiggles, so its result does not depend on
+                                the batches it went through */
 } fl_graph_desc;
 
 typedef struct fl_batch fl_batch;
@@ -282,10 +302,12 @@ int32_t fl_radix_sort(const uint64_t* keys, const uint32_t* vals, int64_t n, int
  * inputs, sorted in place; they must not otherwise overlap); the sort runs on `stream` (NULL:
  * the default stream) and the call returns when it has finished. Its scratch is a built-in
  * device array of about 3.6 MB, present on every device that loads this library until the
- * process exits, so n may not exceed FL_SORT_NOALLOC_MAX_PAIRS (FL_E_ARG otherwise). The first
- * call on a device looks the array's address up (cudaGetSymbolAddress): make that first call
- * before any stream capture. Calls share the array, so calls that overlap on the GPU (from
- * several host threads, or on several streams) race and corrupt each other's results. */
+ * process exits, so n may not exceed FL_SORT_NOALLOC_MAX_PAIRS (FL_E_ARG otherwise). Every
+ * call looks the array's address up in the current context (cudaGetSymbolAddress, which
+ * allocates nothing); the first call in a context also loads the library's device code there:
+ * make that first call before any stream capture. Calls share the array, so calls that overlap
+ * on the GPU (from several host threads, or on several streams) race and corrupt each other's
+ * results. */
 #define FL_SORT_NOALLOC_MAX_PAIRS 262144
 int32_t fl_radix_sort_noalloc(const uint64_t* keys, const uint32_t* vals, int64_t n,
                               int32_t lo_bit, uint64_t* keys_out, uint32_t* vals_out,
@@ -298,6 +320,12 @@ int32_t fl_radix_sort_noalloc(const uint64_t* keys, const uint32_t* vals, int64_
  * Any output may be NULL. */
 int32_t fl_debug_tree(fl_sim* sim, int32_t index, uint64_t* keys, uint32_t* perm, uint32_t* left,
                       uint32_t* right, uint8_t* depth, float* cube5);
+
+/* The link CSR the engine holds for force `index` (a link force), as the reference builds it on
+ * the host (src/gpu/passes/link.js:65-101): row[n + 1] offsets of each node's entries, then per
+ * entry [2m] the other end's node index and its code, link * 2 + (this node is the target),
+ * each node's entries in link order. Any output may be NULL. */
+int32_t fl_debug_links(fl_sim* sim, int32_t index, int32_t* row, int32_t* other, uint32_t* code);
 
 #ifdef __cplusplus
 }

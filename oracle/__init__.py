@@ -77,6 +77,8 @@ def lib():
         L.ofl_tick.argtypes = [P, I32]
         L.ofl_apply_force.argtypes = [P, I32, ctypes.c_double]
         L.ofl_walk_stats.argtypes = [P, ctypes.c_void_p]
+        L.ofl_collide_probe.restype = I32
+        L.ofl_collide_probe.argtypes = [P, I32, I32, ctypes.c_void_p, I32, ctypes.c_void_p]
         L.ofl_manybody_probe.restype = I32
         L.ofl_manybody_probe.argtypes = [P, I32, ctypes.c_double, I32, I32, ctypes.c_void_p, I32,
                                          ctypes.c_void_p]
@@ -243,6 +245,17 @@ class OracleSim:
                                       int(threads), out.ctypes.data)
         if rc != 0:
             raise ValueError("manybody_probe: bad force index or target")
+        return out
+
+    def collide_probe(self, k, targets, threads=1):
+        """Velocity change one Jacobi iteration of collide force k gives the target nodes (count
+        x 3), state unchanged: the values of the JACOBI mode's full pass, at O(count n)."""
+        t = np.ascontiguousarray(targets, dtype=np.int32)
+        out = np.zeros((len(t), 3), dtype=np.float64)
+        rc = lib().ofl_collide_probe(self._h, int(k), len(t), t.ctypes.data, int(threads),
+                                     out.ctypes.data)
+        if rc != 0:
+            raise ValueError("collide_probe: bad force index or target")
         return out
 
     def walk_stats(self):

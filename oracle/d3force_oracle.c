@@ -595,6 +595,85 @@ static void collide_jacobi(osim* s, oforce* f) {
   free(acc);
 }
 
+/* collide_jacobi's velocity change of target node t in one iteration, from the snapshot
+ * coords = x + v: every pair (a, b), a < b, that holds t, with the same expressions as the loop
+ * of collide_jacobi, and in its order (pairs (j, t) for j < t, then (t, j) for j > t), so the
+ * same value. */
+static void collide_jacobi_node(const osim* s, const oforce* f, const double* coords, int32_t t,
+                                double* out3) {
+  int d = s->ndim;
+  int32_t n = s->n;
+  double strength = f->p[0];
+  double ax = 0, ay = 0, az = 0;
+  for (int32_t j = 0; j < n; ++j) {
+    if (j == t) continue;
+    const int32_t a = j < t ? j : t, b = j < t ? t : j;
+    const double* pa = &coords[3 * (size_t)a];
+    const double* pb = &coords[3 * (size_t)b];
+    double ra = f->a[a], rb = f->a[b], r = ra + rb;
+    double x = pa[0] - pb[0], y = d > 1 ? pa[1] - pb[1] : 0, z = d > 2 ? pa[2] - pb[2] : 0;
+    double l = x * x + y * y + z * z;
+    if (!(l < r * r) || l == 0) continue;
+    l = sqrt(l);
+    l = (r - l) / l * strength;
+    double ra2 = ra * ra, rb2 = rb * rb, w = rb2 / (ra2 + rb2);
+    if (t == a) {
+      ax += x * l * w, ay += y * l * w, az += z * l * w;
+    } else {
+      w = 1 - w;
+      ax -= x * l * w, ay -= y * l * w, az -= z * l * w;
+    }
+  }
+  out3[0] = ax, out3[1] = d > 1 ? ay : 0, out3[2] = d > 2 ? az : 0;
+}
+
+typedef struct {
+  const osim* s;
+  const oforce* f;
+  const double* coords;
+  const int32_t* targets;
+  int32_t lo, hi;
+  double* out3;
+} collide_job;
+
+static void* collide_probe_run(void* arg) {
+  collide_job* j = (collide_job*)arg;
+  for (int32_t k = j->lo; k < j->hi; ++k)
+    collide_jacobi_node(j->s, j->f, j->coords, j->targets[k], &j->out3[3 * (size_t)k]);
+  return NULL;
+}
+
+int32_t ofl_collide_probe(osim* s, int32_t k, int32_t count, const int32_t* targets,
+                          int32_t threads, double* out3) {
+  if (k < 0 || k >= s->nforces || s->forces[k].type != 3 || count < 0) return -1;
+  const oforce* f = &s->forces[k];
+  for (int32_t i = 0; i < count; ++i)
+    if (targets[i] < 0 || targets[i] >= s->n) return -1;
+  double* coords = (double*)malloc(sizeof(double) * 3 * (size_t)(s->n > 0 ? s->n : 1));
+  for (size_t i = 0; i < 3 * (size_t)s->n; ++i) coords[i] = s->x[i] + s->v[i];
+  if (threads < 1) threads = 1;
+  if (threads > 256) threads = 256;
+  if (threads > count) threads = count > 0 ? count : 1;
+  pthread_t tid[256];
+  collide_job jobs[256];
+  for (int32_t t = 0; t < threads; ++t) {
+    jobs[t].s = s, jobs[t].f = f, jobs[t].coords = coords, jobs[t].targets = targets;
+    jobs[t].lo = (int32_t)((int64_t)count * t / threads);
+    jobs[t].hi = (int32_t)((int64_t)count * (t + 1) / threads);
+    jobs[t].out3 = out3;
+  }
+  int32_t started = 0;
+  for (int32_t t = 1; t < threads; ++t) {
+    if (pthread_create(&tid[t], NULL, collide_probe_run, &jobs[t]) != 0) break;
+    started = t;
+  }
+  collide_probe_run(&jobs[0]);
+  for (int32_t t = 1; t <= started; ++t) pthread_join(tid[t], NULL);
+  for (int32_t t = started + 1; t < threads; ++t) collide_probe_run(&jobs[t]);  /* not started */
+  free(coords);
+  return 0;
+}
+
 /* ------------------------------------------------------------------ center, radial, x/y/z */
 
 static void center_force(osim* s, oforce* f) {

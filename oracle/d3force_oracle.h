@@ -86,6 +86,13 @@ void ofl_apply_force(osim* s, int32_t k, double alpha);
 int32_t ofl_manybody_probe(osim* s, int32_t k, double alpha, int32_t mode, int32_t count,
                            const int32_t* targets, int32_t threads, double* out3);
 
+/* The velocity change one iteration of collide force k in its Jacobi form (every pair against
+ * one snapshot of p + v) gives each of `count` target nodes, state unchanged: the values the
+ * JACOBI mode's full pass gives those nodes, at O(count * n) on `threads` host threads.
+ * out3: 3 * count doubles. Returns 0, or -1 for a bad force index or target. */
+int32_t ofl_collide_probe(osim* s, int32_t k, int32_t count, const int32_t* targets,
+                          int32_t threads, double* out3);
+
 /* Counters of the last many-body d3 tree walk: [0] approximated cells (internal cells that
  * passed the theta test, with a nonzero value), [1] point interactions (leaf data visited),
  * [2] cells opened (internal cells that failed the theta test). */

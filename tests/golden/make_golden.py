@@ -4,7 +4,7 @@ The reference's CPU known-answer tests and published layout sizes are read as te
 checkout of erw-1/d3-force-3d-webgpu and written out as small fixtures, so that the GPU machine
 (which has no copy of the reference) can check the oracle against them.
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path of the reference checkout>
 
 Sources (paths within the reference):
   test/simulation-test.js:10-17   phyllotaxis start of three 2D nodes
@@ -60,4 +60,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path of the erw-1/d3-force-3d-webgpu checkout>")
+    main(sys.argv[1])

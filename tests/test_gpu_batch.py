@@ -65,21 +65,28 @@ def test_every_graph_of_a_batch_matches_the_oracle(dims):
         assert_close(p, want, 1e-3, tree_outliers(len(p)))
 
 
-def test_a_graph_alone_and_in_a_mix_agree():
-    """The same graph laid out alone and among others: its result does not depend on the rest
-    of the batch (the continuous-batching property a server relies on)."""
-    me = spec(900, 3, 5)
-    others = [spec(n, 3, 20 + i) for i, n in enumerate([300, 2, 1200, 77])]
+@pytest.mark.parametrize("dims", [2, 3])
+def test_a_graph_alone_and_in_a_mix_agree_bit_for_bit(dims):
+    """The same graph laid out alone and among others, 300 ticks: its result does not depend on
+    the rest of the batch (the continuous-batching property a server relies on). Every sum of a
+    graph is the graph's own: exact integer centre sums and cell sums at the graph's own scale,
+    walk groups that start at the graph's first point, jiggles drawn from graph-local ids. So
+    the layouts agree bit for bit (a force layout is chaotic: any difference in the last bit
+    would grow by orders of magnitude over 300 ticks)."""
+    me = spec(900, dims, 5)
+    me.xyz = me.xyz.copy()
+    me.xyz[7] = me.xyz[3]  # a coincident pair: jiggles in the walk
+    others = [spec(n, dims, 20 + i) for i, n in enumerate([300, 2, 1200, 77, 33])]
     alone = Batch()
-    alone.set_graphs([me], ndim=3, seed=3)
-    alone.run(20)
+    alone.set_graphs([me], ndim=dims, seed=3)
+    alone.run(300)
     a = alone.positions()[0]
     mix = Batch()
-    mix.set_graphs(others[:2] + [me] + others[2:], ndim=3, seed=3)
-    mix.run(20)
+    mix.set_graphs(others[:2] + [me] + others[2:], ndim=dims, seed=3)
+    mix.run(300)
     m = mix.positions()[2]
-    # the same tree, interactions and forces; only the order of some float sums may differ
-    assert_close(m, a, 1e-4, tree_outliers(900))
+    assert np.isfinite(a).all()
+    assert np.array_equal(m, a)
 
 
 def test_graphs_with_finished_schedules_and_many_ticks_stay_finite():

@@ -98,9 +98,14 @@ def _pairs(n, d):
     return nodes
 
 
+@pytest.mark.parametrize("iterations", [1, 3])
 @pytest.mark.parametrize("dims", DIMS)
-def test_collide_separated_pairs(dims):
-    r = run_both(dims, 100, 4, lambda: [("collide", forceCollide(lambda d, i, *a: 6 + i % 3).strength(0.9))],
+def test_collide_separated_pairs(dims, iterations):
+    """Each node overlaps one partner only, so d3's sequential pushes equal the GPU's Jacobi
+    ones; with iterations(3), each iteration sees the velocities the one before left
+    (src/gpu/passes/collide.js:127-133)."""
+    r = run_both(dims, 100, 4, lambda: [("collide", forceCollide(lambda d, i, *a: 6 + i % 3)
+                                         .strength(0.9).iterations(iterations))],
                  nodes_fn=_pairs)
     assert_nodes_close(r["gpu"], r["cpu"], dims, rtol=1e-3)
 
@@ -219,8 +224,9 @@ def test_tree_20_ticks():
 
 # --- collide on large graphs: the grid finds the pairs ---
 
+@pytest.mark.parametrize("iterations", [1, 3])
 @pytest.mark.parametrize("dims", DIMS)
-def test_collide_grid_separated_pairs(dims):
+def test_collide_grid_separated_pairs(dims, iterations):
     def pairs(n, d):
         nodes, side = [], math.ceil((n / 2) ** (1 / d))
         for i in range(0, n, 2):
@@ -232,7 +238,8 @@ def test_collide_grid_separated_pairs(dims):
                 a["z"] = b["z"] = float((k // side // side) * 40)
             nodes += [a, b]
         return nodes
-    r = run_both(dims, 10000, 3, lambda: [("collide", forceCollide(lambda d, i, *a: 6 + i % 3).strength(0.9))],
+    r = run_both(dims, 10000, 3, lambda: [("collide", forceCollide(lambda d, i, *a: 6 + i % 3)
+                                           .strength(0.9).iterations(iterations))],
                  nodes_fn=pairs)
     assert_nodes_close(r["gpu"], r["cpu"], dims, rtol=1e-3)
 

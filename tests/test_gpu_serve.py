@@ -39,27 +39,32 @@ class FakeClock:
 
 @pytest.mark.parametrize("dims", [2, 3])
 def test_a_job_alone_and_in_the_mix_gives_the_same_layout(dims):
-    # A force layout is chaotic: float sums taken in another order (the walk's, the centre's
-    # atomics) differ in the last bits and the difference grows tick by tick, by about 10x every
-    # 10 ticks here; so the job runs 12 ticks, in blocks of 4, with the mix changing around it.
-    ticks = 12
-    alone = LayoutServer(block=4, clock=FakeClock())
+    """300 ticks, in blocks of 10, with the mix changing around the job: others join the running
+    batch and leave it while it runs. Every sum of a layout is its own (exact integer centre
+    sums, cell sums at the layout's own scale, walk groups from its own first point, jiggles
+    from its own ids and tick count), so the layout comes out bit for bit the same; a force
+    layout is chaotic, and any difference in a last bit would have grown by orders of
+    magnitude over 300 ticks."""
+    ticks = 300
+    alone = LayoutServer(block=10, clock=FakeClock())
     me = alone.submit(job(600, dims, 11, ticks))
     alone.run_until_idle()
     alone.close()
     # the same job in a mix: it joins a running batch, others join and leave while it runs
-    srv = LayoutServer(block=4, clock=FakeClock())
-    srv.submit(job(300, dims, 12, 6, arrival=0.0))
-    srv.submit(job(1500, dims, 13, 20, arrival=0.0))
+    srv = LayoutServer(block=10, clock=FakeClock())
+    srv.submit(job(300, dims, 12, 60, arrival=0.0))
+    srv.submit(job(1500, dims, 13, 200, arrival=0.0))
     mine = srv.submit(job(600, dims, 11, ticks, arrival=3.0))
-    srv.submit(job(50, dims, 14, 5, arrival=6.0))
-    srv.submit(job(900, dims, 15, 9, arrival=9.0))
+    srv.submit(job(50, dims, 14, 50, arrival=6.0))
+    srv.submit(job(900, dims, 15, 120, arrival=9.0))
+    srv.submit(job(2000, dims, 16, 100, arrival=17.0))
     srv.run_until_idle()
     srv.close()
     assert all(j.result is not None for j in srv.finished)
-    assert len(srv.finished) == 5
+    assert len(srv.finished) == 6
     assert mine.done_ticks == ticks
-    assert close(mine.result, me.result, tree_outliers(600))
+    assert np.isfinite(me.result).all()
+    assert np.array_equal(mine.result, me.result)
 
 
 def test_admission_waits_for_memory_to_free_up():

@@ -331,6 +331,28 @@ def test_with_readback_false_keeps_the_nodes_untouched_until_sync():
     sim.destroy()
 
 
+@pytest.mark.parametrize("n,ticks", [(2000, 300), (60000, 40)])
+def test_is_deterministic_with_the_centre_force(n, ticks):
+    """link + charge + center, twice from the same start: bit for bit the same layout. The
+    centre's mean is an exact integer sum (independent of the order its blocks add in), the
+    tree and its cell sums are exact, and every walk sums in a fixed order."""
+    from forcegpu.graphs import benchmark_links
+
+    def once():
+        nodes = make_nodes(n, 3, 200)
+        src, dst = benchmark_links(n, n // 2, seed=9)
+        links = [{"source": int(a), "target": int(b)} for a, b in zip(src, dst)]
+        sim = make(nodes, 3).stop().force("link", forceLink(links)).force("charge", forceManyBody()) \
+            .force("center", forceCenter(3, -2, 1))
+        run(sim.tickAsync(ticks))
+        sim.destroy()
+        return np.array([(d["x"], d["y"], d["z"], d["vx"], d["vy"], d["vz"]) for d in nodes])
+
+    a, b = once(), once()
+    assert np.isfinite(a).all()
+    assert np.array_equal(a, b)
+
+
 def test_is_deterministic_for_a_given_random_source_coincident_nodes():
     def once():
         nodes = [{"x": 0.0, "y": 0.0, "z": 0.0} for _ in range(20)]

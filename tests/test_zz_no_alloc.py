@@ -42,6 +42,10 @@ def test_noalloc_sort_matches_the_allocating_sort_on_consecutive_calls():
         got_k, got_v = device_sort(keys, vals, lo)
         np.testing.assert_array_equal(got_k, want_k)
         np.testing.assert_array_equal(got_v, want_v)
+        # and directly against numpy's stable sort on the same key bits
+        order = np.argsort(keys >> np.uint64(lo), kind="stable")
+        np.testing.assert_array_equal(got_k, keys[order])
+        np.testing.assert_array_equal(got_v, vals[order])
     # a third call, sorting in place
     want_k, want_v = radix_sort(k2, v2, 8)
     got_k, got_v = device_sort(k2, v2, 8, in_place=True)
@@ -55,3 +59,20 @@ def test_noalloc_sort_rejects_sizes_beyond_its_scratch():
         radix_sort_noalloc(0, 0, SORT_NOALLOC_MAX_PAIRS + 1, 0, 0, 0, 0)  # rejected before any use
     assert e.value.code == FL_E_ARG
     assert "exceeds the maximum of %d pairs" % SORT_NOALLOC_MAX_PAIRS in str(e.value)
+
+
+@pytest.mark.gpu
+def test_noalloc_sort_rejects_outputs_overlapping_the_other_input():
+    """keys_out over the values (or vals_out over the keys) would be overwritten before it is
+    read: rejected with FL_E_ARG, nothing launched."""
+    n = 1024
+    k = torch.zeros(n, dtype=torch.int64, device="cuda")
+    v = torch.zeros(2 * n, dtype=torch.int32, device="cuda")  # 8 n bytes: room for n keys too
+    ko = torch.empty_like(k)
+    torch.cuda.synchronize()
+    with pytest.raises(FlError) as e:  # keys_out placed over the values
+        radix_sort_noalloc(k.data_ptr(), v.data_ptr(), n, 0, v.data_ptr(), ko.data_ptr(), 0)
+    assert e.value.code == FL_E_ARG
+    with pytest.raises(FlError) as e:  # vals_out placed over the keys
+        radix_sort_noalloc(k.data_ptr(), v.data_ptr(), n, 0, ko.data_ptr(), k.data_ptr(), 0)
+    assert e.value.code == FL_E_ARG
