@@ -883,16 +883,17 @@ struct WalkShared {
 // whose widest cell is too close (the child is approximated at the first, widest, depth of the
 // chain that passes the theta test), a zero component of the displacement (d3 replaces it with
 // a jiggle) and distanceMin. `va` arrives as the value at the chain's top depth.
-// The jiggle's ids of a pair are the graph's own: a point's node index less its graph's first
-// node (`first`: 0 outside a batch), and for a cell a hash of its centroid's bits (a point's ids
-// are below 2^26, a cell's have the top bit set), so that a layout draws the same jiggles alone
-// or in any batch.
+// The jiggle's ids of a pair are the graph's own, so that a layout draws the same jiggles alone
+// or in any batch: a point's node index less its graph's first node (`first`), and for a cell
+// the graph's node count `ng` plus the cell's first child slot counted from the graph's first
+// (`cellbase`: the slot before it). Outside a batch: first 0, ng = n, cellbase 0.
 template <int NDIM>
 __device__ __forceinline__ void rare_case(uint32_t meta, uint32_t top, uint32_t idx, float T0,
                                           float dmin2, uint32_t myid, uint32_t first,
+                                          uint32_t ng, uint32_t cellbase,
                                           const uint32_t* __restrict__ perm, int n, uint32_t step,
-                                          uint32_t seed, float cx, float cy, float cz, float& va,
-                                          float& dx, float& dy, float& dz, float& l) {
+                                          uint32_t seed, float& va, float& dx, float& dy,
+                                          float& dz, float& l) {
   if (meta != kLeafMark) {
     const uint32_t D = (meta >> 26) & 31u;
     if (top < D && T0 * pow4neg(top) >= l) {
@@ -905,8 +906,7 @@ __device__ __forceinline__ void rare_case(uint32_t meta, uint32_t top, uint32_t 
     const uint32_t other =
         meta == kLeafMark
             ? perm[idx < (uint32_t)n ? idx : 0] - first
-            : 0x80000000u | fl::mix32(__float_as_uint(cx) ^
-                                      fl::mix32(__float_as_uint(cy) ^ fl::mix32(__float_as_uint(cz))));
+            : ng + (idx - cellbase);
     myid -= first;
     if (dx == 0.f) dx = fl::jiggle(myid, other, 0, step, seed), l += dx * dx;
     if (NDIM > 1 && dy == 0.f) dy = fl::jiggle(myid, other, 1, step, seed), l += dy * dy;
@@ -989,7 +989,7 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
   const uint64_t MX = pk2(me.x, me.x), MY = pk2(me.y, me.y), MZ = pk2(me.z, me.z);
   // the lane's own graph: what its uncommon cases and distanceMax use
   float myT0 = T0, mydmin2 = dmin2, mydmax2 = dmax2;
-  uint32_t myfirst = 0, mystep = step;
+  uint32_t myfirst = 0, mystep = step, myng = (uint32_t)n, mycb = 0;
   int sp;
   if (!BATCH) {
     if (gl == 0 && act) sset(0, make_uint4(0u, 1u, 0u, act));  // the root: slot 0, top depth 0
@@ -1002,7 +1002,10 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
     if (live) {
       const FlGraph& gr = segs.g[g];
       myT0 = gr.T0, mydmin2 = gr.dmin2, mydmax2 = gr.dmax2;
-      myfirst = (uint32_t)gr.first, mystep = step + gr.tick0;
+      myfirst = (uint32_t)gr.first, mystep = step + gr.tick0, myng = (uint32_t)gr.count;
+      // the graph's root sits in slot g; its first child slot less one is where the graph's
+      // slots are counted from (a lone simulation's root has its children from slot 1)
+      if (gr.count > 1) mycb = __ldg(&cmeta[g].x) - 1u;
       tree = gr.count > 1 && !gr.frozen;
     }
     const uint32_t peers = __match_any_sync(FL_FULL, tree ? g : 0xffffffffu) & gmask;
@@ -1116,13 +1119,13 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
           float2 dx = up2(DX), dy = up2(DY), dz = up2(DZ);
           if (c0) {
             const uint2 k0 = scold[j];
-            rare_case<NDIM>(k0.x, k0.y & 0xffu, r0.w, myT0, mydmin2, myid, myfirst, perm, n, mystep,
-                            seed, pa.x, pa.z, pb.x, v0, dx.x, dy.x, dz.x, l.x);
+            rare_case<NDIM>(k0.x, k0.y & 0xffu, r0.w, myT0, mydmin2, myid, myfirst, myng, mycb,
+                            perm, n, mystep, seed, v0, dx.x, dy.x, dz.x, l.x);
           }
           if (c1) {
             const uint2 k1 = scold[j + 1];
-            rare_case<NDIM>(k1.x, k1.y & 0xffu, r1.w, myT0, mydmin2, myid, myfirst, perm, n, mystep,
-                            seed, pa.y, pa.w, pb.y, v1, dx.y, dy.y, dz.y, l.y);
+            rare_case<NDIM>(k1.x, k1.y & 0xffu, r1.w, myT0, mydmin2, myid, myfirst, myng, mycb,
+                            perm, n, mystep, seed, v1, dx.y, dy.y, dz.y, l.y);
           }
           DX = pk2(dx.x, dx.y), DY = pk2(dy.x, dy.y), DZ = pk2(dz.x, dz.y);
         }
