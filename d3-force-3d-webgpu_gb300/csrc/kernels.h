@@ -86,13 +86,14 @@ struct FlSortBufs {
   uint32_t test_spins;
 };
 constexpr int kSortCounters = 16;
-// A onesweep tile: kSortItems pairs per thread; 1024 threads, or 256 for up to kSortSmallMax
-// pairs (small sorts take more, shorter tiles: the time of a pass is that of one tile's steps).
+// A onesweep tile: 256 threads x kSortItems pairs for up to kSortSmallMax pairs (small sorts
+// take more, shorter tiles: the time of a pass is that of one tile's steps); above, 1024 threads
+// x 5 to kSortItems pairs, as few as give every SM a tile (fl_sort_tile).
 constexpr int kSortThreads = 1024, kSortThreadsSmall = 256, kSortItems = 8;
-constexpr int kSortTile = kSortThreads * kSortItems, kSortTileSmall = kSortThreadsSmall * kSortItems;
+constexpr int kSortTileSmall = kSortThreadsSmall * kSortItems;
 constexpr int64_t kSortSmallMax = 131072;
 int fl_sort_tile(int64_t n);  // pairs per tile for a sort of n pairs
-int fl_sms();        // SMs of the current device (cached per process)
+int fl_sms();        // SMs of the current device (cached per device)
 size_t fl_sort_bytes(int64_t n);
 // Carve the buffers out of one allocation of fl_sort_bytes(n) bytes.
 void fl_sort_carve(FlSortBufs* b, void* base, int64_t n);

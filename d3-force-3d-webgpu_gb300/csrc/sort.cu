@@ -3,7 +3,7 @@
 // Replaces the reference's three-dispatch-per-digit sort (src/gpu/sort.js:4-20, 139-190) with
 // the GB300 form of Adinets & Merrill's "Onesweep" (2022): the digit histograms of every pass
 // come from one read of the keys (fused into the key producer where possible); each pass is one
-// kernel that ranks a tile of kSortTile keys by digit within each warp (eight ballots, one per digit
+// kernel that ranks a tile of keys (fl_sort_tile) by digit within each warp (eight ballots, one per digit
 // bit, give the lanes that share a lane's digit: cheaper here than the match instruction), publishes
 // the tile's digit counts, and takes its global offsets from a decoupled look-back over the
 // preceding tiles (bounded: a wait gives up after FL_SPIN_LIMIT polls and raises an error bit
@@ -15,7 +15,6 @@
 
 namespace {
 
-constexpr int kItems = kSortItems;
 constexpr uint32_t kValMask = (1u << 30) - 1;
 constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagPre = 2u << 30;
@@ -80,7 +79,7 @@ __device__ __forceinline__ uint32_t match_digit(uint32_t d, bool valid) {
   return valid ? m : (1u << (threadIdx.x & 31));
 }
 
-template <int kThreads>
+template <int kThreads, int kItems>
 __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_onesweep(
     const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
     uint32_t* __restrict__ vout, int64_t n, int shift, const uint32_t* __restrict__ ghist,
@@ -390,17 +389,17 @@ static bool first_on_device(std::atomic<uint64_t>& done) {
   return !(done.fetch_or(bit) & bit);
 }
 
-template <int T>
+template <int T, int I>
 void launch_pass(const uint64_t* kin, const uint32_t* vin, uint64_t* kout, uint32_t* vout,
                  int64_t n, int shift, const uint32_t* ghist, uint32_t* status, uint32_t* ticket,
                  uint32_t* err, uint32_t spin_limit, int hold, cudaStream_t st) {
   static std::atomic<uint64_t> configured{0};
-  const size_t dyn = (size_t)T * kItems * 12;
+  const size_t dyn = (size_t)T * I * 12;
   if (first_on_device(configured))
-    cudaFuncSetAttribute(k_onesweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
-  const int64_t tiles = (n + T * kItems - 1) / (T * kItems);
-  k_onesweep<T><<<(int)tiles, T, dyn, st>>>(kin, vin, kout, vout, n, shift, ghist, status, ticket,
-                                            err, spin_limit, hold);
+    cudaFuncSetAttribute(k_onesweep<T, I>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+  const int64_t tiles = (n + T * I - 1) / (T * I);
+  k_onesweep<T, I><<<(int)tiles, T, dyn, st>>>(kin, vin, kout, vout, n, shift, ghist, status,
+                                               ticket, err, spin_limit, hold);
 }
 uint32_t longs_cap_for(int64_t n) { return (uint32_t)(n / (kRunShort + 1) + 1); }
 
@@ -445,7 +444,18 @@ __global__ void __launch_bounds__(kRankWarps * 32) k_ranksort(const uint64_t* __
 
 }  // namespace
 
-int fl_sort_tile(int64_t n) { return n <= kSortSmallMax ? kSortTileSmall : kSortTile; }
+// Keys per thread of a pass's tiles of 1024 threads: as few as fill every SM with one tile (the
+// pass then takes one wave, each tile's time growing with its keys), from 5 up to 8 (beyond
+// 152 SMs x 8 x 1024 = 1.2 M keys, more than one wave of the largest tiles).
+static int sort_items(int64_t n) {
+  const int64_t per_sm = (int64_t)fl_sms() * kSortThreads;
+  int64_t it = (n + per_sm - 1) / per_sm;
+  return it < 5 ? 5 : it > kSortItems ? kSortItems : (int)it;
+}
+
+int fl_sort_tile(int64_t n) {
+  return n <= kSortSmallMax ? kSortTileSmall : kSortThreads * sort_items(n);
+}
 
 // The SM count of the current device, queried once per device index. The cache entries are
 // atomics: threads that race on a device's first query store the same value.
@@ -518,14 +528,17 @@ int fl_sort_passes(const FlSortBufs* b, int64_t n, int lo_bit, uint32_t* err, cu
   for (int p = 0; p < passes; ++p) {
     uint32_t* status = b->status + (size_t)p * tiles * 256;
     const int hold = b->test_spins && p == 0;
-    if (fl_sort_tile(n) == kSortTileSmall)
-      launch_pass<kSortThreadsSmall>(b->keys[cur], b->vals[cur], b->keys[1 - cur], b->vals[1 - cur],
-                                     n, lo_bit + 8 * p, b->hist + p * 256, status, b->counters + p,
-                                     err, limit, hold, st);
-    else
-      launch_pass<kSortThreads>(b->keys[cur], b->vals[cur], b->keys[1 - cur], b->vals[1 - cur], n,
-                                lo_bit + 8 * p, b->hist + p * 256, status, b->counters + p, err,
-                                limit, hold, st);
+#define FL_PASS(T, I)                                                                          \
+  launch_pass<T, I>(b->keys[cur], b->vals[cur], b->keys[1 - cur], b->vals[1 - cur], n,            \
+                    lo_bit + 8 * p, b->hist + p * 256, status, b->counters + p, err, limit, hold, st)
+    switch (fl_sort_tile(n)) {
+      case kSortTileSmall: FL_PASS(kSortThreadsSmall, kSortItems); break;
+      case 5 * kSortThreads: FL_PASS(kSortThreads, 5); break;
+      case 6 * kSortThreads: FL_PASS(kSortThreads, 6); break;
+      case 7 * kSortThreads: FL_PASS(kSortThreads, 7); break;
+      default: FL_PASS(kSortThreads, 8); break;
+    }
+#undef FL_PASS
     ++*launches;
     cur = 1 - cur;
   }

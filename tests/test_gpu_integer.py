@@ -13,7 +13,7 @@ from gpu_helpers import make_nodes
 
 pytestmark = pytest.mark.gpu
 
-SMALL_TILE, TILE = 2048, 8192  # pairs per onesweep tile: up to 131,072 pairs, and above
+SMALL_TILE, TILE = 2048, 5120  # pairs per onesweep tile: up to 131,072 pairs, and the fewest above
 
 
 def lcg_keys(n, spread, seed=7):
@@ -28,8 +28,11 @@ def stable_order(keys):
     return np.argsort(keys, kind="stable")
 
 
+# above 131,072 pairs the tiles hold 1024 threads x 5 to 8 pairs, as few as give every SM one
+# (5 up to 152 x 5,120 pairs, then 6, 7 and 8)
 @pytest.mark.parametrize("n", [1, 2, 3, 255, 256, 257, SMALL_TILE - 1, SMALL_TILE, SMALL_TILE + 1,
-                               3 * SMALL_TILE + 17, 100000, 131072, 131073, 131072 + 3 * TILE + 5])
+                               3 * SMALL_TILE + 17, 100000, 131072, 131073, 131072 + 3 * TILE + 5,
+                               700001, 900000, 1_100_003, 1_300_000])
 def test_sort_random_32bit_keys(n):
     keys32 = lcg_keys(n, 1 << 32)
     keys = keys32 << np.uint64(32)
