@@ -64,6 +64,11 @@ struct fl_batch {
   Buf pos, vel[2], fix, mask, gid, off, prm, red, gr, alphas, charge, row, entry, code, errw;
   Buf sort1, sort2, tree, gid_pos, groups;
   int32_t ngroups = 0;
+  // collide: per-node radii, the grid (run starts, sorted snapshot, sorted graph ids) and the
+  // most iterations any graph's collide force has (0: no graph collides)
+  Buf radius, grid, sgid;
+  FlGridBufs gb{};
+  int32_t citer_max = 0;
   FlSortBufs sb{}, sb2{};
   FlTreeBufs tb{};
   int cur = 0;
@@ -192,6 +197,21 @@ void encode_batch_tick(fl_batch* b, const double* alpha, const FlTick* tk) {
                    err, nullptr, 32, st, segs, tk);
     ++b->launches;
   }
+  // collide (every graph with a collide force, each with its own cell side and iterations),
+  // against a snapshot: read v, write the other velocity buffer. Its sort reuses the trees'
+  // first sort buffers, free once the walk has run.
+  for (int it = 0; it < b->citer_max; ++it) {
+    const int gbits = b->gb.bits, lo_bit = 63 - gbits;
+    fl_sort_reset(&b->sb, n, (64 - lo_bit + 7) / 8, st);
+    fl_launch_bgrid_keys(b->pos.as<float4>(), bvel(b), n, b->ndim, gid, gr, it, gbits,
+                         b->sb.keys[0], b->sb.vals[0], b->sb.hist, lo_bit, st);
+    const int r = fl_sort_passes(&b->sb, n, lo_bit, err, st, &b->launches);
+    fl_launch_bgrid_query(&b->gb, b->sb.keys[r], b->sb.vals[r], b->pos.as<float4>(), bvel(b),
+                          b->vel[1 - b->cur].as<float4>(), b->radius.as<float>(), b->ndim, gid, gr,
+                          b->sgid.as<uint32_t>(), tk, st, &b->launches);
+    b->cur = 1 - b->cur;
+    ++b->launches;
+  }
   // centre shift (per graph) and integration
   fl_launch_integrate(b->pos.as<float4>(), bvel(b), b->fix.as<float4>(), b->mask.as<uint32_t>(),
                       n, b->ndim, 1.f, nullptr, 0, 0, 0, 0, st, gr, gid);
@@ -271,6 +291,8 @@ int32_t fl_batch_set_graphs(fl_batch* b, int32_t ndim, int32_t graphs, const fl_
   std::vector<float> charge((size_t)std::max<int64_t>(n, 1), -30.f);
   std::vector<int32_t> off(graphs + 1, 0);
   std::vector<FlBatchParams> prm(graphs);
+  std::vector<float> radius((size_t)std::max<int64_t>(n, 1), 0.f);
+  int32_t citer_max = 0;
   bool neg = false, posv = false;
   double smax = 0, dmax_any = INFINITY;
   // the walk's point groups: each graph's sorted positions in runs of 32 from its first one (a
@@ -280,6 +302,7 @@ int32_t fl_batch_set_graphs(fl_batch* b, int32_t ndim, int32_t graphs, const fl_
     off[g] = at;
     const fl_graph_desc& x = d[g];
     double gmax = x.charge ? 0.0 : 30.0;
+    float rmax = 0.f;  // collide: the graph's largest radius
     if (x.n >= 2)
       for (int32_t j = 0; j < x.n; j += 32)
         groups.push_back(make_uint2((uint32_t)(at + j), (uint32_t)(at + std::min(j + 32, x.n))));
@@ -290,6 +313,11 @@ int32_t fl_batch_set_graphs(fl_batch* b, int32_t ndim, int32_t graphs, const fl_
         if (x.vel4 && k < ndim) vel[4 * (size_t)(at + i) + k] = x.vel4[4 * (size_t)i + k];
       }
       gid[at + i] = (uint32_t)g;
+      if (x.radii) {  // non-numbers count as 0, as the plain engine's radii
+        const float r = std::isfinite(x.radii[i]) ? x.radii[i] : 0.f;
+        radius[at + i] = r;
+        rmax = std::max(rmax, r);
+      }
       const float c = x.charge ? x.charge[i] : -30.f;
       charge[at + i] = std::isfinite(c) ? c : 0.f;
       neg = neg || charge[at + i] < 0.f, posv = posv || charge[at + i] > 0.f;
@@ -300,7 +328,16 @@ int32_t fl_batch_set_graphs(fl_batch* b, int32_t ndim, int32_t graphs, const fl_
     // out the same bit for bit, alone or in any batch
     prm[g] = FlBatchParams{x.theta2, x.distance_min2, x.distance_max2, x.center_x, x.center_y,
                            x.center_z, x.center_strength, 1.0 - x.velocity_decay,
-                           fl_fixed_exponent(x.n, gmax * (ndim == 1 ? 8192.0 : 1.0)), x.tick0};
+                           fl_fixed_exponent(x.n, gmax * (ndim == 1 ? 8192.0 : 1.0)), x.tick0,
+                           0, 0.f, 0.f};
+    // collide as the plain engine runs it: cells twice the largest radius, nothing to do
+    // without a radius above 0 or a second node
+    if (x.radii && x.n >= 2 && rmax > 0.f && x.collide_iterations > 0) {
+      prm[g].citer = x.collide_iterations;
+      prm[g].cinv = 1.f / (2.f * rmax);
+      prm[g].cstr = (float)x.collide_strength;
+      citer_max = std::max(citer_max, x.collide_iterations);
+    }
     if (x.distance_max2 < 3e38) dmax_any = 1.0;  // some graph has a finite distanceMax
     at += x.n;
     off[g + 1] = at;
@@ -377,6 +414,13 @@ int32_t fl_batch_set_graphs(fl_batch* b, int32_t ndim, int32_t graphs, const fl_
   FB_CK(b, b->sort1.reserve(fl_sort_bytes(n)));
   FB_CK(b, b->sort2.reserve(fl_sort_bytes(n)));
   FB_CK(b, b->tree.reserve(fl_tree_bytes(n)));
+  b->citer_max = citer_max;
+  if (citer_max) {
+    FB_CK(b, b->radius.reserve(4 * N));
+    FB_CK(b, b->grid.reserve(fl_grid_bytes(n)));
+    FB_CK(b, b->sgid.reserve(4 * N));
+    fl_grid_carve(&b->gb, b->grid.p, n);
+  }
   b->ngroups = (int32_t)groups.size();
   FB_CK(b, b->groups.reserve(8 * std::max<size_t>(groups.size(), 1)));
   fl_sort_carve(&b->sb, b->sort1.p, n);
@@ -391,6 +435,8 @@ int32_t fl_batch_set_graphs(fl_batch* b, int32_t ndim, int32_t graphs, const fl_
   FB_CK(b, cudaMemsetAsync(b->mask.p, 0, 4 * N, st));
   FB_CK(b, cudaMemcpyAsync(b->gid.p, gid.data(), 4 * N, cudaMemcpyHostToDevice, st));
   FB_CK(b, cudaMemcpyAsync(b->charge.p, charge.data(), 4 * N, cudaMemcpyHostToDevice, st));
+  if (citer_max)
+    FB_CK(b, cudaMemcpyAsync(b->radius.p, radius.data(), 4 * N, cudaMemcpyHostToDevice, st));
   FB_CK(b, cudaMemcpyAsync(b->off.p, off.data(), 4 * (size_t)(graphs + 1), cudaMemcpyHostToDevice, st));
   FB_CK(b, cudaMemcpyAsync(b->prm.p, prm.data(), sizeof(FlBatchParams) * (size_t)graphs,
                            cudaMemcpyHostToDevice, st));
@@ -644,7 +690,8 @@ int32_t fl_batch_query(fl_batch* b, int32_t what, int64_t* out) {
     case FL_Q_DEVICE_BYTES: {
       const Buf* all[] = {&b->pos, &b->vel[0], &b->vel[1], &b->fix, &b->mask, &b->gid, &b->off,
                           &b->prm, &b->red, &b->gr, &b->alphas, &b->charge, &b->row, &b->entry,
-                          &b->code, &b->sort1, &b->sort2, &b->tree, &b->gid_pos};
+                          &b->code, &b->sort1, &b->sort2, &b->tree, &b->gid_pos,
+                          &b->groups, &b->radius, &b->grid, &b->sgid};
       size_t s = 0;
       for (const Buf* x : all) s += x->bytes;
       *out = (int64_t)s;

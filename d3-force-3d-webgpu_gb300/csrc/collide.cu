@@ -206,7 +206,163 @@ __global__ void __launch_bounds__(kThreads) k_grid_query(
   vel_out[i] = v;
 }
 
+// ---- batches: one grid over all the graphs of a batch, each with its own cell side
+
+// The slot of a graph's cell: as cell_slot, the graph mixed into the hash of the block, so that
+// different graphs' cells spread over the table (two sharing a slot only cost tests, and a node
+// never pairs with another graph's).
+__device__ __forceinline__ uint32_t bcell_slot(int cx, int cy, int cz, int ndim, uint32_t mask,
+                                               uint32_t g) {
+  uint32_t bx, by = 0, bz = 0, w;
+  if (ndim == 3) {
+    bx = (uint32_t)cx >> 2, by = (uint32_t)cy >> 2, bz = (uint32_t)cz >> 2;
+    w = spread3_3(cx & 3) | spread3_3(cy & 3) << 1 | spread3_3(cz & 3) << 2;
+  } else if (ndim == 2) {
+    bx = (uint32_t)cx >> 3, by = (uint32_t)cy >> 3;
+    w = spread2_3(cx & 7) | spread2_3(cy & 7) << 1;
+  } else {
+    bx = (uint32_t)cx >> 6;
+    w = cx & 63;
+  }
+  const uint32_t h = fl::mix32(bx ^ fl::mix32(by ^ fl::mix32(bz ^ fl::mix32(g + 0x9e3779b9u))));
+  return ((h << 6) + w) & mask;
+}
+
+// A node takes part in iteration `iter` when its graph has that many collide iterations and
+// does not sit the tick out.
+__device__ __forceinline__ bool bcollides(const FlGraph& g, int iter) {
+  return g.citer > iter && !g.frozen;
+}
+
+__global__ void __launch_bounds__(kKeyThreads) k_bgrid_keys(
+    const float4* __restrict__ pos, const float4* __restrict__ vel, int n, int ndim,
+    const uint32_t* __restrict__ gid, const FlGraph* __restrict__ gr, int iter, int bits,
+    uint64_t* __restrict__ keys, uint32_t* __restrict__ vals, uint32_t* __restrict__ hist,
+    int lo_bit) {
+  __shared__ uint32_t sh[8 * 256];
+  for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) sh[i] = 0;
+  __syncthreads();
+  const int passes = (64 - lo_bit + 7) / 8;
+  const uint32_t mask = (1u << bits) - 1;
+  const int stride = gridDim.x * blockDim.x;
+  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const int i = base + threadIdx.x;
+    const bool ok = i < n;
+    uint64_t key = ~0ull;  // not taking part: after every cell
+    if (ok) {
+      const uint32_t g = gid[i];
+      const FlGraph& G = gr[g];
+      if (bcollides(G, iter)) {
+        const float4 p = pos[i], v = vel[i];
+        const int cx = cell_coord(p.x + v.x, G.cinv);
+        const int cy = ndim > 1 ? cell_coord(p.y + v.y, G.cinv) : 0;
+        const int cz = ndim > 2 ? cell_coord(p.z + v.z, G.cinv) : 0;
+        key = (uint64_t)bcell_slot(cx, cy, cz, ndim, mask, g) << (63 - bits);
+      }
+      keys[i] = key;
+      vals[i] = (uint32_t)i;
+    }
+    for (int p = 0; p < passes; ++p)
+      fl::hist_add(sh + p * 256, (uint32_t)(key >> (lo_bit + 8 * p)) & 255u, ok);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < passes * 256; i += blockDim.x)
+    if (sh[i]) atomicAdd(&hist[i], sh[i]);
+}
+
+// Run starts of the cells, and each sorted node's snapshot position, radius and graph.
+__global__ void __launch_bounds__(kThreads) k_bgrid_begin(
+    const uint64_t* __restrict__ skeys, const uint32_t* __restrict__ perm,
+    const float4* __restrict__ pos, const float4* __restrict__ vel,
+    const float* __restrict__ radius, const uint32_t* __restrict__ gid, int n, int bits,
+    uint32_t* __restrict__ starts, float4* __restrict__ sorted, uint32_t* __restrict__ sgid) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const uint64_t k = skeys[s];
+  if (k == ~0ull) return;  // not taking part (and sorted after every node that does)
+  if (s == 0 || skeys[s - 1] != k) starts[(uint32_t)(k >> (63 - bits))] = (uint32_t)s;
+  const uint32_t i = perm[s];
+  const float4 p = pos[i], v = vel[i];
+  sorted[s] = make_float4(p.x + v.x, p.y + v.y, p.z + v.z, radius[i]);
+  sgid[s] = gid[i];
+}
+
+// Each node's pushes from the overlapping nodes of its own graph in the 3^d cells around its
+// own (the jiggle's ids and step are the graph's own: the same alone or in any batch).
+__global__ void __launch_bounds__(kThreads) k_bgrid_query(
+    const uint64_t* __restrict__ skeys, const uint32_t* __restrict__ perm,
+    const uint32_t* __restrict__ starts, const float4* __restrict__ sorted,
+    const uint32_t* __restrict__ sgid, const FlGraph* __restrict__ gr,
+    const float4* __restrict__ vel_in, float4* __restrict__ vel_out, int n, int ndim, int bits,
+    const FlTick* __restrict__ tk) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const uint32_t i = perm[s];
+  float4 v = vel_in[i];
+  const uint64_t mykey = skeys[s];
+  if (mykey != ~0ull) {
+    const uint32_t g = sgid[s];
+    const FlGraph& G = gr[g];
+    const uint32_t first = (uint32_t)G.first, step = tk->step + G.tick0, seed = tk->seed;
+    const float4 me4 = sorted[s];
+    const float3 me = make_float3(me4.x, me4.y, me4.z);
+    const float ri = me4.w, ri2 = ri * ri;
+    const uint32_t mask = (1u << bits) - 1;
+    const int hx = cell_coord(me.x, G.cinv), hy = ndim > 1 ? cell_coord(me.y, G.cinv) : 0,
+              hz = ndim > 2 ? cell_coord(me.z, G.cinv) : 0;
+    const int ry = ndim > 1 ? 1 : 0, rz = ndim > 2 ? 1 : 0;
+    uint32_t seen[27];
+    int nseen = 0;
+    float3 acc = make_float3(0.f, 0.f, 0.f);
+    for (int dz = -rz; dz <= rz; ++dz)
+      for (int dy = -ry; dy <= ry; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+          const uint32_t slot = bcell_slot(hx + dx, hy + dy, hz + dz, ndim, mask, g);
+          bool again = false;
+          for (int q = 0; q < nseen; ++q) again |= seen[q] == slot;
+          if (again) continue;
+          seen[nseen++] = slot;
+          const uint32_t start = starts[slot];
+          const uint64_t key = (uint64_t)slot << (63 - bits);
+          if (start >= (uint32_t)n || skeys[start] != key || (start > 0 && skeys[start - 1] == key))
+            continue;
+          for (uint32_t t = start; t < (uint32_t)n && skeys[t] == key; ++t)
+            if (t != (uint32_t)s && sgid[t] == g)
+              pair_push(me, ri2, ri, sorted[t], i - first, perm[t] - first, ndim, G.cstr, step,
+                        seed, acc);
+        }
+    v.x += acc.x;
+    if (ndim > 1) v.y += acc.y;
+    if (ndim > 2) v.z += acc.z;
+  }
+  vel_out[i] = v;
+}
+
 }  // namespace
+
+void fl_launch_bgrid_keys(const float4* pos, const float4* vel, int n, int ndim,
+                          const uint32_t* gid, const FlGraph* gr, int iter, int bits,
+                          uint64_t* keys, uint32_t* vals, uint32_t* hist, int lo_bit,
+                          cudaStream_t st) {
+  int g = (n + kKeyThreads - 1) / kKeyThreads;  // as fl_launch_grid_keys
+  if (g > 2 * fl_sms()) g = 2 * fl_sms();
+  if (g < 1) g = 1;
+  k_bgrid_keys<<<g, kKeyThreads, 0, st>>>(pos, vel, n, ndim, gid, gr, iter, bits, keys, vals,
+                                          hist, lo_bit);
+}
+
+void fl_launch_bgrid_query(const FlGridBufs* g, const uint64_t* skeys, const uint32_t* perm,
+                           const float4* pos, const float4* vel_in, float4* vel_out,
+                           const float* radius, int ndim, const uint32_t* gid,
+                           const FlGraph* gr, uint32_t* sgid, const FlTick* tk, cudaStream_t st,
+                           int64_t* launches) {
+  const int n = g->n, blocks = (n + kThreads - 1) / kThreads;
+  k_bgrid_begin<<<blocks, kThreads, 0, st>>>(skeys, perm, pos, vel_in, radius, gid, n, g->bits,
+                                             g->starts, g->sorted, sgid);
+  k_bgrid_query<<<blocks, kThreads, 0, st>>>(skeys, perm, g->starts, g->sorted, sgid, gr, vel_in,
+                                             vel_out, n, ndim, g->bits, tk);
+  *launches += 2;
+}
 
 void fl_launch_collide_allpairs(const float4* pos, const float4* vel_in, float4* vel_out,
                                 const float* radius, int n, int ndim, float strength,

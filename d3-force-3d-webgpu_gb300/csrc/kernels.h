@@ -27,6 +27,8 @@ struct FlGraph {
   int32_t frozen;         // 1: the graph sits this tick out (its alpha was given as negative)
   int32_t fx;             // scale exponent of the graph's fixed-point cell sums
   uint32_t tick0;         // the graph's own tick count when the batch started (jiggle steps)
+  int32_t citer;          // collide: iterations (0: the graph has no collide force)
+  float cinv, cstr;       // collide: 1 / grid cell side (2 x largest radius); strength
   uint32_t pad;
 };
 // A batch of independent graphs, concatenated: graph g owns nodes [off[g], off[g+1]) and, after
@@ -53,6 +55,8 @@ struct FlBatchParams {
   int32_t fx;      // scale exponent of the fixed-point cell sums, from the graph's own size and
                    // strengths (as a lone simulation of that graph chooses it)
   uint32_t tick0;  // the graph's tick count when the batch started
+  int32_t citer;   // collide force: iterations (0: none), 1 / cell side, strength
+  float cinv, cstr;
 };
 void fl_launch_breduce(const float4* pos, int n, int ndim, const uint32_t* gid, FlReduce* red,
                        cudaStream_t st);
@@ -258,6 +262,20 @@ void fl_grid_carve(FlGridBufs* g, void* base, int64_t n);
 void fl_launch_grid_keys(const float4* pos, const float4* vel, int n, int ndim, float inv_cell,
                          int bits, uint64_t* keys, uint32_t* vals, uint32_t* hist, int lo_bit,
                          cudaStream_t st);
+// Collide in a batch: one grid over all graphs, cells keyed by (graph, cell); iteration `iter`
+// of each graph's collide force (a graph with fewer iterations, none, or sitting the tick out
+// keeps its velocities). keys[0]/vals[0] of the sort buffers take the cell keys (bit 63 clear;
+// ~0 for nodes not taking part), sorted on bits [lo_bit, 64); sgid[n] holds each sorted node's
+// graph.
+void fl_launch_bgrid_keys(const float4* pos, const float4* vel, int n, int ndim,
+                          const uint32_t* gid, const FlGraph* gr, int iter, int bits,
+                          uint64_t* keys, uint32_t* vals, uint32_t* hist, int lo_bit,
+                          cudaStream_t st);
+void fl_launch_bgrid_query(const FlGridBufs* g, const uint64_t* skeys, const uint32_t* perm,
+                           const float4* pos, const float4* vel_in, float4* vel_out,
+                           const float* radius, int ndim, const uint32_t* gid,
+                           const FlGraph* gr, uint32_t* sgid, const FlTick* tk, cudaStream_t st,
+                           int64_t* launches);
 void fl_launch_grid_query(const FlGridBufs* g, const uint64_t* skeys, const uint32_t* perm,
                           const float4* pos, const float4* vel_in, float4* vel_out,
                           const float* radius, int ndim, float inv_cell, float strength,

@@ -268,6 +268,7 @@ __global__ void __launch_bounds__(kThreads) k_bgraph(int graphs, int ndim, const
   o.frozen = alpha[g] < 0.0 ? 1 : 0;
   o.fx = p.fx;
   o.tick0 = p.tick0;
+  o.citer = p.citer, o.cinv = p.cinv, o.cstr = p.cstr;
   o.pad = 0u;
   gr[g] = o;
 }

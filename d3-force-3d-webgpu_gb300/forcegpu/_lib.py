@@ -72,6 +72,8 @@ class GraphDesc(ctypes.Structure):
         ("center_x", ctypes.c_double), ("center_y", ctypes.c_double), ("center_z", ctypes.c_double),
         ("center_strength", ctypes.c_double), ("velocity_decay", ctypes.c_double),
         ("tick0", ctypes.c_uint32),
+        ("radii", ctypes.c_void_p), ("collide_strength", ctypes.c_double),
+        ("collide_iterations", ctypes.c_int32),
     ]
 
 

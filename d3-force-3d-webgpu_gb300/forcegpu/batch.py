@@ -6,8 +6,9 @@
     b.run(300)                 # each graph's own alpha schedule (d3 defaults), 300 ticks
     positions = b.positions()  # one (n_g, ndim) array per graph
 
-Each graph has a link force, a many-body force and (optionally) a centre force, as the
-reference's benchmark layout; its parameters follow d3's defaults unless given. The alpha
+Each graph has a link force, a many-body force, optionally a collide force (after the
+many-body force) and optionally a centre force, as the reference's benchmark layout and the
+served jobs; its parameters follow d3's defaults unless given. The alpha
 schedule of every graph is d3's (src/simulation.js:28-32, :49-56), advanced on the host; a
 graph's own alphaDecay / alphaMin / alphaTarget may differ from the others'.
 """
@@ -46,6 +47,9 @@ class GraphSpec:
     alpha_target: float = 0.0
     vel: np.ndarray = None
     tick0: int = 0  # ticks the layout ran before (a job moved between batches keeps its count)
+    radii: np.ndarray = None  # collide radii (None: no collide force)
+    collide_strength: float = 1.0
+    collide_iterations: int = 1
     _keep: list = field(default_factory=list, repr=False)
 
 
@@ -115,6 +119,12 @@ class Batch:
             d.center_strength = s.center_strength
             d.velocity_decay = s.velocity_decay
             d.tick0 = int(s.tick0) & 0xffffffff
+            if s.radii is not None:
+                r = np.ascontiguousarray(np.broadcast_to(s.radii, (n,)), dtype=np.float32)
+                keep.append(r)
+                d.radii = r.ctypes.data
+                d.collide_strength = float(s.collide_strength)
+                d.collide_iterations = int(s.collide_iterations)
             s._keep = keep
         self._check(self.L.fl_batch_set_graphs(self.h, self.ndim, len(self.specs), descs))
         if seed is not None:

@@ -7,14 +7,14 @@ continuous batching on one GPU.
     job.result                    # (n, ndim) positions; job.latency in seconds
 
 Scheduling:
-  * Jobs with link + many-body + centre forces (the reference benchmark's force set) run in a
-    batch per dimensionality (fl_batch_*): every tick of a batch is one launch per kernel for
-    all its graphs. A batch advances in blocks of `block` ticks; between blocks, finished jobs
-    leave and waiting jobs join (the batch is rebuilt from the running jobs' current state), so
-    a request that arrives while others are on the GPU starts at the next block boundary. A job
-    whose tick count ends inside a block sits the rest of the block out (negative alpha).
-  * Jobs that also have a collide force run on their own plain engine (fl_sim), each on its own
-    CUDA stream, overlapping with the batches and with each other on the device.
+  * Every job (link + many-body + centre forces, the reference benchmark's force set, and for
+    some a collide force too) runs in a batch per dimensionality (fl_batch_*): every tick of a
+    batch is one launch per kernel for all its graphs. A batch advances in blocks of `block`
+    ticks; between blocks, finished jobs leave and waiting jobs join (the batch is rebuilt from
+    the running jobs' current state), so a request that arrives while others are on the GPU
+    starts at the next block boundary. A job whose tick count ends inside a block sits the rest
+    of the block out (negative alpha).
+  * With batching=False (the serial comparison), each job runs on its own plain engine (fl_sim).
   * Admission by device-memory footprint: a job is admitted when the footprints of the running
     jobs plus its own fit `hbm_budget`; jobs are admitted in arrival order.
 
@@ -114,7 +114,7 @@ class _Lane:
         return GraphSpec(xyz=j.pos[:, :self.ndim], source=j.source, target=j.target,
                          theta=j.theta, velocity_decay=j.velocity_decay,
                          vel=j.vel[:, :self.ndim] if j.vel is not None else None,
-                         tick0=j.done_ticks)
+                         tick0=j.done_ticks, radii=j.radii)
 
     def _rebuild(self, seed):
         live = self.live()
@@ -180,7 +180,7 @@ class LayoutServer:
         self.queue = deque()
         # the batches of 2D and 3D jobs exist from the start (creating one loads its kernels)
         self.lanes = {d: _Lane(d, device) for d in (2, 3)} if batching else {}
-        self.plain = []  # (job, engine) with a collide force
+        self.plain = []  # (job, engine, descs): each job on its own plain engine (batching off)
         # finished plain engines: freeing device memory waits for the whole device, so they are
         # closed when nothing else is in flight (or at close())
         self.retired = []
@@ -233,7 +233,7 @@ class LayoutServer:
             j.admitted = self.now()
             j.pos = np.zeros((j.n, 3))
             j.pos[:, :j.ndim] = j.xyz
-            if j.radii is not None or not self.batching:
+            if not self.batching:
                 self._start_plain(j)
             else:
                 lane = self.lanes.get(j.ndim)

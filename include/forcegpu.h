@@ -235,7 +235,8 @@ int32_t fl_profile_read(fl_sim* sim, int32_t cap, const char** names, double* ms
  * its closest relatives are the per-device engine sharing of src/gpu/device.js:4 and the
  * step batching of src/gpu/engine.js:7-9, :362-389. A batch holds G graphs, each with a link
  * force, a many-body force and an optional centre force (the forces of the reference's
- * benchmark), all in one dimensionality; every kernel of a tick runs once for the whole batch.
+ * benchmark), an optional collide force (applied after the many-body force, as the served jobs
+ * list it), all in one dimensionality; every kernel of a tick runs once for the whole batch.
  * Each graph has its own alpha schedule, theta, distances, centre and velocity decay. */
 typedef struct fl_graph_desc {
   int32_t n;                 /* nodes */
@@ -255,6 +256,9 @@ typedef struct fl_graph_desc {
                                 moved from batch to batch keeps its own tick count, which seeds
                                 its coincident-node jiggles, so its result does not depend on
                                 the batches it went through */
+  const float* radii;        /* [n] collide radii (src/collide.js:134-136), or NULL: no collide force */
+  double collide_strength;   /* collide strength (d3's default 1) */
+  int32_t collide_iterations; /* collide iterations (d3's default 1) */
 } fl_graph_desc;
 
 typedef struct fl_batch fl_batch;

@@ -24,7 +24,8 @@ def spec(n, dims, seed, **kw):
 
 
 def oracle_run(s, dims, ticks):
-    """The reference's CPU simulation of one graph (Jacobi links, as the GPU)."""
+    """The reference's CPU simulation of one graph (Jacobi links and collide, as the GPU), the
+    forces in the batch's order: link, many-body, collide, centre."""
     n = len(s.xyz)
     xyz = np.zeros((n, 3))
     xyz[:, :dims] = s.xyz
@@ -33,6 +34,9 @@ def oracle_run(s, dims, ticks):
     if len(s.source):
         o.link(s.source, s.target, mode=oracle.MODE_JACOBI)
     o.manybody(theta=s.theta, distanceMin=s.distance_min, distanceMax=s.distance_max)
+    if s.radii is not None:
+        o.collide(np.asarray(s.radii, float), s.collide_strength, s.collide_iterations,
+                  oracle.MODE_JACOBI)
     if s.center_strength:
         o.center(*s.center, strength=s.center_strength)
     o.tick(ticks)
@@ -66,6 +70,29 @@ def test_every_graph_of_a_batch_matches_the_oracle(dims):
 
 
 @pytest.mark.parametrize("dims", [2, 3])
+def test_graphs_with_collide_in_a_batch_match_the_oracle(dims):
+    """Collide in a batch: one grid over every graph, each with its own cell side (twice its
+    largest radius), strength and iterations; graphs without a collide force beside them."""
+    sizes = [300, 2, 1200, 40, 900, 5000]
+    specs = [spec(n, dims, 300 + i) for i, n in enumerate(sizes)]
+    rng = np.random.default_rng(8)
+    for i, s_ in enumerate(specs):
+        if i % 3 != 1:  # graphs 1 and 4 have no collide force
+            s_.radii = rng.uniform(1.0, 5.0, len(s_.xyz)).astype(np.float32).astype(float)
+            # dense enough for overlaps: spacing ~ a few radii
+            s_.xyz = np.float32(s_.xyz * (0.15 if dims == 3 else 0.05)).astype(float)
+    specs[2].collide_strength, specs[2].collide_iterations = 0.7, 2
+    b = Batch()
+    b.set_graphs(specs, ndim=dims, seed=7)
+    ticks = 3
+    b.run(ticks)
+    got = b.positions()
+    for s_, p in zip(specs, got):
+        want = oracle_run(s_, dims, ticks)
+        assert_close(p, want, 1e-3, tree_outliers(len(p)) + len(p) // 200)
+
+
+@pytest.mark.parametrize("dims", [2, 3])
 def test_a_graph_alone_and_in_a_mix_agree_bit_for_bit(dims):
     """The same graph laid out alone and among others, 300 ticks: its result does not depend on
     the rest of the batch (the continuous-batching property a server relies on). Every sum of a
@@ -74,9 +101,11 @@ def test_a_graph_alone_and_in_a_mix_agree_bit_for_bit(dims):
     the layouts agree bit for bit (a force layout is chaotic: any difference in the last bit
     would grow by orders of magnitude over 300 ticks)."""
     me = spec(900, dims, 5)
-    me.xyz = me.xyz.copy()
-    me.xyz[7] = me.xyz[3]  # a coincident pair: jiggles in the walk
+    me.xyz = me.xyz.copy() * 0.2
+    me.xyz[7] = me.xyz[3]  # a coincident pair: jiggles in the walk and the collide
+    me.radii = 1.0 + np.arange(900) % 4
     others = [spec(n, dims, 20 + i) for i, n in enumerate([300, 2, 1200, 77, 33])]
+    others[2].radii = np.full(1200, 3.0)
     alone = Batch()
     alone.set_graphs([me], ndim=dims, seed=3)
     alone.run(300)
