@@ -75,7 +75,8 @@ struct fl_batch {
   size_t alpha_cap = 0;
   uint32_t step = 0, seed = 0x9e3779b9u;
   int fx_exp = 32;
-  bool closed = true;
+  bool closed = true, neg = false, posv = false;  // strengths: some below 0, some above
+  double smax = 0;
   float sign = -1.f;
   double dmax_any = INFINITY;  // finite when some graph has a finite distanceMax
   int64_t ticks = 0, launches = 0;
@@ -267,191 +268,324 @@ int32_t fl_batch_destroy(fl_batch* b) {
 
 const char* fl_batch_last_error(const fl_batch* b) { return b ? b->err.c_str() : "no batch"; }
 
+}  // extern "C"
+
+namespace {
+
+// The host-side arrays of graphs [graph0, graph0 + count) of a batch, whose nodes start at node
+// node0 and links at link m0: what fl_batch_set_graphs uploads for all graphs and
+// fl_batch_add_graphs for the graphs it appends.
+struct HostPart {
+  int64_t n = 0, m = 0;
+  std::vector<float> pos, vel, charge, radius;
+  std::vector<uint32_t> gid;
+  std::vector<int32_t> off;  // count entries: each graph's first node (global)
+  std::vector<FlBatchParams> prm;
+  std::vector<uint2> groups;
+  std::vector<int32_t> row;  // n entries: the rows' ends (global entry offsets)
+  std::vector<float> entry;
+  std::vector<uint32_t> code;
+  bool neg = false, posv = false, has_radius = false;
+  double smax = 0, dmax_any = INFINITY;
+  int32_t citer_max = 0;
+};
+
+int32_t check_descs(fl_batch* b, int32_t count, const fl_graph_desc* d, int64_t* n, int64_t* m) {
+  *n = 0, *m = 0;
+  for (int32_t g = 0; g < count; ++g) {
+    if (d[g].n < 0 || d[g].m < 0 || (d[g].n && !d[g].pos4) || (d[g].m && (!d[g].source || !d[g].target)))
+      return bfail(b, FL_E_ARG, "graph " + std::to_string(g) + ": bad sizes or arrays");
+    if (!(d[g].theta2 >= 0) || !(d[g].distance_min2 >= 0) || !(d[g].distance_max2 > 0))
+      return bfail(b, FL_E_ARG, "graph " + std::to_string(g) + ": bad many-body parameters");
+    for (int32_t j = 0; j < d[g].m; ++j) {
+      const int32_t a = d[g].source[j], c = d[g].target[j];
+      if (a < 0 || a >= d[g].n || c < 0 || c >= d[g].n)
+        return bfail(b, FL_E_ARG, "graph " + std::to_string(g) + " link " + std::to_string(j) + ": node not found");
+    }
+    *n += d[g].n, *m += d[g].m;
+  }
+  return FL_OK;
+}
+
+// step0: the batch's tick counter when these graphs join (a graph's jiggle step is the batch's
+// plus its own tick count at joining, less step0).
+void build_part(int32_t ndim, int32_t count, const fl_graph_desc* d, int64_t node0, int32_t graph0,
+                int64_t m0, uint32_t step0, HostPart* hp) {
+  int64_t n = 0, m = 0;
+  for (int32_t g = 0; g < count; ++g) n += d[g].n, m += d[g].m;
+  hp->n = n, hp->m = m;
+  const size_t N = (size_t)std::max<int64_t>(n, 1);
+  hp->pos.assign(4 * N, 0.f), hp->vel.assign(4 * N, 0.f);
+  hp->gid.assign(N, 0u), hp->charge.assign(N, -30.f), hp->radius.assign(N, 0.f);
+  hp->off.assign(count, 0), hp->prm.assign(count, FlBatchParams{});
+  hp->groups.clear();
+  for (int32_t g = 0, at = 0; g < count; ++g) {
+    const int64_t gat = node0 + at;  // the graph's first node in the batch
+    hp->off[g] = (int32_t)gat;
+    const fl_graph_desc& x = d[g];
+    double gmax = x.charge ? 0.0 : 30.0;
+    float rmax = 0.f;  // collide: the graph's largest radius
+    // the walk's point groups: the graph's sorted positions in runs of 32 from its first one (a
+    // graph of one point has no tree and no group)
+    if (x.n >= 2)
+      for (int32_t j = 0; j < x.n; j += 32)
+        hp->groups.push_back(make_uint2((uint32_t)(gat + j), (uint32_t)(gat + std::min(j + 32, x.n))));
+    for (int32_t i = 0; i < x.n; ++i) {
+      for (int k = 0; k < 4; ++k) {
+        const float p = k < ndim ? x.pos4[4 * (size_t)i + k] : 0.f;
+        hp->pos[4 * (size_t)(at + i) + k] = std::isfinite(p) ? p : 0.f;
+        if (x.vel4 && k < ndim) hp->vel[4 * (size_t)(at + i) + k] = x.vel4[4 * (size_t)i + k];
+      }
+      hp->gid[at + i] = (uint32_t)(graph0 + g);
+      if (x.radii) {  // non-numbers count as 0, as the plain engine's radii
+        const float r = std::isfinite(x.radii[i]) ? x.radii[i] : 0.f;
+        hp->radius[at + i] = r;
+        rmax = std::max(rmax, r);
+      }
+      const float c = x.charge ? x.charge[i] : -30.f;
+      const float cc = std::isfinite(c) ? c : 0.f;
+      hp->charge[at + i] = cc;
+      hp->neg = hp->neg || cc < 0.f, hp->posv = hp->posv || cc > 0.f;
+      hp->smax = std::max(hp->smax, (double)std::fabs(cc));
+      gmax = std::max(gmax, (double)std::fabs(cc));
+    }
+    // the graph's own fixed-point scale, as a lone simulation of it chooses it: its cells come
+    // out the same bit for bit, alone or in any batch
+    hp->prm[g] = FlBatchParams{x.theta2, x.distance_min2, x.distance_max2, x.center_x, x.center_y,
+                               x.center_z, x.center_strength, 1.0 - x.velocity_decay,
+                               fl_fixed_exponent(x.n, gmax * (ndim == 1 ? 8192.0 : 1.0)),
+                               x.tick0 - step0, 0, 0.f, 0.f};
+    // collide as the plain engine runs it: cells twice the largest radius, nothing to do
+    // without a radius above 0 or a second node
+    if (x.radii) hp->has_radius = true;
+    if (x.radii && x.n >= 2 && rmax > 0.f && x.collide_iterations > 0) {
+      hp->prm[g].citer = x.collide_iterations;
+      hp->prm[g].cinv = 1.f / (2.f * rmax);
+      hp->prm[g].cstr = (float)x.collide_strength;
+      hp->citer_max = std::max(hp->citer_max, x.collide_iterations);
+    }
+    if (x.distance_max2 < 3e38) hp->dmax_any = 1.0;  // some graph has a finite distanceMax
+    at += x.n;
+  }
+  // links: a CSR over the part's nodes, node indices made global; d3's default strength and
+  // bias; each entry's code holds its link's index within its own graph (the jiggle of a link
+  // is the graph's own)
+  std::vector<int32_t> cnt(N + 1, 0);  // per node: its entries; then the rows' starts
+  {
+    int64_t at = 0;
+    for (int32_t g = 0; g < count; ++g) {
+      for (int32_t j = 0; j < d[g].m; ++j) ++cnt[at + d[g].source[j]], ++cnt[at + d[g].target[j]];
+      at += d[g].n;
+    }
+  }
+  hp->row.assign(N, 0);
+  std::vector<int32_t> cur(N, 0);
+  {
+    int64_t run = 2 * m0;
+    for (int64_t i = 0; i < n; ++i) cur[i] = (int32_t)(run - 2 * m0), run += cnt[i], hp->row[i] = (int32_t)run;
+  }
+  hp->entry.assign(4 * (size_t)std::max<int64_t>(2 * m, 1), 0.f);
+  hp->code.assign((size_t)std::max<int64_t>(2 * m, 1), 0u);
+  int64_t at = 0;
+  for (int32_t g = 0; g < count; ++g) {
+    const fl_graph_desc& x = d[g];
+    for (int32_t j = 0; j < x.m; ++j) {
+      const int32_t a = x.source[j], c = x.target[j];
+      const int32_t ga = (int32_t)(node0 + at + a), gc = (int32_t)(node0 + at + c);
+      const float dist = x.link_distance ? x.link_distance[j] : 30.f;
+      // src/link.js:73-75, :36-38: bias = count(source) / (count(source) + count(target)),
+      // strength = 1 / min(count(source), count(target))
+      const int32_t ca = cnt[at + a], cc = cnt[at + c];
+      const float bias = x.link_bias ? x.link_bias[j] : (float)((double)ca / (ca + cc));
+      const float str = x.link_strength ? x.link_strength[j] : (float)(1.0 / std::min(ca, cc));
+      int32_t e = cur[at + a]++;
+      std::memcpy(&hp->entry[4 * (size_t)e], &gc, 4);
+      hp->entry[4 * (size_t)e + 1] = dist, hp->entry[4 * (size_t)e + 2] = str;
+      hp->entry[4 * (size_t)e + 3] = (float)(1.0 - (double)bias);
+      hp->code[e] = 2u * (uint32_t)j;
+      e = cur[at + c]++;
+      std::memcpy(&hp->entry[4 * (size_t)e], &ga, 4);
+      hp->entry[4 * (size_t)e + 1] = dist, hp->entry[4 * (size_t)e + 2] = str;
+      hp->entry[4 * (size_t)e + 3] = bias;
+      hp->code[e] = 2u * (uint32_t)j + 1u;
+    }
+    at += x.n;
+  }
+}
+
+// The per-node and per-tick scratch of a batch of n nodes (recomputed every tick: no contents
+// to keep), and the collide grid.
+int32_t size_scratch(fl_batch* b) {
+  const int64_t n = b->n;
+  const size_t N = (size_t)std::max<int64_t>(n, 1);
+  FB_CK(b, b->gid_pos.reserve(4 * N));
+  FB_CK(b, b->red.reserve(sizeof(FlReduce) * (size_t)b->graphs));
+  FB_CK(b, b->gr.reserve(sizeof(FlGraph) * (size_t)b->graphs));
+  FB_CK(b, b->sort1.reserve(fl_sort_bytes(n)));
+  FB_CK(b, b->sort2.reserve(fl_sort_bytes(n)));
+  FB_CK(b, b->tree.reserve(fl_tree_bytes(n)));
+  fl_sort_carve(&b->sb, b->sort1.p, n);
+  fl_sort_carve(&b->sb2, b->sort2.p, n);
+  fl_tree_carve(&b->tb, b->tree.p, n, b->ndim);
+  if (b->citer_max) {
+    FB_CK(b, b->grid.reserve(fl_grid_bytes(n)));
+    FB_CK(b, b->sgid.reserve(4 * N));
+    fl_grid_carve(&b->gb, b->grid.p, n);
+  }
+  return FL_OK;
+}
+
+// At least `bytes` bytes in buf, keeping its first `keep` bytes (copied on the batch's stream).
+int32_t grow(fl_batch* b, Buf& buf, size_t bytes, size_t keep) {
+  if (buf.p && bytes <= buf.bytes) return FL_OK;
+  Buf nb;
+  FB_CK(b, nb.alloc(bytes + bytes / 2));
+  if (keep && buf.p) FB_CK(b, cudaMemcpyAsync(nb.p, buf.p, keep, cudaMemcpyDeviceToDevice, b->st));
+  FB_CK(b, cudaStreamSynchronize(b->st));
+  std::swap(buf.p, nb.p);
+  std::swap(buf.bytes, nb.bytes);
+  return FL_OK;  // nb frees the old buffer
+}
+
+// Upload part hp at nodes [node0, ...), graphs [graph0, ...), entries [2 m0, ...) (the buffers
+// already hold room for them), and fold its flags into the batch's.
+int32_t upload_part(fl_batch* b, const HostPart& hp, int64_t node0, int32_t graph0, int64_t m0,
+                    int32_t count) {
+  cudaStream_t st = b->st;
+  const size_t n = (size_t)hp.n;
+  if (n) {
+    FB_CK(b, cudaMemcpyAsync(b->pos.as<float4>() + node0, hp.pos.data(), 16 * n, cudaMemcpyHostToDevice, st));
+    FB_CK(b, cudaMemcpyAsync(bvel(b) + node0, hp.vel.data(), 16 * n, cudaMemcpyHostToDevice, st));
+    FB_CK(b, cudaMemsetAsync(b->fix.as<float4>() + node0, 0, 16 * n, st));
+    FB_CK(b, cudaMemsetAsync(b->mask.as<uint32_t>() + node0, 0, 4 * n, st));
+    FB_CK(b, cudaMemcpyAsync(b->gid.as<uint32_t>() + node0, hp.gid.data(), 4 * n, cudaMemcpyHostToDevice, st));
+    FB_CK(b, cudaMemcpyAsync(b->charge.as<float>() + node0, hp.charge.data(), 4 * n, cudaMemcpyHostToDevice, st));
+    if (b->radius.p)
+      FB_CK(b, cudaMemcpyAsync(b->radius.as<float>() + node0, hp.radius.data(), 4 * n, cudaMemcpyHostToDevice, st));
+    FB_CK(b, cudaMemcpyAsync(b->row.as<int32_t>() + node0 + 1, hp.row.data(), 4 * n, cudaMemcpyHostToDevice, st));
+  }
+  FB_CK(b, cudaMemcpyAsync(b->off.as<int32_t>() + graph0, hp.off.data(), 4 * (size_t)count,
+                           cudaMemcpyHostToDevice, st));
+  const int32_t end = (int32_t)(node0 + hp.n);
+  FB_CK(b, cudaMemcpyAsync(b->off.as<int32_t>() + graph0 + count, &end, 4, cudaMemcpyHostToDevice, st));
+  FB_CK(b, cudaMemcpyAsync(b->prm.as<FlBatchParams>() + graph0, hp.prm.data(),
+                           sizeof(FlBatchParams) * (size_t)count, cudaMemcpyHostToDevice, st));
+  if (!hp.groups.empty())
+    FB_CK(b, cudaMemcpyAsync(b->groups.as<uint2>() + (b->ngroups - hp.groups.size()), hp.groups.data(),
+                             8 * hp.groups.size(), cudaMemcpyHostToDevice, st));
+  if (hp.m) {
+    FB_CK(b, cudaMemcpyAsync(b->entry.as<float4>() + 2 * m0, hp.entry.data(), 32 * (size_t)hp.m,
+                             cudaMemcpyHostToDevice, st));
+    FB_CK(b, cudaMemcpyAsync(b->code.as<uint32_t>() + 2 * m0, hp.code.data(), 8 * (size_t)hp.m,
+                             cudaMemcpyHostToDevice, st));
+  }
+  b->hoff.resize((size_t)graph0);
+  b->hoff.insert(b->hoff.end(), hp.off.begin(), hp.off.end());
+  b->hoff.push_back(end);
+  // the host vectors may go out of scope at return: wait for the copies that read them
+  FB_CK(b, cudaStreamSynchronize(st));
+  return FL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int32_t fl_batch_set_graphs(fl_batch* b, int32_t ndim, int32_t graphs, const fl_graph_desc* d) {
   int32_t rc = bcheck(b);
   if (rc) return rc;
   if (ndim < 1 || ndim > 3) return bfail(b, FL_E_ARG, "ndim must be 1, 2 or 3");
   if (graphs < 1 || graphs > 65535 || !d) return bfail(b, FL_E_ARG, "graphs must be 1..65535");
-  FB_CK(b, cudaStreamSynchronize(b->st));
-  clear_blocks(b);
   int64_t n = 0, m = 0;
-  for (int32_t g = 0; g < graphs; ++g) {
-    if (d[g].n < 0 || d[g].m < 0 || (d[g].n && !d[g].pos4) || (d[g].m && (!d[g].source || !d[g].target)))
-      return bfail(b, FL_E_ARG, "graph " + std::to_string(g) + ": bad sizes or arrays");
-    if (!(d[g].theta2 >= 0) || !(d[g].distance_min2 >= 0) || !(d[g].distance_max2 > 0))
-      return bfail(b, FL_E_ARG, "graph " + std::to_string(g) + ": bad many-body parameters");
-    n += d[g].n, m += d[g].m;
-  }
+  if ((rc = check_descs(b, graphs, d, &n, &m))) return rc;
   if (n > kMaxBatchNodes) return bfail(b, FL_E_ARG, "too many nodes in one batch");
   if (m > (int64_t(1) << 30)) return bfail(b, FL_E_ARG, "too many links in one batch");
+  FB_CK(b, cudaStreamSynchronize(b->st));
+  clear_blocks(b);
+  HostPart hp;
+  build_part(ndim, graphs, d, 0, 0, 0, 0u, &hp);
   b->ndim = ndim, b->graphs = graphs, b->n = (int32_t)n, b->m = (int32_t)m;
-  // nodes: state, graph ids, charges; graphs: offsets and fixed parameters
-  std::vector<float> pos(4 * (size_t)std::max<int64_t>(n, 1), 0.f), vel(pos.size(), 0.f);
-  std::vector<uint32_t> gid((size_t)std::max<int64_t>(n, 1), 0);
-  std::vector<float> charge((size_t)std::max<int64_t>(n, 1), -30.f);
-  std::vector<int32_t> off(graphs + 1, 0);
-  std::vector<FlBatchParams> prm(graphs);
-  std::vector<float> radius((size_t)std::max<int64_t>(n, 1), 0.f);
-  int32_t citer_max = 0;
-  bool neg = false, posv = false;
-  double smax = 0, dmax_any = INFINITY;
-  // the walk's point groups: each graph's sorted positions in runs of 32 from its first one (a
-  // graph of one point has no tree and no group)
-  std::vector<uint2> groups;
-  for (int32_t g = 0, at = 0; g < graphs; ++g) {
-    off[g] = at;
-    const fl_graph_desc& x = d[g];
-    double gmax = x.charge ? 0.0 : 30.0;
-    float rmax = 0.f;  // collide: the graph's largest radius
-    if (x.n >= 2)
-      for (int32_t j = 0; j < x.n; j += 32)
-        groups.push_back(make_uint2((uint32_t)(at + j), (uint32_t)(at + std::min(j + 32, x.n))));
-    for (int32_t i = 0; i < x.n; ++i) {
-      for (int k = 0; k < 4; ++k) {
-        const float p = k < ndim ? x.pos4[4 * (size_t)i + k] : 0.f;
-        pos[4 * (size_t)(at + i) + k] = std::isfinite(p) ? p : 0.f;
-        if (x.vel4 && k < ndim) vel[4 * (size_t)(at + i) + k] = x.vel4[4 * (size_t)i + k];
-      }
-      gid[at + i] = (uint32_t)g;
-      if (x.radii) {  // non-numbers count as 0, as the plain engine's radii
-        const float r = std::isfinite(x.radii[i]) ? x.radii[i] : 0.f;
-        radius[at + i] = r;
-        rmax = std::max(rmax, r);
-      }
-      const float c = x.charge ? x.charge[i] : -30.f;
-      charge[at + i] = std::isfinite(c) ? c : 0.f;
-      neg = neg || charge[at + i] < 0.f, posv = posv || charge[at + i] > 0.f;
-      smax = std::max(smax, (double)std::fabs(charge[at + i]));
-      gmax = std::max(gmax, (double)std::fabs(charge[at + i]));
-    }
-    // the graph's own fixed-point scale, as a lone simulation of it chooses it: its cells come
-    // out the same bit for bit, alone or in any batch
-    prm[g] = FlBatchParams{x.theta2, x.distance_min2, x.distance_max2, x.center_x, x.center_y,
-                           x.center_z, x.center_strength, 1.0 - x.velocity_decay,
-                           fl_fixed_exponent(x.n, gmax * (ndim == 1 ? 8192.0 : 1.0)), x.tick0,
-                           0, 0.f, 0.f};
-    // collide as the plain engine runs it: cells twice the largest radius, nothing to do
-    // without a radius above 0 or a second node
-    if (x.radii && x.n >= 2 && rmax > 0.f && x.collide_iterations > 0) {
-      prm[g].citer = x.collide_iterations;
-      prm[g].cinv = 1.f / (2.f * rmax);
-      prm[g].cstr = (float)x.collide_strength;
-      citer_max = std::max(citer_max, x.collide_iterations);
-    }
-    if (x.distance_max2 < 3e38) dmax_any = 1.0;  // some graph has a finite distanceMax
-    at += x.n;
-    off[g + 1] = at;
-  }
-  b->closed = !(neg && posv);
-  b->sign = neg ? -1.f : 1.f;
-  b->fx_exp = fl_fixed_exponent(n, smax * (ndim == 1 ? 8192.0 : 1.0));
-  b->dmax_any = dmax_any;
-  // links: one CSR over the batch, node indices made global; d3's default strength and bias
-  std::vector<int32_t> row((size_t)n + 1, 0);
-  std::vector<int32_t> src((size_t)std::max<int64_t>(m, 1)), dst(src.size());
-  std::vector<float> dist(src.size()), str(src.size()), bias(src.size());
-  // each link's index within its own graph: the jiggle of a link is the graph's own
-  std::vector<uint32_t> local((size_t)std::max<int64_t>(m, 1));
-  {
-    int64_t k = 0;
-    for (int32_t g = 0; g < graphs; ++g) {
-      const fl_graph_desc& x = d[g];
-      std::vector<int32_t> cnt((size_t)std::max(x.n, 1), 0);
-      for (int32_t j = 0; j < x.m; ++j) {
-        const int32_t a = x.source[j], c = x.target[j];
-        if (a < 0 || a >= x.n || c < 0 || c >= x.n)
-          return bfail(b, FL_E_ARG, "graph " + std::to_string(g) + " link " + std::to_string(j) + ": node not found");
-        ++cnt[a], ++cnt[c];
-      }
-      for (int32_t j = 0; j < x.m; ++j, ++k) {
-        const int32_t a = x.source[j], c = x.target[j];
-        src[k] = off[g] + a, dst[k] = off[g] + c;
-        local[k] = (uint32_t)j;
-        dist[k] = x.link_distance ? x.link_distance[j] : 30.f;
-        // src/link.js:73-75, :36-38: bias = count(source) / (count(source) + count(target)),
-        // strength = 1 / min(count(source), count(target))
-        bias[k] = x.link_bias ? x.link_bias[j] : (float)((double)cnt[a] / (cnt[a] + cnt[c]));
-        str[k] = x.link_strength ? x.link_strength[j] : (float)(1.0 / std::min(cnt[a], cnt[c]));
-      }
-    }
-  }
-  for (int64_t k = 0; k < m; ++k) ++row[src[k] + 1], ++row[dst[k] + 1];
-  for (int64_t i = 0; i < n; ++i) row[i + 1] += row[i];
-  std::vector<int32_t> cur(row.begin(), row.end() - 1);
-  std::vector<float> entry(4 * (size_t)std::max<int64_t>(2 * m, 1));
-  std::vector<uint32_t> code((size_t)std::max<int64_t>(2 * m, 1));
-  for (int64_t k = 0; k < m; ++k) {
-    const int32_t a = src[k], c = dst[k];
-    int32_t e = cur[a]++;
-    std::memcpy(&entry[4 * (size_t)e], &c, 4);
-    entry[4 * (size_t)e + 1] = dist[k], entry[4 * (size_t)e + 2] = str[k];
-    entry[4 * (size_t)e + 3] = (float)(1.0 - (double)bias[k]);
-    code[e] = 2u * local[k];
-    e = cur[c]++;
-    std::memcpy(&entry[4 * (size_t)e], &a, 4);
-    entry[4 * (size_t)e + 1] = dist[k], entry[4 * (size_t)e + 2] = str[k];
-    entry[4 * (size_t)e + 3] = bias[k];
-    code[e] = 2u * local[k] + 1u;
-  }
-  // device buffers
-  const size_t N = (size_t)std::max<int64_t>(n, 1);
+  b->cur = 0;
+  b->step = 0;
+  b->neg = hp.neg, b->posv = hp.posv, b->smax = hp.smax;
+  b->closed = !(hp.neg && hp.posv);
+  b->sign = hp.neg ? -1.f : 1.f;
+  b->fx_exp = fl_fixed_exponent(n, hp.smax * (ndim == 1 ? 8192.0 : 1.0));
+  b->dmax_any = hp.dmax_any;
+  b->citer_max = hp.citer_max;
+  b->ngroups = (int32_t)hp.groups.size();
+  // device buffers: the batch's state and graphs
+  const size_t N = (size_t)std::max<int64_t>(n, 1), E = (size_t)std::max<int64_t>(2 * m, 1);
   FB_CK(b, b->pos.reserve(16 * N));
   FB_CK(b, b->vel[0].reserve(16 * N));
   FB_CK(b, b->vel[1].reserve(16 * N));
   FB_CK(b, b->fix.reserve(16 * N));
   FB_CK(b, b->mask.reserve(4 * N));
   FB_CK(b, b->gid.reserve(4 * N));
-  FB_CK(b, b->gid_pos.reserve(4 * N));
   FB_CK(b, b->charge.reserve(4 * N));
-  b->hoff = off;
+  if (hp.has_radius) FB_CK(b, b->radius.reserve(4 * N));
+  else b->radius.release();
   FB_CK(b, b->off.reserve(4 * (size_t)(graphs + 1)));
   FB_CK(b, b->prm.reserve(sizeof(FlBatchParams) * (size_t)graphs));
-  FB_CK(b, b->red.reserve(sizeof(FlReduce) * (size_t)graphs));
-  FB_CK(b, b->gr.reserve(sizeof(FlGraph) * (size_t)graphs));
   FB_CK(b, b->row.reserve(4 * ((size_t)n + 1)));
-  FB_CK(b, b->entry.reserve(16 * (size_t)std::max<int64_t>(2 * m, 1)));
-  FB_CK(b, b->code.reserve(4 * (size_t)std::max<int64_t>(2 * m, 1)));
-  FB_CK(b, b->sort1.reserve(fl_sort_bytes(n)));
-  FB_CK(b, b->sort2.reserve(fl_sort_bytes(n)));
-  FB_CK(b, b->tree.reserve(fl_tree_bytes(n)));
-  b->citer_max = citer_max;
-  if (citer_max) {
-    FB_CK(b, b->radius.reserve(4 * N));
-    FB_CK(b, b->grid.reserve(fl_grid_bytes(n)));
-    FB_CK(b, b->sgid.reserve(4 * N));
-    fl_grid_carve(&b->gb, b->grid.p, n);
+  FB_CK(b, b->entry.reserve(16 * E));
+  FB_CK(b, b->code.reserve(4 * E));
+  FB_CK(b, b->groups.reserve(8 * std::max<size_t>(hp.groups.size(), 1)));
+  if ((rc = size_scratch(b))) return rc;
+  const int32_t zero = 0;
+  FB_CK(b, cudaMemcpyAsync(b->row.p, &zero, 4, cudaMemcpyHostToDevice, b->st));
+  FB_CK(b, cudaMemsetAsync(b->vel[1].p, 0, 16 * N, b->st));
+  return upload_part(b, hp, 0, 0, 0, graphs);
+}
+
+int32_t fl_batch_add_graphs(fl_batch* b, int32_t count, const fl_graph_desc* d) {
+  int32_t rc = bcheck(b);
+  if (rc) return rc;
+  if (!b->graphs) return bfail(b, FL_E_STATE, "no graphs set: fl_batch_set_graphs first");
+  if (count < 1 || b->graphs + (int64_t)count > 65535 || !d)
+    return bfail(b, FL_E_ARG, "count must keep the batch at 1..65535 graphs");
+  int64_t n = 0, m = 0;
+  if ((rc = check_descs(b, count, d, &n, &m))) return rc;
+  const int64_t n0 = b->n, m0 = b->m;
+  const int32_t g0 = b->graphs;
+  if (n0 + n > kMaxBatchNodes) return bfail(b, FL_E_ARG, "too many nodes in one batch");
+  if (m0 + m > (int64_t(1) << 30)) return bfail(b, FL_E_ARG, "too many links in one batch");
+  FB_CK(b, cudaStreamSynchronize(b->st));
+  clear_blocks(b);
+  HostPart hp;
+  build_part(b->ndim, count, d, n0, g0, m0, b->step, &hp);
+  const int64_t N1 = std::max<int64_t>(n0 + n, 1), E1 = std::max<int64_t>(2 * (m0 + m), 1);
+  // the kept state grows in place of a rebuild: positions, the current velocities, pins,
+  // graph ids, charges, radii, links, offsets, parameters, walk groups
+  if ((rc = grow(b, b->pos, 16 * N1, 16 * n0))) return rc;
+  if ((rc = grow(b, b->vel[b->cur], 16 * N1, 16 * n0))) return rc;
+  if ((rc = grow(b, b->vel[1 - b->cur], 16 * N1, 0))) return rc;
+  if ((rc = grow(b, b->fix, 16 * N1, 16 * n0))) return rc;
+  if ((rc = grow(b, b->mask, 4 * N1, 4 * n0))) return rc;
+  if ((rc = grow(b, b->gid, 4 * N1, 4 * n0))) return rc;
+  if ((rc = grow(b, b->charge, 4 * N1, 4 * n0))) return rc;
+  if (hp.has_radius || b->radius.p) {
+    const bool had = b->radius.p != nullptr;
+    if ((rc = grow(b, b->radius, 4 * N1, had ? 4 * n0 : 0))) return rc;
+    if (!had && n0) FB_CK(b, cudaMemsetAsync(b->radius.p, 0, 4 * n0, b->st));
   }
-  b->ngroups = (int32_t)groups.size();
-  FB_CK(b, b->groups.reserve(8 * std::max<size_t>(groups.size(), 1)));
-  fl_sort_carve(&b->sb, b->sort1.p, n);
-  fl_sort_carve(&b->sb2, b->sort2.p, n);
-  fl_tree_carve(&b->tb, b->tree.p, n, ndim);
-  // uploads on the batch's own stream (from pageable memory: staged before each call returns)
-  cudaStream_t st = b->st;
-  FB_CK(b, cudaMemcpyAsync(b->pos.p, pos.data(), 16 * N, cudaMemcpyHostToDevice, st));
-  FB_CK(b, cudaMemcpyAsync(b->vel[0].p, vel.data(), 16 * N, cudaMemcpyHostToDevice, st));
-  FB_CK(b, cudaMemsetAsync(b->vel[1].p, 0, 16 * N, st));
-  FB_CK(b, cudaMemsetAsync(b->fix.p, 0, 16 * N, st));
-  FB_CK(b, cudaMemsetAsync(b->mask.p, 0, 4 * N, st));
-  FB_CK(b, cudaMemcpyAsync(b->gid.p, gid.data(), 4 * N, cudaMemcpyHostToDevice, st));
-  FB_CK(b, cudaMemcpyAsync(b->charge.p, charge.data(), 4 * N, cudaMemcpyHostToDevice, st));
-  if (citer_max)
-    FB_CK(b, cudaMemcpyAsync(b->radius.p, radius.data(), 4 * N, cudaMemcpyHostToDevice, st));
-  FB_CK(b, cudaMemcpyAsync(b->off.p, off.data(), 4 * (size_t)(graphs + 1), cudaMemcpyHostToDevice, st));
-  FB_CK(b, cudaMemcpyAsync(b->prm.p, prm.data(), sizeof(FlBatchParams) * (size_t)graphs,
-                           cudaMemcpyHostToDevice, st));
-  FB_CK(b, cudaMemcpyAsync(b->row.p, row.data(), 4 * ((size_t)n + 1), cudaMemcpyHostToDevice, st));
-  if (!groups.empty())
-    FB_CK(b, cudaMemcpyAsync(b->groups.p, groups.data(), 8 * groups.size(), cudaMemcpyHostToDevice, st));
-  if (m) {
-    FB_CK(b, cudaMemcpyAsync(b->entry.p, entry.data(), 32 * (size_t)m, cudaMemcpyHostToDevice, st));
-    FB_CK(b, cudaMemcpyAsync(b->code.p, code.data(), 8 * (size_t)m, cudaMemcpyHostToDevice, st));
-  }
-  // the host vectors go out of scope at return: wait for the copies that read them
-  FB_CK(b, cudaStreamSynchronize(st));
-  b->cur = 0;
-  b->step = 0;
-  return FL_OK;
+  if ((rc = grow(b, b->off, 4 * (size_t)(g0 + count + 1), 4 * (size_t)(g0 + 1)))) return rc;
+  if ((rc = grow(b, b->prm, sizeof(FlBatchParams) * (size_t)(g0 + count), sizeof(FlBatchParams) * (size_t)g0))) return rc;
+  if ((rc = grow(b, b->row, 4 * (size_t)(N1 + 1), 4 * (size_t)(n0 + 1)))) return rc;
+  if ((rc = grow(b, b->entry, 16 * (size_t)E1, 32 * (size_t)m0))) return rc;
+  if ((rc = grow(b, b->code, 4 * (size_t)E1, 8 * (size_t)m0))) return rc;
+  const size_t ng1 = (size_t)b->ngroups + hp.groups.size();
+  if ((rc = grow(b, b->groups, 8 * std::max<size_t>(ng1, 1), 8 * (size_t)b->ngroups))) return rc;
+  b->graphs = g0 + count, b->n = (int32_t)(n0 + n), b->m = (int32_t)(m0 + m);
+  b->ngroups = (int32_t)ng1;
+  b->neg = b->neg || hp.neg, b->posv = b->posv || hp.posv, b->smax = std::max(b->smax, hp.smax);
+  b->closed = !(b->neg && b->posv);
+  b->sign = b->neg ? -1.f : 1.f;
+  b->fx_exp = fl_fixed_exponent(b->n, b->smax * (b->ndim == 1 ? 8192.0 : 1.0));
+  if (hp.dmax_any < 3e38) b->dmax_any = 1.0;
+  b->citer_max = std::max(b->citer_max, hp.citer_max);
+  if ((rc = size_scratch(b))) return rc;
+  return upload_part(b, hp, n0, g0, m0, count);
 }
 
 int32_t fl_batch_set_seed(fl_batch* b, uint32_t seed) {

@@ -29,7 +29,8 @@ EXPORTS = ["fl_create", "fl_destroy", "fl_last_error", "fl_fits", "fl_set_nodes"
            "fl_batch_destroy", "fl_batch_last_error", "fl_batch_set_graphs", "fl_batch_set_seed",
            "fl_batch_enqueue", "fl_batch_sync", "fl_batch_query", "fl_batch_stream",
            "fl_autotune", "fl_batch_set_tuning", "fl_batch_autotune", "fl_batch_read",
-           "fl_update_positions_packed", "fl_sync_packed", "fl_upload_all", "fl_debug_links"]
+           "fl_update_positions_packed", "fl_sync_packed", "fl_upload_all", "fl_debug_links",
+           "fl_batch_add_graphs"]
 SORT_NOALLOC_MAX_PAIRS = 262144  # FL_SORT_NOALLOC_MAX_PAIRS
 TUNE_WALK_GROUP, TUNE_CELL_SUMS, TUNE_GRAPHS = 1, 2, 3
 TUNE_SORT_PASSES, TUNE_WALK_BLOCKS, TUNE_COLLIDE_CELL, TUNE_TEST_LOOKBACK = 4, 5, 6, 7
@@ -136,6 +137,7 @@ def load():
         "fl_batch_destroy": (I32, [P]),
         "fl_batch_last_error": (ctypes.c_char_p, [P]),
         "fl_batch_set_graphs": (I32, [P, I32, I32, ctypes.POINTER(GraphDesc)]),
+        "fl_batch_add_graphs": (I32, [P, I32, ctypes.POINTER(GraphDesc)]),
         "fl_batch_set_seed": (I32, [P, U32]),
         "fl_batch_enqueue": (I32, [P, P, I32]),
         "fl_batch_sync": (I32, [P, P, P]),

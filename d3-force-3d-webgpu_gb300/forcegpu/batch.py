@@ -83,11 +83,9 @@ class Batch:
         except Exception:
             pass
 
-    def set_graphs(self, specs, ndim=3, seed=None):
-        self.specs = list(specs)
-        self.ndim = int(ndim)
-        descs = (GraphDesc * max(1, len(self.specs)))()
-        for i, s in enumerate(self.specs):
+    def _descs(self, specs):
+        descs = (GraphDesc * max(1, len(specs)))()
+        for i, s in enumerate(specs):
             xyz = np.asarray(s.xyz, dtype=np.float64).reshape(-1, self.ndim)
             n = len(xyz)
             pos4 = np.zeros((n, 4), np.float32)
@@ -126,11 +124,30 @@ class Batch:
                 d.collide_strength = float(s.collide_strength)
                 d.collide_iterations = int(s.collide_iterations)
             s._keep = keep
+        return descs
+
+    def set_graphs(self, specs, ndim=3, seed=None):
+        self.specs = list(specs)
+        self.ndim = int(ndim)
+        descs = self._descs(self.specs)
         self._check(self.L.fl_batch_set_graphs(self.h, self.ndim, len(self.specs), descs))
         if seed is not None:
             self._check(self.L.fl_batch_set_seed(self.h, int(seed) & 0xffffffff))
         self.sizes = np.array([len(np.asarray(s.xyz).reshape(-1, self.ndim)) for s in self.specs], np.int64)
         self.alphas = np.array([s.alpha for s in self.specs], dtype=np.float64)
+
+    def add_graphs(self, specs):
+        """Append graphs to the running batch (fl_batch_add_graphs): the present graphs and their
+        state stay as they are; each new graph's alpha starts from its spec."""
+        specs = list(specs)
+        if not specs:
+            return
+        descs = self._descs(specs)
+        self._check(self.L.fl_batch_add_graphs(self.h, len(specs), descs))
+        self.specs += specs
+        self.sizes = np.concatenate([self.sizes, [len(np.asarray(s.xyz).reshape(-1, self.ndim))
+                                                  for s in specs]]).astype(np.int64)
+        self.alphas = np.concatenate([self.alphas, [s.alpha for s in specs]])
 
     def alpha_schedule(self, ticks):
         """The next `ticks` alphas of every graph, (ticks, graphs), advancing each graph's alpha

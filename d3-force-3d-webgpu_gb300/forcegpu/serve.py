@@ -89,26 +89,32 @@ class Job:
 
 
 class _Lane:
-    """The batch of one dimensionality. Jobs join at block boundaries (the batch is rebuilt from
-    the running jobs' current state plus the new ones). A job that finishes stays in the batch,
-    sitting every tick out, until the finished jobs hold `dead_share` of the batch's nodes or
-    another job joins: a rebuild reads every running job's state back, so it is not done for
-    each job that ends. Only a finished job's own nodes are read back when it ends."""
+    """The batch of one dimensionality. Jobs join at block boundaries, appended to the running
+    batch (fl_batch_add_graphs: the running jobs' state stays on the device). A job that
+    finishes stays in the batch, sitting every tick out, until the finished jobs hold
+    `dead_share` of the batch's nodes: then the batch is rebuilt from the running jobs' current
+    state (read back) plus the new ones. Only a finished job's own nodes are read back when it
+    ends.
 
-    def __init__(self, ndim, device, dead_share=0.3):
+    Blocks are pipelined: a job's alphas are known in advance, so the block after a block is
+    queued before the first one has run (up to `depth` blocks in flight), and the host waits for
+    the GPU only to read a finished job back or to change the batch."""
+
+    def __init__(self, ndim, device, dead_share=0.5, depth=2):
         self.ndim = ndim
         self.batch = Batch(device)
         self.jobs = []       # in the batch, in its order (finished ones included until a rebuild)
         self.incoming = []   # admitted, waiting for the next block boundary
         self.dead = 0        # nodes of finished jobs still in the batch
         self.dead_share = dead_share
-        self.pending = None  # alphas of the block in flight
+        self.depth = depth
+        self.pending = deque()  # per block in flight: the (graph, job) pairs that end in it
 
     def live(self):
         return [j for j in self.jobs if j.done_ticks < j.ticks]
 
     def busy(self):
-        return bool(self.incoming) or any(j.done_ticks < j.ticks for j in self.jobs)
+        return bool(self.incoming or self.pending) or any(j.done_ticks < j.ticks for j in self.jobs)
 
     def spec(self, j):
         return GraphSpec(xyz=j.pos[:, :self.ndim], source=j.source, target=j.target,
@@ -130,23 +136,25 @@ class _Lane:
         if self.jobs:
             self.batch.set_graphs([self.spec(j) for j in self.jobs], ndim=self.ndim, seed=seed)
 
-    def launch(self, block, seed):
-        total = sum(j.n for j in self.jobs)
-        if self.incoming or (self.jobs and self.dead > self.dead_share * total):
-            self._rebuild(seed)
-        if not any(j.done_ticks < j.ticks for j in self.jobs):
-            return
-        al = np.stack([j.next_alphas(block) for j in self.jobs], axis=1)
-        self.batch.enqueue(al)
-        self.pending = al
-
-    def land(self, now):
-        """Wait for the block, update the jobs; returns the ones that finished in it."""
-        if self.pending is None:
-            return []
+    def launch(self, block, seed, now):
+        """Queue the next block (changing the batch first if jobs join or the finished ones are
+        many); returns the jobs whose results were read back on the way."""
         done = []
+        total = sum(j.n for j in self.jobs)
+        compact = self.jobs and self.dead > self.dead_share * total
+        if compact or self.incoming:
+            done = self.land(now, drain=True)  # every result out before the batch changes
+            if compact or not self.live():
+                self._rebuild(seed)  # compact, or start afresh
+            else:  # join the running batch
+                self.batch.add_graphs([self.spec(j) for j in self.incoming])
+                self.jobs += self.incoming
+                self.incoming = []
+        if len(self.pending) >= self.depth or not any(j.done_ticks < j.ticks for j in self.jobs):
+            return done
+        al = np.stack([j.next_alphas(block) for j in self.jobs], axis=1)
         ended = []
-        for g, (j, col) in enumerate(zip(self.jobs, self.pending.T)):
+        for g, (j, col) in enumerate(zip(self.jobs, al.T)):  # the jobs' schedules move on now
             ran = int((col >= 0).sum())
             if not ran:
                 continue
@@ -154,7 +162,20 @@ class _Lane:
             j.done_ticks += ran
             if j.done_ticks >= j.ticks:
                 ended.append((g, j))
-        if ended:
+        self.batch.enqueue(al)
+        self.pending.append(ended)
+        return done
+
+    def land(self, now, drain=False):
+        """Read back the jobs that ended in the oldest blocks in flight (waiting for them), as
+        many blocks as hold a finished job or exceed the pipeline's depth (all with drain);
+        returns those jobs. A finished job sits later blocks out, so its state is still its
+        result when read after them."""
+        done = []
+        while self.pending and (drain or self.pending[0] or len(self.pending) >= self.depth):
+            ended = self.pending.popleft()
+            if not ended:
+                self.batch.wait()
             for g, j in ended:
                 p, _ = self.batch.read(g, 1)
                 j.result = p[:, :self.ndim].copy()
@@ -162,9 +183,6 @@ class _Lane:
                 j.pos = j.vel = None
                 self.dead += j.n
                 done.append(j)
-        else:
-            self.batch.wait()
-        self.pending = None
         return done
 
 
@@ -281,8 +299,9 @@ class LayoutServer:
                 eng.enqueue(al, 1 - j.velocity_decay)
                 j.alpha = float(al[-1])
                 j.done_ticks += k
+        landed = []
         for lane in self.lanes.values():
-            lane.launch(self.block, self.seed)
+            landed += lane.launch(self.block, self.seed, self.now)
         done = []
         still = []
         for j, eng, descs in self.plain:
@@ -295,6 +314,7 @@ class LayoutServer:
             j.finished = self.now()
             done.append(j)
         self.plain = still
+        done += landed
         for lane in self.lanes.values():
             done += lane.land(self.now)
         for j in done:

@@ -267,6 +267,12 @@ int32_t fl_batch_destroy(fl_batch* b);
 const char* fl_batch_last_error(const fl_batch* b);
 /* Replace the batch's graphs (copied; the state starts from pos4 / vel4). */
 int32_t fl_batch_set_graphs(fl_batch* b, int32_t ndim, int32_t graphs, const fl_graph_desc* descs);
+/* Append graphs to the batch, keeping every graph it holds and their state (continuous
+ * batching: a layout job joins a batch that is running without a readback of the others). The
+ * appended graphs are numbered after the present ones; their descriptors are as
+ * fl_batch_set_graphs's, in the batch's dimensionality, and a graph's tick0 is its own tick
+ * count. No counterpart in the reference. */
+int32_t fl_batch_add_graphs(fl_batch* b, int32_t count, const fl_graph_desc* descs);
 int32_t fl_batch_set_seed(fl_batch* b, uint32_t seed);
 /* Queue `ticks` ticks without waiting; alphas[k * graphs + g] is graph g's alpha at tick k. A
  * negative alpha makes graph g sit tick k out: its positions and velocities do not change (a

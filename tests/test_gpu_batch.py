@@ -145,3 +145,28 @@ def test_the_batch_counts_its_launches_per_tick_independent_of_graphs():
     many.run(2)
     one.sync(), many.sync()
     assert one.launches() == many.launches(), "one launch per kernel per tick, whatever the batch"
+
+
+def test_graphs_added_to_a_running_batch_match_them_alone():
+    """fl_batch_add_graphs: a graph appended to a batch that has run for a while (without a
+    readback of the others) lays out as it would alone, and the graphs already there go on as
+    if nothing joined, bit for bit."""
+    a, b_, c = spec(700, 3, 61), spec(90, 3, 62), spec(500, 3, 63)
+    c.xyz = c.xyz * 0.3
+    c.xyz[5] = c.xyz[9]  # coincident: jiggles in the walk and the collide
+    c.radii = 1.0 + np.arange(500) % 3
+    mix = Batch()
+    mix.set_graphs([a, b_], ndim=3, seed=4)
+    mix.run(7)
+    mix.add_graphs([c])
+    mix.run(9)
+    got = mix.positions()
+    alone_a = Batch()
+    alone_a.set_graphs([a], ndim=3, seed=4)
+    alone_a.run(16)
+    alone_c = Batch()
+    alone_c.set_graphs([c], ndim=3, seed=4)
+    alone_c.run(9)
+    assert np.isfinite(got[2]).all()
+    assert np.array_equal(got[0], alone_a.positions()[0])
+    assert np.array_equal(got[2], alone_c.positions()[0])
