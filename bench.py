@@ -66,7 +66,7 @@ WALK_BYTES_PER_NODE = 16 + 4 + 48 + 32
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one walk launch of the default
 # 1M-node workload, from an ncu capture of that launch: a profiler figure, not something this
 # run can measure, so it is reported at that size only, with where it came from
-WALK_DRAM_BYTES_1M = 73.5e6
+WALK_DRAM_BYTES_1M = 74.4e6
 WALK_DRAM_SOURCE = "ncu --set full capture of one k_walk launch, 1M-node workload"
 FLOPS_PER_INTERACTION = 20  # FP32 ops per accepted cell or point interaction
 FLOPS_PER_OPEN = 8          # per opened-cell test
@@ -87,8 +87,8 @@ def parse():
                    help="ticks queued per enqueue call (a block seen twice runs as a CUDA graph)")
     p.add_argument("--no-autotune", action="store_true",
                    help="keep the default tuning (else fl_autotune picks it before the warm-up)")
-    p.add_argument("--walk-group", type=int, default=32, choices=[16, 32],
-                   help="points per tree-walk traversal (FL_TUNE_WALK_GROUP)")
+    p.add_argument("--walk-group", type=int, default=0, choices=[0, 1, 16, 32],
+                   help="points per tree-walk traversal (FL_TUNE_WALK_GROUP; 0 = by size)")
     p.add_argument("--precision", action="store_true",
                    help="print the many-body force accuracy report instead of the timing line")
     p.add_argument("--precision-ticks", type=int, default=100)

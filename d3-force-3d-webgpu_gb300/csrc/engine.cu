@@ -119,7 +119,7 @@ struct fl_sim {
   std::vector<std::unique_ptr<Pass>> plan;
   uint32_t seed = 0, step = 0;
   int64_t ticks = 0, launches = 0;
-  int walk_group = 32;  // points per tree-walk traversal (tuning: 16 or 32)
+  int walk_group = 0;  // points per tree-walk traversal (tuning: 1, 16 or 32; 0 = by size)
   // per-tick values in device memory and the CUDA graphs of tick blocks (fl_enqueue)
   const FlTick* tkp = nullptr;  // the tick being encoded (null: parameters)
   DevMem tickbuf;
@@ -1047,7 +1047,8 @@ int32_t fl_set_tuning(fl_sim* s, int32_t key, int32_t value) {
   clear_blocks(s);
   switch (key) {
     case FL_TUNE_WALK_GROUP:
-      if (value != 16 && value != 32) return fail(s, FL_E_ARG, "walk group must be 16 or 32");
+      if (value != 0 && value != 1 && value != 16 && value != 32)
+        return fail(s, FL_E_ARG, "walk group must be 0, 1, 16 or 32");
       s->walk_group = value;
       return FL_OK;
     case FL_TUNE_CELL_SUMS:
@@ -1107,7 +1108,11 @@ int32_t fl_autotune(fl_sim* s, int32_t ticks, double alpha, double decay,
       if (std::find(seen.begin(), seen.end(), lo) == seen.end()) seen.push_back(lo), passes.push_back(c);
     }
     knobs.push_back({FL_TUNE_SORT_PASSES, "sort_passes", passes, 0});
-    knobs.push_back({FL_TUNE_WALK_GROUP, "walk_group", {32, 16}, 32});
+    // the default by size first, then the other groups
+    std::vector<int> groups{0};
+    for (int g : {32, 16, 1})
+      if (g != fl_walk_group_for(n)) groups.push_back(g);
+    knobs.push_back({FL_TUNE_WALK_GROUP, "walk_group", groups, 0});
     knobs.push_back({FL_TUNE_WALK_BLOCKS, "walk_blocks", {0, 8, 6, 4}, 0});
   }
   if (grid) knobs.push_back({FL_TUNE_COLLIDE_CELL, "collide_cell", {100, 150, 200}, 100});

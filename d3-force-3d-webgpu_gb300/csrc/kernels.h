@@ -235,13 +235,17 @@ void fl_launch_aggregate(const FlTreeBufs* t, const uint64_t* skeys, bool closed
 int fl_fixed_exponent(int64_t n, double wmax);
 // stats (optional): [0] child tests made by the warps (32 per child), [1] of those, tests by a
 // lane whose point needed them (the d3 traversal's own work)
-// group: points per traversal (16 or 32)
+// group: points per traversal (16 or 32), 1 for one point per warp with the lanes over the
+// point's children (small layouts), 0 for the default by size (fl_walk_group_for)
 // A batch (segs.graphs > 0): cube, alpha, theta2 and dmin2 are per graph (segs.g); dmax2 is
 // only tested when finite (pass the largest of the graphs').
 void fl_launch_walk(const FlTreeBufs* t, const uint32_t* perm, const float* cube, float4* vel,
                     float alpha, double theta2, double dmin2, double dmax2, uint32_t step,
                     uint32_t seed, uint32_t* err, unsigned long long* stats, int group,
                     cudaStream_t st, FlSegs segs = FlSegs{}, const FlTick* tk = nullptr);
+// The walk group a layout of n points gets by default: 1 (one point per warp) up to a size at
+// which groups of 32 points fill the device, else 32.
+int fl_walk_group_for(int n);
 // Exact all-pairs sum (theta ~ 0): O(n^2), tiled through shared memory.
 void fl_launch_allpairs(const float4* pos, const float* strength, float4* vel, int n, int ndim,
                         float alpha, float dmin2, float dmax2, uint32_t step, uint32_t seed,

@@ -834,6 +834,8 @@ constexpr int kStack = 96;  // entries per group in shared memory; deeper entrie
 __host__ __device__ constexpr int kWalkStackLayers(int ndim) { return (ndim == 3 ? 21 : 24) + 1; }
 constexpr int kWalkSpillPerWarp = 704;  // max over dims and group sizes of NG ((levels+1) G - kStack)
 constexpr int kWalkBlocksPerSm = 10;    // blocks of the persistent walk grid per SM
+// the largest layout whose walk runs one point per warp by default (FL_TUNE_WALK_GROUP 0)
+constexpr int kLaneWalkMaxNodes = 32768;
 
 // Packed FP32 pairs (the f32x2 arithmetic of sm_100 and later): two children per instruction.
 __device__ __forceinline__ uint64_t pk2(float a, float b) {
@@ -1196,6 +1198,181 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
   }
 }
 
+// The walk of one point per warp, for small layouts: where the union walk above has too few
+// groups of 32 points to fill the device (a 1,000-node layout is 32 warps, each a long serial
+// chain of rounds), each warp walks one point's own d3 traversal and its lanes test up to 32
+// children of it at once. The children are gathered from the top of the point's stack as in the
+// union walk; a lane tests its child against the point, applies it, takes the uncommon case or
+// pushes the child's children. Each lane sums what it applied, and the warp adds the lanes'
+// sums in a fixed shuffle tree, so a layout is the same run after run. The stack holds the
+// bound on its depth in shared memory, 8 bytes an entry (first child slot; count | top depth
+// << 26), so nothing spills and the grid is not limited by spill regions.
+// stats (STATS): [0] children tested, [1] of those, the ones the point's d3 traversal needs
+// (not a zero value, not the point itself; the union walk's [1], [3] and [4] count the same
+// (point, child) pairs), [2] deepest stack, [3] cells opened, [4] cells or points applied,
+// [5] rounds in which a lane took the uncommon case.
+template <int NDIM, bool STATS, bool DMAX>
+__global__ void __launch_bounds__(kWalkThreads) k_walk_lanes(
+    const float4* __restrict__ cdata, const uint2* __restrict__ cmeta,
+    const float4* __restrict__ leaf, const uint32_t* __restrict__ perm,
+    const float* __restrict__ cube, float4* __restrict__ vel, int n, float alpha,
+    double theta2, float dmin2, float dmax2, uint32_t step, uint32_t seed, uint32_t* err,
+    unsigned long long* stats, uint32_t* work, const FlTick* __restrict__ tk) {
+  if (tk) alpha = tk->alpha, step = tk->step, seed = tk->seed;
+  // at most 32 children per round and one push per child: the union walk's bound with G = 32
+  constexpr int kAll = kWalkStackLayers(NDIM) * 32;
+  __shared__ uint2 s_stack[kWalkWarps][kAll];
+  __shared__ uint32_t s_own[kWalkWarps][32];
+  __shared__ float s_T0;
+  if (threadIdx.x == 0) s_T0 = (float)((double)cube[3] * (double)cube[3] / theta2);
+  __syncthreads();
+  const float T0 = s_T0;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t below_me = (1u << lane) - 1u;
+  const float dmin_le = below(dmin2);
+  const uint32_t slot_cap = 2u * (uint32_t)n + 1u;
+  unsigned long long st_tests = 0, st_useful = 0, st_open = 0, st_apply = 0, st_rare = 0;
+  int maxsp = 0;
+  uint2* stk = s_stack[warp];
+  uint32_t* sown = s_own[warp];
+  int t = lane == 0 ? (int)atomicAdd(work, 1u) : 0;
+  t = __shfl_sync(FL_FULL, t, 0);
+  while (t < n) {
+    const float4 me = leaf[t];  // the same address in every lane: one load
+    const uint32_t myid = perm[t];
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    if (lane == 0) stk[0] = make_uint2(0u, 1u);  // the root: slot 0, one child, top depth 0
+    int sp = 1;
+    uint32_t guard = 0;
+    const uint32_t guard_max = 4u * (uint32_t)n + 64u;
+    __syncwarp();
+    while (sp > 0) {
+      // lane i reads the i-th entry from the top; a prefix sum of the entries' child counts
+      // places each entry's children in the round, and lane j finds the entry of child j
+      const bool has = lane < sp;
+      const uint2 se = has ? stk[sp - 1 - lane] : make_uint2(0u, 0u);
+      uint4 e = make_uint4(se.x, se.y & kCountMask, se.y >> 26, 0u);
+      if (has && (e.x >= slot_cap || e.y > slot_cap - e.x)) {  // a malformed tree: never read past it
+        atomicOr(err, FL_ERR_TREE);
+        e.y = e.x >= slot_cap ? 0u : slot_cap - e.x;
+      }
+      uint32_t inc = e.y;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(FL_FULL, inc, o);
+        if (lane >= o) inc += u;
+      }
+      const uint32_t exc = inc - e.y;
+      const uint32_t avail = __shfl_sync(FL_FULL, inc, 31);
+      const uint32_t total = avail < 32u ? avail : 32u;
+      // entries taken whole leave the stack; one taken in part keeps the rest (the new top)
+      const uint32_t taken = __ballot_sync(FL_FULL, has && inc <= total);
+      if (has && exc < total && inc > total)
+        stk[sp - 1 - lane] = make_uint2(e.x + (total - exc), (inc - total) | e.z << 26);
+      sp -= __popc(taken);
+      sown[lane] = 0u;
+      __syncwarp();
+      if (e.y && exc < total) sown[exc] = (uint32_t)lane;
+      __syncwarp();
+      uint32_t own = sown[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(FL_FULL, own, o);
+        if (lane >= o && u > own) own = u;
+      }
+      const uint32_t own_first = __shfl_sync(FL_FULL, e.x, (int)own);
+      const uint32_t own_exc = __shfl_sync(FL_FULL, exc, (int)own);
+      const uint32_t my_top = __shfl_sync(FL_FULL, e.z, (int)own);
+      __syncwarp();
+      bool o = false, a = false, rare = false, need = false;
+      uint2 m = make_uint2(0u, 0u);
+      uint32_t D = 0;
+      if ((uint32_t)lane < total) {
+        const uint32_t slot = own_first + ((uint32_t)lane - own_exc);
+        const float4 q = __ldg(cdata + slot);
+        m = __ldg(cmeta + slot);
+        const bool lf = m.y == kLeafMark;
+        D = (m.y >> 26) & 31u;
+        // d3 skips a zero value and all it holds, and the point itself
+        const bool mask = q.w != 0.f && !(lf && m.x == (uint32_t)t);
+        need = mask;
+        const bool chain = !lf && my_top < D;
+        const float topen = lf ? -INFINITY : T0 * pow4neg(D);
+        const float ttop = chain ? T0 * pow4neg(my_top) : topen;
+        float va = chain ? q.w * alpha * damp(NDIM, (int)(D - my_top)) : q.w * alpha;
+        float dx = q.x - me.x;
+        float dy = NDIM > 1 ? q.y - me.y : 0.f;
+        float dz = NDIM > 2 ? q.z - me.z : 0.f;
+        float l = dx * dx;
+        if (NDIM > 1) l = fmaf(dy, dy, l);
+        if (NDIM > 2) l = fmaf(dz, dz, l);
+        const float zp = NDIM == 3 ? (dx * dy) * dz : NDIM == 2 ? dx * dy : dx;
+        o = mask && topen >= l;
+        a = mask && !o && (!DMAX || l < dmax2);
+        rare = a && (l <= fmaxf(ttop, dmin_le) || zp == 0.f);
+        if (rare)
+          rare_case<NDIM>(m.y, my_top, m.x, T0, dmin2, myid, 0u, (uint32_t)n, 0u, perm, n, step,
+                          seed, va, dx, dy, dz, l);
+        if (a) {
+          const float w = va * rcp_approx(l);
+          ax = fmaf(dx, w, ax);
+          if (NDIM > 1) ay = fmaf(dy, w, ay);
+          if (NDIM > 2) az = fmaf(dz, w, az);
+        }
+      }
+      // the children to open go on the stack in child order, the last on top
+      const uint32_t opened = __ballot_sync(FL_FULL, o);
+      if (o) {
+        const int at = sp + __popc(opened & below_me);
+        if (at < kAll) stk[at] = make_uint2(m.x, (m.y & kCountMask) | (D + 1u) << 26);
+      }
+      sp += __popc(opened);
+      if (sp > kAll) {  // beyond the bound on the stack's depth: a malformed tree
+        if (lane == 0) atomicOr(err, FL_ERR_STACK);
+        sp = kAll;
+      }
+      if (STATS) {
+        const uint32_t ap = __ballot_sync(FL_FULL, a), nd = __ballot_sync(FL_FULL, need);
+        const bool rr = __any_sync(FL_FULL, rare);
+        if (lane == 0) {
+          st_tests += total, st_useful += __popc(nd), st_open += __popc(opened);
+          st_apply += __popc(ap), st_rare += rr;
+          if (sp > maxsp) maxsp = sp;
+        }
+      }
+      __syncwarp();
+      if (++guard > guard_max) {
+        if (lane == 0) atomicOr(err, FL_ERR_STACK);
+        break;
+      }
+    }
+#pragma unroll
+    for (int k = 16; k > 0; k >>= 1) {
+      ax += __shfl_xor_sync(FL_FULL, ax, k);
+      if (NDIM > 1) ay += __shfl_xor_sync(FL_FULL, ay, k);
+      if (NDIM > 2) az += __shfl_xor_sync(FL_FULL, az, k);
+    }
+    if (lane == 0) {
+      float4 v = vel[myid];
+      v.x += ax;
+      if (NDIM > 1) v.y += ay;
+      if (NDIM > 2) v.z += az;
+      vel[myid] = v;
+    }
+    __syncwarp();
+    t = lane == 0 ? (int)atomicAdd(work, 1u) : 0;
+    t = __shfl_sync(FL_FULL, t, 0);
+  }
+  if (STATS && lane == 0) {
+    atomicAdd(stats, st_tests);
+    atomicAdd(stats + 1, st_useful);
+    atomicMax(stats + 2, (unsigned long long)maxsp);
+    atomicAdd(stats + 3, st_open);
+    atomicAdd(stats + 4, st_apply);
+    atomicAdd(stats + 5, st_rare);
+  }
+}
+
 // Exact all-pairs sum (theta ~ 0; src/gpu/passes/manyBody.js:5-16 semantics): each block
 // streams the points through shared memory in tiles.
 constexpr int kPairThreads = 256;
@@ -1442,6 +1619,25 @@ int walk_blocks_per_sm() {
   return c;
 }
 
+template <int NDIM, bool STATS, bool DMAX>
+int walk_lanes_blocks_per_sm() {
+  static std::atomic<int> blocks{0};
+  int c = blocks.load(std::memory_order_relaxed);
+  if (!c) {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_walk_lanes<NDIM, STATS, DMAX>,
+                                                      kWalkThreads, 0) != cudaSuccess || b < 1) {
+      cudaGetLastError();
+      b = 1;
+    }
+    c = b < kWalkBlocksPerSm ? b : kWalkBlocksPerSm;
+    blocks.store(c, std::memory_order_relaxed);
+  }
+  return c;
+}
+
+int fl_walk_group_for(int n) { return n <= kLaneWalkMaxNodes ? 1 : 32; }
+
 void fl_launch_walk(const FlTreeBufs* t, const uint32_t* perm, const float* cube, float4* vel,
                     float alpha, double theta2, double dmin2, double dmax2, uint32_t step,
                     uint32_t seed, uint32_t* err, unsigned long long* stats, int group,
@@ -1476,7 +1672,33 @@ void fl_launch_walk(const FlTreeBufs* t, const uint32_t* perm, const float* cube
     if (fmax2 < INFINITY) FL_WALK_ONE(D, 32, false, true, true);                               \
     else FL_WALK_ONE(D, 32, false, false, true);                                               \
   } while (0)
-  if (segs.graphs) {
+  if (!segs.graphs && group == 0) group = fl_walk_group_for(n);
+  if (!segs.graphs && group == 1) {
+    // one point per warp: no more blocks than the points need (the stacks are in shared
+    // memory, so the grid needs no spill regions)
+#define FL_LANES_ONE(D, S, M)                                                                  \
+  do {                                                                                         \
+    int per = walk_lanes_blocks_per_sm<D, S, M>();                                             \
+    if (t->walk_blocks > 0 && t->walk_blocks < per) per = t->walk_blocks;                      \
+    int g = t->sms * per;                                                                      \
+    if (g > (n + kWalkWarps - 1) / kWalkWarps) g = (n + kWalkWarps - 1) / kWalkWarps;          \
+    if (g < 1) g = 1;                                                                          \
+    k_walk_lanes<D, S, M><<<g, kWalkThreads, 0, st>>>(                                         \
+        t->child_data, t->child_meta, t->leaf, perm, cube, vel, n, alpha, theta2,              \
+        (float)dmin2, fmax2, step, seed, err, stats, t->work, tk);                             \
+  } while (0)
+#define FL_LANES(D)                                                                            \
+  do {                                                                                         \
+    if (stats) FL_LANES_ONE(D, true, true);                                                    \
+    else if (fmax2 < INFINITY) FL_LANES_ONE(D, false, true);                                   \
+    else FL_LANES_ONE(D, false, false);                                                        \
+  } while (0)
+    if (t->ndim == 3) FL_LANES(3);
+    else if (t->ndim == 2) FL_LANES(2);
+    else FL_LANES(1);
+#undef FL_LANES
+#undef FL_LANES_ONE
+  } else if (segs.graphs) {
     if (t->ndim == 3) FL_WALK_BATCH(3);
     else if (t->ndim == 2) FL_WALK_BATCH(2);
     else FL_WALK_BATCH(1);

@@ -160,7 +160,8 @@ int32_t fl_buffers(fl_sim* sim, fl_buffer_info* out);
 
 /* Tuning parameters (no reference counterpart; the reference's closest are its fixed
  * constants, e.g. src/gpu/passes/barnesHut.js:49-58): FL_TUNE_WALK_GROUP, points that share one
- * tree-walk traversal, 16 or 32 (default); FL_TUNE_CELL_SUMS, how the many-body cells' values
+ * tree-walk traversal, 16 or 32, or 1 for one point per warp with the warp's lanes testing up to
+ * 32 of its children at once (0, the default: 1 up to 32,768 nodes, else 32); FL_TUNE_CELL_SUMS, how the many-body cells' values
  * and centroids are summed: FL_CELLS_AUTO (default: exact fixed-point prefix sums when the
  * strengths share one sign, else the bottom-up recursion with FP64 sums near the root),
  * FL_CELLS_FP64_TOP (always that recursion) or FL_CELLS_FP32 (the recursion all in FP32, for

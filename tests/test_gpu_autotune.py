@@ -55,7 +55,7 @@ def test_autotune_keeps_the_state_and_the_layout(dims, collide, tmp_path):
     after_p, after_v = e.sync()
     assert np.array_equal(after_p, before_p) and np.array_equal(after_v, before_v)
     assert e.query(Q_TICKS) == ticks
-    assert got["walk_group"] in (16, 32) and 0 <= got["sort_passes"] <= 8
+    assert got["walk_group"] in (0, 1, 16, 32) and 0 <= got["sort_passes"] <= 8
     assert got["walk_blocks"] in (0, 8, 6, 4) and got["collide_cell"] in (100, 150, 200)
     assert got["candidates"] >= 2 and got["from_cache"] == 0
     assert 0 < got["ms_per_tick"] <= got["ms_default"] * 1.0001
@@ -85,6 +85,7 @@ def test_autotune_reads_its_cache(tmp_path):
 
 @pytest.mark.parametrize("key,value", [(TUNE_SORT_PASSES, 3), (TUNE_SORT_PASSES, 8),
                                        (TUNE_WALK_BLOCKS, 4), (TUNE_WALK_GROUP, 16),
+                                       (TUNE_WALK_GROUP, 32), (TUNE_WALK_GROUP, 1),
                                        (TUNE_COLLIDE_CELL, 200)])
 def test_each_knob_value_lays_out_the_same(key, value):
     n = 12000

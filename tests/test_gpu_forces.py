@@ -140,7 +140,7 @@ def _walk_group(group):
     return lambda sim, _: sim._engine.eng.set_tuning(TUNE_WALK_GROUP, group)
 
 
-@pytest.mark.parametrize("group", [32, 16])
+@pytest.mark.parametrize("group", [32, 16, 1])
 def test_tree_walk_groups_distances_theta(group):
     r = run_both(3, 2000, 2, lambda: [("charge", forceManyBody().theta(0.7)
                                        .strength(lambda d, i, *a: -10 - i % 7)
@@ -149,7 +149,7 @@ def test_tree_walk_groups_distances_theta(group):
     assert_nodes_close(r["gpu"], r["cpu"], 3, rtol=1e-3, outliers=tree_outliers(2000))
 
 
-@pytest.mark.parametrize("group", [32, 16])
+@pytest.mark.parametrize("group", [32, 16, 1])
 def test_tree_walk_groups_mixed_signs(group):
     r = run_both(3, 2000, 2, lambda: [("charge", forceManyBody().theta(0.7)
                                        .strength(lambda d, i, *a: -20 if i % 4 else 12))],
