@@ -116,6 +116,10 @@ struct fl_sim {
   DevMem reds[2];
   int red_cur = 0;
   bool pre_valid = false;
+  // p + v of every node when the tick's first pass is a link: that link's snapshot, written by the
+  // integrate of the tick before (snap_valid) unless the state changed since
+  DevMem snap;
+  bool snap_valid = false;
   std::vector<std::unique_ptr<Pass>> plan;
   uint32_t seed = 0, step = 0;
   int64_t ticks = 0, launches = 0;
@@ -128,7 +132,7 @@ struct fl_sim {
   struct Block {
     int32_t count;
     int cur_in, cur_out, red_in, red_out;
-    bool pre_in, pre_out;
+    bool pre_in, pre_out, snap_in, snap_out;
     int64_t launches;
     bool captured;
     cudaGraphExec_t exec;
@@ -550,8 +554,15 @@ void encode_tick(fl_sim* s, float alpha, float decay) {
         for (int it = 0; it < p->d.iterations; ++it) {
           Scope sc(s, G_LINK);
           FlLinkCsr csr{p->row.as<int32_t>(), p->entry.as<float4>(), p->code.as<uint32_t>()};
+          // the tick's first pass reads the snapshot the last integrate wrote (or makes it)
+          const bool snapped = k == 0 && it == 0;
+          if (snapped && !s->snap_valid) {
+            fl_launch_snapshot(s->pos.as<float4>(), vel_cur(s), s->snap.as<float4>(), n, s->st);
+            ++s->launches;
+          }
           fl_launch_link(s->pos.as<float4>(), vel_cur(s), vel_next(s), csr, n, s->ndim, alpha,
-                         s->step, s->seed, s->st, nullptr, nullptr, s->tkp);
+                         s->step, s->seed, s->st, nullptr, nullptr, s->tkp,
+                         snapped ? s->snap.as<float4>() : nullptr);
           ++s->launches;
           s->cur = 1 - s->cur;
         }
@@ -595,13 +606,17 @@ void encode_tick(fl_sim* s, float alpha, float decay) {
     // the next tick needs the same reduction of the positions this integrate writes
     FlReduce* next = pre ? s->reds[1 - s->red_cur].as<FlReduce>() : nullptr;
     if (next) cudaMemsetAsync(next, 0, sizeof(FlReduce), s->st);
+    // the next tick's link snapshot, when a link is its first pass
+    const bool snap = np > 0 && plan[0]->type == FL_FORCE_LINK && plan[0]->m > 0;
     fl_launch_integrate(s->pos.as<float4>(), vel_cur(s), s->fix.as<float4>(),
                         s->mask.as<uint32_t>(), n, s->ndim, decay, c ? red_of(s) : nullptr,
                         c ? c->d.x : 0, c ? c->d.y : 0, c ? c->d.z : 0, c ? c->d.strength : 0,
-                        s->st, nullptr, nullptr, s->tkp, next, tree_at_start, fuse_center);
+                        s->st, nullptr, nullptr, s->tkp, next, tree_at_start, fuse_center,
+                        snap ? s->snap.as<float4>() : nullptr);
     ++s->launches;
     if (next) s->red_cur = 1 - s->red_cur;
     s->pre_valid = next != nullptr;
+    s->snap_valid = snap;
   }
 }
 
@@ -740,11 +755,12 @@ int32_t fl_set_nodes(fl_sim* s, int32_t n, int32_t ndim, const float* pos4, cons
   s->n = n;
   s->ndim = std::min(3, std::max(1, (int)ndim));
   s->cur = 0;
-  s->pre_valid = false;
+  s->pre_valid = s->snap_valid = false;
   const size_t v4 = 16 * (size_t)std::max(n, 1);
   FL_CK(s, s->pos.alloc(v4));
   FL_CK(s, s->vel[0].alloc(v4));
   FL_CK(s, s->vel[1].alloc(v4));
+  FL_CK(s, s->snap.alloc(v4));
   FL_CK(s, s->fix.alloc(v4));
   FL_CK(s, s->mask.alloc(4 * (size_t)std::max(n, 1)));
   FL_CK(s, s->pack.alloc(8 * (size_t)s->ndim * (size_t)std::max(n, 1)));
@@ -770,7 +786,7 @@ int32_t fl_upload_all(fl_sim* s, const float* pos4, const float* vel4, const flo
   // so that a tick block captured from that start replays from this one
   s->cur = 0;
   s->red_cur = 0;
-  s->pre_valid = false;
+  s->pre_valid = s->snap_valid = false;
   const size_t b4 = 16 * (size_t)s->n;
   if (s->n) {
     FL_CK(s, cudaMemcpyAsync(s->pos.p, pos4, b4, cudaMemcpyHostToDevice, s->st));
@@ -794,7 +810,7 @@ int32_t fl_update_positions(fl_sim* s, int32_t first, int32_t count, const float
   if (count)
     FL_CK(s, cudaMemcpyAsync(s->pos.as<float4>() + first, pos4, 16 * (size_t)count,
                              cudaMemcpyHostToDevice, s->st));
-  s->pre_valid = false;  // the next tick reduces the positions afresh (count 0: written on the device)
+  s->pre_valid = s->snap_valid = false;  // the next tick reduces the positions afresh (count 0: written on the device)
   FL_CK(s, cudaStreamSynchronize(s->st));
   return FL_OK;
 }
@@ -810,7 +826,7 @@ int32_t fl_update_positions_packed(fl_sim* s, int32_t first, int32_t count, cons
     fl_launch_unpack(s->pack.as<float>(), count, s->ndim, s->pos.as<float4>() + first, s->st);
     ++s->launches;
   }
-  s->pre_valid = false;
+  s->pre_valid = s->snap_valid = false;
   FL_CK(s, cudaStreamSynchronize(s->st));
   return FL_OK;
 }
@@ -824,6 +840,7 @@ int32_t fl_update_velocities(fl_sim* s, int32_t first, int32_t count, const floa
     FL_CK(s, cudaMemcpyAsync(vel_cur(s) + first, vel4, 16 * (size_t)count, cudaMemcpyHostToDevice,
                              s->st));
   FL_CK(s, cudaStreamSynchronize(s->st));
+  s->snap_valid = false;  // the link's snapshot holds p + v (count 0: written on the device)
   return FL_OK;
 }
 
@@ -886,7 +903,7 @@ int32_t fl_set_forces(fl_sim* s, int32_t count, const fl_force_desc* descs) {
   if (sig != s->plan_sig) {
     clear_blocks(s);
     s->plan_sig = std::move(sig);
-    s->pre_valid = false;  // the reduction the new passes want may differ
+    s->pre_valid = s->snap_valid = false;  // the reduction the new passes want may differ
   }
   return FL_OK;
 }
@@ -929,15 +946,16 @@ int32_t fl_enqueue(fl_sim* s, const double* alphas, int32_t count, double decay)
   if (s->use_graphs && !s->profiling)
     for (auto& x : s->blocks)
       if (x.count == count && x.cur_in == s->cur && x.red_in == s->red_cur &&
-          x.pre_in == s->pre_valid)
+          x.pre_in == s->pre_valid && x.snap_in == s->snap_valid)
         b = &x;
   if (b && b->captured) {
     FL_CK(s, cudaGraphLaunch(b->exec, s->st));
     s->cur = b->cur_out, s->red_cur = b->red_out, s->pre_valid = b->pre_out;
+    s->snap_valid = b->snap_out;
     s->launches += b->launches;
   } else if (b) {
     const int cur0 = s->cur, red0 = s->red_cur;
-    const bool pre0 = s->pre_valid;
+    const bool pre0 = s->pre_valid, snap0 = s->snap_valid;
     const int64_t l0 = s->launches;
     cudaGraph_t g = nullptr;
     bool ok = cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
@@ -956,13 +974,13 @@ int32_t fl_enqueue(fl_sim* s, const double* alphas, int32_t count, double decay)
       cudaGetLastError();
       if (g) cudaGraphDestroy(g);
       s->use_graphs = false;
-      s->cur = cur0, s->red_cur = red0, s->pre_valid = pre0;
+      s->cur = cur0, s->red_cur = red0, s->pre_valid = pre0, s->snap_valid = snap0;
       s->launches = l0;
       encode();
     }
   } else {
     const int cur0 = s->cur, red0 = s->red_cur;
-    const bool pre0 = s->pre_valid;
+    const bool pre0 = s->pre_valid, snap0 = s->snap_valid;
     const int64_t l0 = s->launches;
     encode();
     if (s->use_graphs && !s->profiling) {
@@ -971,7 +989,7 @@ int32_t fl_enqueue(fl_sim* s, const double* alphas, int32_t count, double decay)
         s->blocks.erase(s->blocks.begin());
       }
       s->blocks.push_back(fl_sim::Block{count, cur0, s->cur, red0, s->red_cur, pre0, s->pre_valid,
-                                        s->launches - l0, false, nullptr});
+                                        snap0, s->snap_valid, s->launches - l0, false, nullptr});
     }
   }
   s->step += (uint32_t)count;
@@ -1135,7 +1153,7 @@ int32_t fl_autotune(fl_sim* s, int32_t ticks, double alpha, double decay,
     FL_CK(s, cudaMemcpyAsync(s->vel[0].p, snap.as<char>() + v4, v4, cudaMemcpyDeviceToDevice, s->st));
     s->cur = 0;
     s->step = step0;
-    s->pre_valid = false;
+    s->pre_valid = s->snap_valid = false;
     return FL_OK;
   };
   cudaEvent_t e0 = nullptr, e1 = nullptr;

@@ -131,12 +131,17 @@ void fl_launch_center_apply(float4* pos, int n, int ndim, const FlReduce* red, d
 // centre force of (cx, cy, cz, strength) computed from red->sum (the centre force fused).
 // In a batch (gr, gid non-null) each node takes its graph's decay and centre shift.
 // With `out` (not in a batch), the new positions are also reduced into it (box and/or sums, as
-// fl_launch_reduce): the next tick's reduction, fused.
+// fl_launch_reduce): the next tick's reduction, fused. With `snap` (not in a batch), p + v of the
+// new state is written there: the next tick's link snapshot (fl_launch_snapshot).
 void fl_launch_integrate(float4* pos, float4* vel, const float4* fix, const uint32_t* mask, int n,
                          int ndim, float decay, const FlReduce* red, double cx, double cy,
                          double cz, double strength, cudaStream_t st, const FlGraph* gr = nullptr,
                          const uint32_t* gid = nullptr, const FlTick* tk = nullptr,
-                         FlReduce* out = nullptr, int want_box = 0, int want_sum = 0);
+                         FlReduce* out = nullptr, int want_box = 0, int want_sum = 0,
+                         float4* snap = nullptr);
+// snap = p + v per node (xyz; w 0): the state the link force reads, one record per node, so that
+// a link end gathers one 16-byte record of the other node instead of two.
+void fl_launch_snapshot(const float4* pos, const float4* vel, float4* snap, int n, cudaStream_t st);
 // Positions and velocities (either may be NULL) to `ndim` floats per node in out: positions at
 // [0, n ndim), velocities at [n ndim, 2 n ndim). And back: ndim floats per node to float4 (the
 // rest 0) at dst[0, count).
@@ -155,11 +160,13 @@ struct FlLinkCsr {
   const float4* entry;     // [2m] (other node as int bits, distance, strength, bias share)
   const uint32_t* code;    // [2m] link * 2 + (this node is the target)
 };
-// In a batch (gr, gid non-null) each node's links use its graph's alpha.
+// In a batch (gr, gid non-null) each node's links use its graph's alpha. With `snap` (p + vel_in
+// per node, fl_launch_snapshot) the kernel reads the nodes' state from it instead of pos and
+// vel_in: the same sums, half the gathered bytes.
 void fl_launch_link(const float4* pos, const float4* vel_in, float4* vel_out, FlLinkCsr csr, int n,
                     int ndim, float alpha, uint32_t step, uint32_t seed, cudaStream_t st,
                     const FlGraph* gr = nullptr, const uint32_t* gid = nullptr,
-                    const FlTick* tk = nullptr);
+                    const FlTick* tk = nullptr, const float4* snap = nullptr);
 
 // ---------------------------------------------------------------- many-body (tree.cu)
 struct FlTreeBufs {

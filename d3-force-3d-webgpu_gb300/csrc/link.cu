@@ -13,6 +13,9 @@
 // v += d_view * k * share. A zero component of d is replaced by the link's jiggle, with the
 // sign of the end that sees it.
 //
+// With a snapshot (snap = p + v per node, written by the integrate before) the node's own state
+// and every other end come from one 16-byte record: the same FP32 sums, half the bytes gathered.
+//
 // Load balance: a warp takes 32 consecutive rows; each lane walks its row with float4 loads.
 // Rows longer than kLong (high-degree hubs) are split across the whole warp and combined with a
 // warp reduction, so one hub does not stall its warp for thousands of iterations.
@@ -23,17 +26,32 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kLong = 64;
 
+// The state p + v of node j: from the snapshot, or summed from p and v.
+template <bool SNAP>
+__device__ __forceinline__ float3 state_of(const float4* __restrict__ pos,
+                                           const float4* __restrict__ vel,
+                                           const float4* __restrict__ snap, int j) {
+  if (SNAP) {
+    const float4 s = __ldg(snap + j);
+    return make_float3(s.x, s.y, s.z);
+  }
+  const float4 pj = __ldg(pos + j), vj = __ldg(vel + j);
+  return make_float3(pj.x + vj.x, pj.y + vj.y, pj.z + vj.z);
+}
+
 // One entry's term. The entry's code word (link * 2 + end) is read only for a zero component,
 // which is rare: the common case streams the float4 entries alone.
+template <bool SNAP>
 __device__ __forceinline__ void link_term(const float4* __restrict__ pos,
-                                          const float4* __restrict__ vel, float3 me, float4 e,
+                                          const float4* __restrict__ vel,
+                                          const float4* __restrict__ snap, float3 me, float4 e,
                                           const uint32_t* __restrict__ codep, int ndim,
                                           float alpha, uint32_t step, uint32_t seed, float3& acc) {
   const int j = __float_as_int(e.x);
-  const float4 pj = __ldg(pos + j), vj = __ldg(vel + j);
-  float dx = (pj.x + vj.x) - me.x;
-  float dy = ndim > 1 ? (pj.y + vj.y) - me.y : 0.f;
-  float dz = ndim > 2 ? (pj.z + vj.z) - me.z : 0.f;
+  const float3 sj = state_of<SNAP>(pos, vel, snap, j);
+  float dx = sj.x - me.x;
+  float dy = ndim > 1 ? sj.y - me.y : 0.f;
+  float dz = ndim > 2 ? sj.z - me.z : 0.f;
   if (dx == 0.f || (ndim > 1 && dy == 0.f) || (ndim > 2 && dz == 0.f)) {
     // jiggle(link): the same value at both ends, negated at the target
     const uint32_t code = __ldg(codep);
@@ -50,6 +68,7 @@ __device__ __forceinline__ void link_term(const float4* __restrict__ pos,
   acc.z += dz * k * e.w;
 }
 
+template <bool SNAP>
 __global__ void __launch_bounds__(kThreads) k_link(const float4* __restrict__ pos,
                                                    const float4* __restrict__ vel_in,
                                                    float4* __restrict__ vel_out,
@@ -59,7 +78,8 @@ __global__ void __launch_bounds__(kThreads) k_link(const float4* __restrict__ po
                                                    int ndim, float alpha, uint32_t step,
                                                    uint32_t seed, const FlGraph* __restrict__ gr,
                                                    const uint32_t* __restrict__ gid,
-                                                   const FlTick* __restrict__ tk) {
+                                                   const FlTick* __restrict__ tk,
+                                                   const float4* __restrict__ snap) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (tk) alpha = tk->alpha, step = tk->step, seed = tk->seed;
   const int lane = threadIdx.x & 31;
@@ -71,16 +91,24 @@ __global__ void __launch_bounds__(kThreads) k_link(const float4* __restrict__ po
     step += g.tick0;  // the graph's own step (its jiggles do not depend on the batch)
   }
   int r0 = 0, r1 = 0;
-  float4 p = make_float4(0, 0, 0, 0), v = p;
+  float4 v = make_float4(0, 0, 0, 0);
+  float3 me = make_float3(0.f, 0.f, 0.f);
   if (live) {
     r0 = row[i], r1 = row[i + 1];
-    p = pos[i], v = vel_in[i];
+    v = vel_in[i];
+    if (SNAP) {
+      const float4 s = snap[i];
+      me = make_float3(s.x, s.y, s.z);
+    } else {
+      const float4 p = pos[i];
+      me = make_float3(p.x + v.x, p.y + v.y, p.z + v.z);
+    }
   }
-  const float3 me = make_float3(p.x + v.x, p.y + v.y, p.z + v.z);
   float3 acc = make_float3(0.f, 0.f, 0.f);
   const bool longrow = !frozen && (r1 - r0) > kLong;
   if (!longrow && !frozen)
-    for (int e = r0; e < r1; ++e) link_term(pos, vel_in, me, __ldg(entry + e), code + e, ndim, alpha, step, seed, acc);
+    for (int e = r0; e < r1; ++e)
+      link_term<SNAP>(pos, vel_in, snap, me, __ldg(entry + e), code + e, ndim, alpha, step, seed, acc);
   // long rows: the warp takes them one at a time
   uint32_t longs = __ballot_sync(FL_FULL, longrow);
   while (longs) {
@@ -93,7 +121,7 @@ __global__ void __launch_bounds__(kThreads) k_link(const float4* __restrict__ po
     const uint32_t sm = __shfl_sync(FL_FULL, step, src);
     float3 part = make_float3(0.f, 0.f, 0.f);
     for (int e = a + lane; e < b; e += 32)
-      link_term(pos, vel_in, m, __ldg(entry + e), code + e, ndim, am, sm, seed, part);
+      link_term<SNAP>(pos, vel_in, snap, m, __ldg(entry + e), code + e, ndim, am, sm, seed, part);
     part.x = fl::warp_sum(part.x), part.y = fl::warp_sum(part.y), part.z = fl::warp_sum(part.z);
     if (lane == src) acc = part;
   }
@@ -108,9 +136,14 @@ __global__ void __launch_bounds__(kThreads) k_link(const float4* __restrict__ po
 
 void fl_launch_link(const float4* pos, const float4* vel_in, float4* vel_out, FlLinkCsr csr, int n,
                     int ndim, float alpha, uint32_t step, uint32_t seed, cudaStream_t st,
-                    const FlGraph* gr, const uint32_t* gid, const FlTick* tk) {
+                    const FlGraph* gr, const uint32_t* gid, const FlTick* tk,
+                    const float4* snap) {
   int g = (n + kThreads - 1) / kThreads;
   if (g < 1) g = 1;
-  k_link<<<g, kThreads, 0, st>>>(pos, vel_in, vel_out, csr.row, csr.entry, csr.code, n, ndim, alpha,
-                                 step, seed, gr, gid, tk);
+  if (snap)
+    k_link<true><<<g, kThreads, 0, st>>>(pos, vel_in, vel_out, csr.row, csr.entry, csr.code, n,
+                                         ndim, alpha, step, seed, gr, gid, tk, snap);
+  else
+    k_link<false><<<g, kThreads, 0, st>>>(pos, vel_in, vel_out, csr.row, csr.entry, csr.code, n,
+                                          ndim, alpha, step, seed, gr, gid, tk, nullptr);
 }

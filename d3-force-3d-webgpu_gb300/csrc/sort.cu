@@ -102,8 +102,8 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_onesweep(
   uint32_t total;
   // digit-wise phases: threads 0..255 take one digit each (a block of 256 or more threads)
   const bool dt = tid < 256;
-  const uint32_t gx = block_excl_scan<kThreads>(dt ? ghist[tid] : 0u, s_warp, &total);  // syncs inside
-  if (dt) s_gexcl[tid] = gx;
+  const uint32_t gh = dt ? ghist[tid] : 0u;
+  __syncthreads();
   const uint32_t tile = s_tile;
   const int64_t tbase = (int64_t)tile * kTile;
 
@@ -123,6 +123,10 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) k_onesweep(
       dig[j] = 256u + lane;  // unique: ranked alone, never stored
     }
   }
+  // the digits' global offsets, while the keys are on their way (a scan has barriers, which
+  // would otherwise hold the loads back)
+  const uint32_t gx = block_excl_scan<kThreads>(gh, s_warp, &total);  // syncs inside
+  if (dt) s_gexcl[tid] = gx;
   const uint32_t lt = fl::lanemask_lt();
 #pragma unroll
   for (int j = 0; j < kItems; ++j) {

@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(kThreads) k_integrate_reduce(
     float4* __restrict__ pos, float4* __restrict__ vel, const float4* __restrict__ fix,
     const uint32_t* __restrict__ mask, int n, int ndim, float decay, const FlReduce* red,
     double cx, double cy, double cz, double strength, const FlTick* __restrict__ tk,
-    FlReduce* out, int want_box, int want_sum) {
+    FlReduce* out, int want_box, int want_sum, float4* __restrict__ snap) {
   if (tk) decay = tk->decay;
   float2 sh[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
   if (red) center_shift(red, n, ndim, cx, cy, cz, strength, sh);  // block-uniform branch
@@ -255,6 +255,7 @@ __global__ void __launch_bounds__(kThreads) k_integrate_reduce(
     integrate_node(p, v, fix, mask[i], i, ndim, decay, red != nullptr, sh);
     pos[i] = p;
     vel[i] = v;
+    if (snap) snap[i] = make_float4(p.x + v.x, p.y + v.y, p.z + v.z, 0.f);
     q.add(p, ndim, want_sum);
   }
   flush_partial(q, ndim, want_box, want_sum, out);
@@ -268,7 +269,8 @@ __global__ void __launch_bounds__(kThreads) k_integrate(float4* __restrict__ pos
                                                         double cx, double cy, double cz,
                                                         double strength, const FlGraph* gr,
                                                         const uint32_t* __restrict__ gid,
-                                                        const FlTick* __restrict__ tk) {
+                                                        const FlTick* __restrict__ tk,
+                                                        float4* __restrict__ snap) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (tk) decay = tk->decay;
   float2 sh[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
@@ -284,6 +286,16 @@ __global__ void __launch_bounds__(kThreads) k_integrate(float4* __restrict__ pos
   integrate_node(p, v, fix, mask[i], i, ndim, decay, red || gr, sh);
   pos[i] = p;
   vel[i] = v;
+  if (snap) snap[i] = make_float4(p.x + v.x, p.y + v.y, p.z + v.z, 0.f);
+}
+
+__global__ void __launch_bounds__(kThreads) k_snapshot(const float4* __restrict__ pos,
+                                                       const float4* __restrict__ vel,
+                                                       float4* __restrict__ snap, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 p = pos[i], v = vel[i];
+  snap[i] = make_float4(p.x + v.x, p.y + v.y, p.z + v.z, 0.f);
 }
 
 __device__ __forceinline__ float or1e6(float v) { return v != 0.f ? v : 1e-6f; }
@@ -394,16 +406,22 @@ void fl_launch_integrate(float4* pos, float4* vel, const float4* fix, const uint
                          int ndim, float decay, const FlReduce* red, double cx, double cy,
                          double cz, double strength, cudaStream_t st, const FlGraph* gr,
                          const uint32_t* gid, const FlTick* tk, FlReduce* out, int want_box,
-                         int want_sum) {
+                         int want_sum, float4* snap) {
+  if (gr) snap = nullptr;  // a batch keeps no snapshot
   if (out && !gr) {
     int g = grid_for(n, kThreads * 4);
     if (g > 4 * fl_sms()) g = 4 * fl_sms();
     k_integrate_reduce<<<g, kThreads, 0, st>>>(pos, vel, fix, mask, n, ndim, decay, red, cx, cy,
-                                                cz, strength, tk, out, want_box, want_sum);
+                                                cz, strength, tk, out, want_box, want_sum, snap);
     return;
   }
   k_integrate<<<grid_for(n, kThreads), kThreads, 0, st>>>(pos, vel, fix, mask, n, ndim, decay, red,
-                                                          cx, cy, cz, strength, gr, gid, tk);
+                                                          cx, cy, cz, strength, gr, gid, tk, snap);
+}
+
+void fl_launch_snapshot(const float4* pos, const float4* vel, float4* snap, int n, cudaStream_t st) {
+  if (n <= 0) return;
+  k_snapshot<<<grid_for(n, kThreads), kThreads, 0, st>>>(pos, vel, snap, n);
 }
 
 void fl_launch_radial(const float4* pos, float4* vel, const float* radius, const float* strength,

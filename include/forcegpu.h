@@ -151,8 +151,10 @@ int32_t fl_idle(fl_sim* sim);
 int32_t fl_busy(fl_sim* sim, int32_t* busy);
 /* Device pointers of the state (engine.buffers), for reading (rendering): positions written
  * through them are not seen by the next tick's bounding box and centre sums, which the last
- * integrate already took; write positions with fl_update_positions, or call
- * fl_update_positions(sim, 0, 0, NULL) after writing them on the device. */
+ * integrate already took, nor velocities by the next tick's link snapshot (p + v, also written
+ * by the last integrate); write positions with fl_update_positions and velocities with
+ * fl_update_velocities, or call fl_update_positions(sim, 0, 0, NULL) /
+ * fl_update_velocities(sim, 0, 0, NULL) after writing them on the device. */
 int32_t fl_buffers(fl_sim* sim, fl_buffer_info* out);
 
 /* ---- measurement (no reference counterpart: the reference times only with performance.now()
