@@ -291,6 +291,9 @@ int32_t ensure_scratch(fl_sim* s, Pass* p) {
   if (p->type == FL_FORCE_MANYBODY) bytes += fl_tree_bytes(n) + 256;
   if (p->type == FL_FORCE_COLLIDE) bytes += fl_grid_bytes(n) + 256;
   FL_CK(s, p->scratch.alloc(bytes));
+  // zero: the sort's counters and look-back words and the walk's group counter start at 0 (each
+  // sort and walk leaves them at 0 again)
+  FL_CK(s, cudaMemset(p->scratch.p, 0, bytes));
   char* base = p->scratch.as<char>();
   fl_sort_carve(&p->sb, base, n);
   base += (fl_sort_bytes(n) + 255) & ~(size_t)255;
@@ -370,8 +373,11 @@ bool is_tree(const Pass* p) {
 // ---------------------------------------------------------------- the tick
 
 // The many-body tree of pass p from the current positions (box: their bounding box, or null to
-// reduce it here), on stream st.
-void encode_tree(fl_sim* s, Pass* p, const FlReduce* box, cudaStream_t st) {
+// reduce it here), on stream st. The sort's histograms, tickets and look-back words are zero
+// before the sort (zeroed with the scratch, then after every sort, on the tree's shorter branch,
+// off the critical path); `zero` (may be null), a reduction record the tick's integrate fills
+// later, is zeroed on that branch too.
+void encode_tree(fl_sim* s, Pass* p, const FlReduce* box, cudaStream_t st, FlReduce* zero = nullptr) {
   const int n = s->n;
   FlTreeBufs* t = &p->tb;
   const float* strength = p->a.as<float>();
@@ -386,9 +392,13 @@ void encode_tree(fl_sim* s, Pass* p, const FlReduce* box, cudaStream_t st) {
   // a small layout's keys are sorted in one launch (unless digit passes were asked for), so
   // the keys need no digit histograms (lo_bit 64: none)
   const bool by_rank = n <= kSortRankMax && s->sort_passes == 0;
+  const int passes = (64 - lo_sort + 7) / 8;
+  auto clean = [&](cudaStream_t cs) {  // what the next sort and the integrate want at zero
+    if (!by_rank) fl_sort_reset(&p->sb, n, passes, cs);
+    if (zero) cudaMemsetAsync(zero, 0, sizeof(FlReduce), cs);
+  };
   {
     Scope sc(s, G_MORTON, st);
-    if (!by_rank) fl_sort_reset(&p->sb, n, (64 - lo_sort + 7) / 8, st);
     fl_launch_morton(s->pos.as<float4>(), n, s->ndim, box, p->sb.keys[0], p->sb.vals[0],
                      by_rank ? nullptr : p->sb.hist, by_rank ? 64 : lo_sort, p->cube.as<float>(),
                      st);
@@ -406,6 +416,7 @@ void encode_tree(fl_sim* s, Pass* p, const FlReduce* box, cudaStream_t st) {
     }
     p->sorted_in = r;
   }
+  if (!(s->aux2 && !s->profiling)) clean(st);
   // the closed form (exact fixed-point sums) when the strengths share one sign, unless a
   // recursion was asked for
   const bool closed = !p->mixed && s->cell_sums == FL_CELLS_AUTO;
@@ -420,6 +431,7 @@ void encode_tree(fl_sim* s, Pass* p, const FlReduce* box, cudaStream_t st) {
     cudaEventRecord(s->ev_nodes, s->aux2);
     fl_launch_build_points(t, p->sb.keys[r], p->sb.vals[r], s->pos.as<float4>(), strength,
                            closed, p->cube.as<float>(), p->fx_exp, st, &s->launches);
+    clean(st);
     cudaStreamWaitEvent(st, s->ev_nodes, 0);
     fl_launch_cells(t, closed, p->sign, p->cube.as<float>(), p->fx_exp, fp64_depth,
                     s->errw.as<uint32_t>(), st, &s->launches);
@@ -535,10 +547,14 @@ void encode_tick(fl_sim* s, float alpha, float decay) {
         break;
       }
     }
+  // the record the integrate reduces the new positions into (zeroed beside the early tree)
+  FlReduce* next = pre ? s->reds[1 - s->red_cur].as<FlReduce>() : nullptr;
+  bool next_zeroed = false;
   if (early >= 0) {
     cudaEventRecord(s->ev_fork, s->st);
     cudaStreamWaitEvent(s->aux, s->ev_fork, 0);
-    encode_tree(s, plan[early].get(), red_of(s), s->aux);
+    encode_tree(s, plan[early].get(), red_of(s), s->aux, next);
+    next_zeroed = next != nullptr;
     cudaEventRecord(s->ev_tree, s->aux);
   }
   bool before_center = true;
@@ -604,8 +620,7 @@ void encode_tick(fl_sim* s, float alpha, float decay) {
     Scope sc(s, G_INTEGRATE);
     const Pass* c = fuse_center ? plan[np - 1].get() : nullptr;
     // the next tick needs the same reduction of the positions this integrate writes
-    FlReduce* next = pre ? s->reds[1 - s->red_cur].as<FlReduce>() : nullptr;
-    if (next) cudaMemsetAsync(next, 0, sizeof(FlReduce), s->st);
+    if (next && !next_zeroed) cudaMemsetAsync(next, 0, sizeof(FlReduce), s->st);
     // the next tick's link snapshot, when a link is its first pass
     const bool snap = np > 0 && plan[0]->type == FL_FORCE_LINK && plan[0]->m > 0;
     fl_launch_integrate(s->pos.as<float4>(), vel_cur(s), s->fix.as<float4>(),

@@ -39,16 +39,11 @@ __device__ __forceinline__ float3 state_of(const float4* __restrict__ pos,
   return make_float3(pj.x + vj.x, pj.y + vj.y, pj.z + vj.z);
 }
 
-// One entry's term. The entry's code word (link * 2 + end) is read only for a zero component,
-// which is rare: the common case streams the float4 entries alone.
-template <bool SNAP>
-__device__ __forceinline__ void link_term(const float4* __restrict__ pos,
-                                          const float4* __restrict__ vel,
-                                          const float4* __restrict__ snap, float3 me, float4 e,
-                                          const uint32_t* __restrict__ codep, int ndim,
-                                          float alpha, uint32_t step, uint32_t seed, float3& acc) {
-  const int j = __float_as_int(e.x);
-  const float3 sj = state_of<SNAP>(pos, vel, snap, j);
+// One entry's term, given the other end's state sj. The entry's code word (link * 2 + end) is
+// read only for a zero component, which is rare: the common case streams the float4 entries alone.
+__device__ __forceinline__ void link_apply(float3 sj, float3 me, float4 e,
+                                           const uint32_t* __restrict__ codep, int ndim,
+                                           float alpha, uint32_t step, uint32_t seed, float3& acc) {
   float dx = sj.x - me.x;
   float dy = ndim > 1 ? sj.y - me.y : 0.f;
   float dz = ndim > 2 ? sj.z - me.z : 0.f;
@@ -66,6 +61,16 @@ __device__ __forceinline__ void link_term(const float4* __restrict__ pos,
   acc.x += dx * k * e.w;
   acc.y += dy * k * e.w;
   acc.z += dz * k * e.w;
+}
+
+template <bool SNAP>
+__device__ __forceinline__ void link_term(const float4* __restrict__ pos,
+                                          const float4* __restrict__ vel,
+                                          const float4* __restrict__ snap, float3 me, float4 e,
+                                          const uint32_t* __restrict__ codep, int ndim,
+                                          float alpha, uint32_t step, uint32_t seed, float3& acc) {
+  link_apply(state_of<SNAP>(pos, vel, snap, __float_as_int(e.x)), me, e, codep, ndim, alpha, step,
+             seed, acc);
 }
 
 template <bool SNAP>
@@ -106,9 +111,20 @@ __global__ void __launch_bounds__(kThreads) k_link(const float4* __restrict__ po
   }
   float3 acc = make_float3(0.f, 0.f, 0.f);
   const bool longrow = !frozen && (r1 - r0) > kLong;
-  if (!longrow && !frozen)
-    for (int e = r0; e < r1; ++e)
+  if (!longrow && !frozen) {
+    // two entries at a time: both loads and both gathers in flight before either term (the terms
+    // still add in row order)
+    int e = r0;
+    for (; e + 1 < r1; e += 2) {
+      const float4 ea = __ldg(entry + e), eb = __ldg(entry + e + 1);
+      const float3 sa = state_of<SNAP>(pos, vel_in, snap, __float_as_int(ea.x));
+      const float3 sb = state_of<SNAP>(pos, vel_in, snap, __float_as_int(eb.x));
+      link_apply(sa, me, ea, code + e, ndim, alpha, step, seed, acc);
+      link_apply(sb, me, eb, code + e + 1, ndim, alpha, step, seed, acc);
+    }
+    if (e < r1)
       link_term<SNAP>(pos, vel_in, snap, me, __ldg(entry + e), code + e, ndim, alpha, step, seed, acc);
+  }
   // long rows: the warp takes them one at a time
   uint32_t longs = __ballot_sync(FL_FULL, longrow);
   while (longs) {

@@ -1186,6 +1186,9 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk(
   wi = lane == 0 ? (int)atomicAdd(work, 1u) : 0;
   wi = __shfl_sync(FL_FULL, wi, 0);
   }
+  // every warp ends on one claim past the last group; the last of those claims puts the counter
+  // back to 0 for the next launch (no other warp touches it after its own last claim)
+  if (lane == 0 && wi == nwarps + (int)(gridDim.x * kWalkWarps) - 1) *work = 0u;
   if (STATS) {
     if (gl == 0) {
       atomicAdd(stats, st_tests);
@@ -1363,6 +1366,8 @@ __global__ void __launch_bounds__(kWalkThreads) k_walk_lanes(
     t = lane == 0 ? (int)atomicAdd(work, 1u) : 0;
     t = __shfl_sync(FL_FULL, t, 0);
   }
+  // as in k_walk: the last claim past the end puts the counter back to 0
+  if (lane == 0 && t == n + (int)(gridDim.x * kWalkWarps) - 1) *work = 0u;
   if (STATS && lane == 0) {
     atomicAdd(stats, st_tests);
     atomicAdd(stats + 1, st_useful);
@@ -1647,7 +1652,9 @@ void fl_launch_walk(const FlTreeBufs* t, const uint32_t* perm, const float* cube
   // a persistent grid of the blocks that fit on the device at once (and that the spill buffer
   // has regions for), each warp walking every (grid)-th group of 32 points
   const int cap = t->walk_slots / kWalkWarps;
-  cudaMemsetAsync(t->work, 0, 4, st);
+  // the counter is 0 before a launch: zeroed with the scratch, and each launch's last claim puts
+  // it back (a batch, whose tree buffers are carved anew as it grows, zeroes it here as well)
+  if (segs.graphs) cudaMemsetAsync(t->work, 0, 4, st);
   const float fmax2 = dmax2 > 3e38 ? INFINITY : (float)dmax2;
 #define FL_WALK_ONE(D, G, S, M, B)                                                             \
   do {                                                                                         \
