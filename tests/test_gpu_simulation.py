@@ -419,3 +419,23 @@ def test_a_destroyed_simulations_nodes_can_be_collected():
         gc.collect()
         time.sleep(0.01)
     assert ref() is None, "still reachable"
+
+
+# --- simulation.find (test/find-test.js) ---
+
+def test_find_finds_the_closest_node_within_a_radius():
+    a, b, c = {"x": 5, "y": 0}, {"x": 10, "y": 16}, {"x": -10, "y": -4}
+    sim = make([a, b, c], 2).stop()
+    assert sim.find(0, 0) is a
+    assert sim.find(0, 0, 1) is None
+    assert sim.find(0, 20) is b
+    sim.destroy()
+
+
+def test_find_uses_every_dimension_of_a_3d_layout():
+    a, b = {"x": 0, "y": 0, "z": 10}, {"x": 0, "y": 0, "z": -3}
+    sim = make([a, b], 3).stop()
+    assert sim.find(0, 0, 8) is a
+    assert sim.find(0, 0, -1) is b
+    assert sim.find(0, 0, 4, 2) is None
+    sim.destroy()
