@@ -830,7 +830,8 @@ int32_t fl_update_positions(fl_sim* s, int32_t first, int32_t count, const float
   return FL_OK;
 }
 
-int32_t fl_update_positions_packed(fl_sim* s, int32_t first, int32_t count, const float* pos) {
+// The packed upload, queued on the stream; `wait` makes the call return after it has run.
+static int32_t update_packed(fl_sim* s, int32_t first, int32_t count, const float* pos, bool wait) {
   int32_t rc = check_sim(s);
   if (rc) return rc;
   if (first < 0 || count < 0 || first + (int64_t)count > s->n || (count && !pos))
@@ -842,8 +843,17 @@ int32_t fl_update_positions_packed(fl_sim* s, int32_t first, int32_t count, cons
     ++s->launches;
   }
   s->pre_valid = s->snap_valid = false;
-  FL_CK(s, cudaStreamSynchronize(s->st));
+  if (wait) FL_CK(s, cudaStreamSynchronize(s->st));
   return FL_OK;
+}
+
+int32_t fl_update_positions_packed(fl_sim* s, int32_t first, int32_t count, const float* pos) {
+  return update_packed(s, first, count, pos, true);
+}
+
+int32_t fl_update_positions_packed_async(fl_sim* s, int32_t first, int32_t count,
+                                         const float* pos) {
+  return update_packed(s, first, count, pos, false);
 }
 
 int32_t fl_update_velocities(fl_sim* s, int32_t first, int32_t count, const float* vel4) {

@@ -29,7 +29,8 @@ EXPORTS = ["fl_create", "fl_destroy", "fl_last_error", "fl_fits", "fl_set_nodes"
            "fl_batch_destroy", "fl_batch_last_error", "fl_batch_set_graphs", "fl_batch_set_seed",
            "fl_batch_enqueue", "fl_batch_sync", "fl_batch_query", "fl_batch_stream",
            "fl_autotune", "fl_batch_set_tuning", "fl_batch_autotune", "fl_batch_read",
-           "fl_update_positions_packed", "fl_sync_packed", "fl_upload_all", "fl_debug_links",
+           "fl_update_positions_packed", "fl_update_positions_packed_async", "fl_sync_packed",
+           "fl_upload_all", "fl_debug_links",
            "fl_batch_add_graphs"]
 SORT_NOALLOC_MAX_PAIRS = 262144  # FL_SORT_NOALLOC_MAX_PAIRS
 TUNE_WALK_GROUP, TUNE_CELL_SUMS, TUNE_GRAPHS = 1, 2, 3
@@ -122,6 +123,7 @@ def load():
         "fl_sync": (I32, [P, P, P]),
         "fl_sync_packed": (I32, [P, P, P]),
         "fl_update_positions_packed": (I32, [P, I32, I32, P]),
+        "fl_update_positions_packed_async": (I32, [P, I32, I32, P]),
         "fl_idle": (I32, [P]),
         "fl_busy": (I32, [P, ctypes.POINTER(I32)]),
         "fl_buffers": (I32, [P, ctypes.POINTER(BufferInfo)]),
@@ -171,6 +173,7 @@ class Engine:
         self.n = 0
         self.ndim = 2
         self._keep = []
+        self._in_flight = None  # the host array an async upload still reads
 
     def _check(self, rc, h=...):
         if rc != FL_OK:
@@ -221,6 +224,17 @@ class Engine:
         pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, self.ndim)
         self._check(self.L.fl_update_positions_packed(self.h, int(first), len(pos), _ptr(pos)))
 
+    def update_positions_packed_async(self, first, pos):
+        """fl_update_positions_packed_async: queued, not waited for. `pos` must be a C-contiguous
+        float32 (count, ndim) array (best in pinned memory); it is used in place, kept alive here
+        and must stay unchanged until the next sync or idle."""
+        if pos.dtype != np.float32 or not pos.flags.c_contiguous or pos.size % self.ndim:
+            raise ValueError("update_positions_packed_async wants a C-contiguous float32 array "
+                             "of count * ndim floats")
+        self._check(self.L.fl_update_positions_packed_async(self.h, int(first),
+                                                            pos.size // self.ndim, _ptr(pos)))
+        self._in_flight = pos
+
     def update_velocities(self, first, vel4):
         vel4 = np.ascontiguousarray(vel4, dtype=np.float32).reshape(-1, 4)
         self._check(self.L.fl_update_velocities(self.h, int(first), len(vel4), _ptr(vel4)))
@@ -251,11 +265,13 @@ class Engine:
         if vel_out is None:
             vel_out = np.empty((self.n, 4), np.float32)
         self._check(self.L.fl_sync(self.h, _ptr(pos_out), _ptr(vel_out)))
+        self._in_flight = None
         return pos_out, vel_out
 
     def sync_into(self, pos_ptr, vel_ptr):
         """Wait, then read back into caller-owned host memory given by address (e.g. pinned)."""
         self._check(self.L.fl_sync(self.h, pos_ptr, vel_ptr))
+        self._in_flight = None
 
     def sync_packed(self, pos_out=None, vel_out=None):
         """fl_sync into float32 (n, ndim) arrays: ndim floats per node cross the host link."""
@@ -267,14 +283,17 @@ class Engine:
             if a.dtype != np.float32 or not a.flags.c_contiguous or a.size != self.n * self.ndim:
                 raise ValueError("sync_packed wants C-contiguous float32 arrays of n * ndim floats")
         self._check(self.L.fl_sync_packed(self.h, _ptr(pos_out), _ptr(vel_out)))
+        self._in_flight = None
         return pos_out, vel_out
 
     def sync_packed_into(self, pos_ptr, vel_ptr):
         """fl_sync_packed into caller-owned host memory given by address (e.g. pinned)."""
         self._check(self.L.fl_sync_packed(self.h, pos_ptr, vel_ptr))
+        self._in_flight = None
 
     def idle(self):
         self._check(self.L.fl_idle(self.h))
+        self._in_flight = None
 
     def busy(self):
         out = ctypes.c_int32()

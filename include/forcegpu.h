@@ -119,6 +119,13 @@ int32_t fl_update_positions(fl_sim* sim, int32_t first, int32_t count, const flo
  * the device, so the host link carries ndim/4 of the bytes. No counterpart in the reference,
  * whose uploadPositions writes vec4s (src/gpu/engine.js:147-156). */
 int32_t fl_update_positions_packed(fl_sim* sim, int32_t first, int32_t count, const float* pos);
+/* fl_update_positions_packed without the wait: the copy and the unpacking are queued on the
+ * simulation's stream and the call returns at once, so that the ticks queued next follow them
+ * with no host round trip in between. The caller keeps `pos` (best pinned: cudaHostAlloc or
+ * cudaHostRegister) unchanged until the next fl_sync, fl_sync_packed or fl_idle returns. No
+ * counterpart in the reference. */
+int32_t fl_update_positions_packed_async(fl_sim* sim, int32_t first, int32_t count,
+                                         const float* pos);
 /* Upload changed pins of nodes [first, first + count) (uploadPinned, src/gpu/engine.js:158-169). */
 int32_t fl_update_pins(fl_sim* sim, int32_t first, int32_t count, const float* fix4,
                        const uint32_t* mask);

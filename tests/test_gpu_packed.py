@@ -82,3 +82,39 @@ def test_packed_calls_check_their_arguments():
         e.sync_packed(np.empty((1000, 4), np.float32), None)
     e.update_positions_packed(0, np.zeros((0, 3), np.float32))  # an empty range is fine
     e.close()
+
+
+@pytest.mark.parametrize("dims", [2, 3])
+def test_a_queued_upload_steps_as_the_waited_one(dims):
+    """fl_update_positions_packed_async: the same layout as the waited upload, tick after tick,
+    with the host array read in place (it stays unchanged until the next sync)."""
+    n = 40000
+    rng = np.random.default_rng(3)
+    out = []
+    for queued in (False, True):
+        e = engine(n, dims)
+        e.enqueue(np.array([0.9]), 0.6)
+        p, _ = (x.copy() for x in e.sync_packed())
+        for k in range(4):
+            up = np.ascontiguousarray(p + rng.normal(0.0, 0.5, p.shape).astype(np.float32)) \
+                if k == 0 else p.copy()
+            if queued:
+                e.update_positions_packed_async(0, up)
+            else:
+                e.update_positions_packed(0, up)
+            e.enqueue(np.array([0.8 - 0.05 * k]), 0.6)
+            p, v = (x.copy() for x in e.sync_packed())
+        out.append((p, v))
+        e.close()
+        rng = np.random.default_rng(3)
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+
+
+def test_a_queued_upload_wants_an_array_it_can_read_in_place():
+    e = engine(1000, 3)
+    with pytest.raises(ValueError):
+        e.update_positions_packed_async(0, np.zeros((1000, 3), np.float64))
+    with pytest.raises(ValueError):
+        e.update_positions_packed_async(0, np.zeros((3, 1000), np.float32).T)
+    e.close()
