@@ -179,11 +179,12 @@ struct FlTreeBufs {
   uint8_t* depth;        // [n-1] d3 depth of each internal node's cell
   uint32_t* count;       // [n-1] children of a head (0 for other nodes)
   uint32_t* first;       // [n-1] first child slot of a head
-  uint32_t* flag;        // [n-1] bottom-up arrival counters
+  uint32_t* flag;        // [n-1] arrivals of each head's child cells (mixed-sign recursion)
   float4* cell;          // [n-1] head: centroid, value at its own depth
   float4* leaf;          // [n] sorted points: position, strength
   float4* child_data;    // [2n] slot: centroid or position, value at own depth / strength
   uint2* child_meta;     // [2n] slot: (first child slot, count | depth << 26) or (sorted index, ~0)
+  double* slot64;        // [2n] slot of a cell: d3's FP64 value at its depth (mixed-sign recursion)
   void* scan_scratch;
   double* wsum;          // [5n] per sorted point |a|, |a| x, |a| y, |a| z, a; then their prefix sums
   double* wtiles;        // [5 tiles] partial sums of the prefix scan

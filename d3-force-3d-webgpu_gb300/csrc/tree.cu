@@ -22,8 +22,9 @@
 //              recursion has a closed form, value(D) = sum_p s_p c^(leafDepth_p - D) and centroid
 //              weights |s_p| c^leafDepth_p, so every cell is a range sum of exact int64
 //              fixed-point prefix sums over the sorted points. With strengths of both signs the
-//              recursion itself runs, bottom-up with atomic arrival flags (FP64 sums for the top
-//              levels).
+//              recursion itself runs over the d3 cells, from the deepest up through the child
+//              slots, with atomic arrival counts: d3's FP64 values bit for bit (so cells that
+//              cancel are skipped as d3 skips them), FP64 centroid sums for the top levels.
 //   slots      each cell writes its children (position or centroid, value at own depth, and for
 //              a child cell its child range and depth) into its slots
 //   walk       a group of G consecutive sorted points (G = 32: a warp, or 16) walks the union of
@@ -38,6 +39,7 @@
 #include <math.h>
 
 #include <atomic>
+#include <cuda/atomic>
 #include <cmath>
 
 #include "kernels.h"
@@ -502,35 +504,6 @@ __global__ void __launch_bounds__(kThreads) k_build(
   depth[i] = (uint8_t)(dep > L ? L : dep);
 }
 
-// Frontier children of head i (the first binary descendants outside its cell), left to right.
-template <typename F>
-__device__ __forceinline__ uint32_t for_children(uint32_t i, int D, int L,
-                                                 const uint32_t* __restrict__ left,
-                                                 const uint32_t* __restrict__ right,
-                                                 const uint32_t* __restrict__ range,
-                                                 const uint8_t* __restrict__ depth, F&& f) {
-  uint32_t c = 0;
-  if (D == L) {  // equal codes: all points of the range
-    const uint32_t a = range[2 * i], b = range[2 * i + 1];
-    for (uint32_t li = a; li <= b; ++li) f(kLeaf | li, c++);
-    return c;
-  }
-  uint32_t stack[16];
-  int sp = 0;
-  stack[sp++] = right[i];
-  stack[sp++] = left[i];
-  while (sp > 0) {
-    const uint32_t x = stack[--sp];
-    if (!(x & kLeaf) && depth[x] == D && sp < 15) {
-      stack[sp++] = right[x];
-      stack[sp++] = left[x];
-    } else {
-      f(x, c++);
-    }
-  }
-  return c;
-}
-
 // Every binary node below the root that is a d3 child (a point, or an internal node deeper than
 // its parent: the first node of another cell) finds the head of its parent's cell, climbing the
 // binary nodes of equal depth, and marks its octant (its keys' digit at the parent's depth) in
@@ -722,65 +695,130 @@ __global__ void __launch_bounds__(kThreads) k_heads(int n, int ndim,
   if (threadIdx.x == kThreads - 1) ctot[blockIdx.x] = before + x;
 }
 
-// The recursion itself (strengths of both signs), bottom-up with arrival flags: the second
-// thread to reach a node proceeds; a head combines its d3 children as accumulate() does.
-__global__ void __launch_bounds__(kThreads) k_cells_climb(
-    int n, int ndim, const uint32_t* __restrict__ left, const uint32_t* __restrict__ right,
-    const uint32_t* __restrict__ parent, const uint32_t* __restrict__ leaf_parent,
-    const uint32_t* __restrict__ range, const uint8_t* __restrict__ depth,
-    const uint32_t* __restrict__ count, uint32_t* __restrict__ flag, float4* cell,
-    const float4* __restrict__ leaf, int fp64_depth, uint32_t* err) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= n) return;
+// The cell children among a head's slots (the rest are points).
+__device__ __forceinline__ uint32_t cells_among(const uint2* __restrict__ cmeta, uint32_t fs,
+                                                uint32_t cnt) {
+  uint32_t k = 0;
+  for (uint32_t j = 0; j < cnt; ++j) k += cmeta[fs + j].y != kLeafMark;
+  return k;
+}
+
+// The recursion itself (strengths of both signs), over the d3 cells from the deepest up, reading
+// each head's children from its slots (k_slots has written the points and every slot's meta):
+// a head whose children are all points starts; a finished cell writes itself into its slot
+// among its parent's children and counts itself in at the parent, and the last of the parent's
+// cell children to arrive combines the parent. So the chain of dependent steps is the d3 depth.
+// A head combines its children as accumulate() does (src/manyBody.js:42-71). With
+// fp64_depth > 0 every value is d3's FP64 number bit for bit: the children's values summed in
+// slot order, which is d3's octant order (z << 2 | y << 1 | x), a chain of one-child cells
+// scaled by c once per level, the sum scaled by c; each cell's FP64 value rides in slot64 beside
+// its slot. So a cell whose children cancel is skipped (`!quad.value`, src/manyBody.js:74)
+// exactly when d3 skips it: a cancellation can leave d3 an FP64 residual, a value that d3
+// opens like any other. Centroids are weighted by the FP32 values, summed in FP64 above
+// fp64_depth and in FP32 below. fp64_depth 0 runs all of it in FP32 (values within 2^-20 of
+// their children's |values| count as 0), for precision comparisons.
+__global__ void __launch_bounds__(kThreads) k_cells_up(
+    int n, int ndim, const uint32_t* __restrict__ parent, const uint32_t* __restrict__ head_of,
+    const uint32_t* __restrict__ omask, const uint8_t* __restrict__ depth,
+    const uint32_t* __restrict__ count, const uint32_t* __restrict__ first,
+    const uint32_t* __restrict__ ctot, uint32_t* __restrict__ arrive, float4* cdata,
+    const uint2* __restrict__ cmeta, double* slot64, int fp64_depth, uint32_t* err, FlSegs seg) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n - 1) return;
+  uint32_t h = (uint32_t)t;
+  int D = depth[h];
+  uint32_t cnt = D == kGapDepth ? 0u : count[h];
+  if (!cnt) return;  // not a head
   const int L = levels_of(ndim);
+  const uint32_t roots = seg.graphs ? (uint32_t)seg.graphs : 1u;
+  const uint32_t nslots = 2u * (uint32_t)n + 1u;
+  uint32_t fs = first_slot(first, ctot, h, roots);
+  if (fs + cnt > nslots) {  // a malformed tree
+    atomicOr(err, FL_ERR_TREE);
+    return;
+  }
+  if (D < L && cells_among(cmeta, fs, cnt)) return;  // its last child cell combines it
   const double c1 = sqrt(4.0 / (double)(1 << ndim));
-  uint32_t node = leaf_parent[s];
-  if (node == kNoParent) return;  // a point alone in its graph
+  const bool exact = fp64_depth > 0;
   for (int guard = 0;; ++guard) {
-    if (guard > 256) {
+    if (guard > 64) {
       atomicOr(err, FL_ERR_TREE);
       return;
     }
-    __threadfence();
-    if (atomicAdd(&flag[node], 1u) == 0) return;  // the sibling subtree is still working
-    __threadfence();
-    if (count[node]) {
-      const int D = depth[node];
-      const bool wide = D < fp64_depth;
-      double sv = 0, sa = 0, sx = 0, sy = 0, sz = 0;
-      float fv = 0, fa = 0, fx = 0, fy = 0, fz = 0;
-      float4 firstpos = make_float4(0, 0, 0, 0);
-      for_children(node, D, L, left, right, range, depth, [&](uint32_t x, uint32_t j) {
-        float4 q;
-        float v;
-        if (x & kLeaf) {
-          q = leaf[x & kIndex];
-          v = q.w;
-        } else {
-          q = __ldcg(cell + x);
-          // the chain of one-child cells from D + 1 down to the child's depth scales by c
-          v = q.w * damp(ndim, depth[x] - D - 1);
-        }
-        if (j == 0) firstpos = q;
-        const float a = fabsf(v);
-        if (!(a > 0.f)) return;  // d3 skips children whose value is 0
-        if (wide) sv += v, sa += a, sx += (double)a * q.x, sy += (double)a * q.y, sz += (double)a * q.z;
-        else fv += v, fa += a, fx += a * q.x, fy += a * q.y, fz += a * q.z;
-      });
-      float4 out;
-      double tv, ta;
-      if (wide) {
-        tv = sv, ta = sa;
-        out = sa > 0 ? make_float4((float)(sx / sa), (float)(sy / sa), (float)(sz / sa), 0.f) : firstpos;
+    const bool wide = D < fp64_depth;
+    double sv = 0, sa = 0, sx = 0, sy = 0, sz = 0;
+    float fv = 0, fa = 0, fx = 0, fy = 0, fz = 0;
+    float4 firstpos = make_float4(0, 0, 0, 0);
+    for (uint32_t j = 0; j < cnt; ++j) {
+      const uint2 m = cmeta[fs + j];
+      const float4 q = __ldcg(cdata + fs + j);
+      float v32 = q.w;  // the centroid weight's value
+      double v = 0;
+      if (m.y == kLeafMark) {
+        if (exact) v = q.w;
       } else {
-        tv = fv, ta = fa;
-        out = fa > 0.f ? make_float4(fx / fa, fy / fa, fz / fa, 0.f) : firstpos;
+        // the chain of one-child cells from D + 1 down to the child's depth scales by c
+        const int cd = (int)(m.y >> 26);
+        v32 *= damp(ndim, cd - D - 1);
+        if (exact) {
+          v = __ldcg(slot64 + fs + j);
+          for (int k = cd - D - 1; k > 0; --k) v *= c1;
+        }
       }
-      out.w = fabs(tv) <= ta * 0x1p-20 ? 0.f : (float)(tv * c1);
-      cell[node] = out;
+      if (j == 0) firstpos = q;
+      const float a = fabsf(v32);
+      if (exact) {
+        // d3 skips children whose value is 0 (or NaN): tested on the bits
+        const unsigned long long b = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+        if (b == 0 || b > 0x7ff0000000000000ull) continue;
+        sv += v;
+      } else {
+        if (!(a > 0.f)) continue;
+        fv += v32;
+      }
+      fa += a;
+      if (wide) sa += a, sx += (double)a * q.x, sy += (double)a * q.y, sz += (double)a * q.z;
+      else fx += a * q.x, fy += a * q.y, fz += a * q.z;
     }
-    if (parent[node] == node) return;  // a graph's root
-    node = parent[node];
+    float4 out;
+    if (wide)
+      out = sa > 0 ? make_float4((float)(sx / sa), (float)(sy / sa), (float)(sz / sa), 0.f) : firstpos;
+    else
+      out = fa > 0.f ? make_float4(fx / fa, fy / fa, fz / fa, 0.f) : firstpos;
+    double val = 0;
+    if (exact) {
+      val = sv * c1;
+      out.w = (float)val;
+      // a residual below FP32's range stays a value the walk does not skip
+      if (val != 0 && out.w == 0.f) out.w = copysignf(1.17549435e-38f, (float)val);
+    } else {
+      out.w = fabsf(fv) <= fa * 0x1p-20f ? 0.f : (float)((double)fv * c1);
+    }
+    if (parent[h] == h) {  // a graph's root: its own slot
+      cdata[seg.graphs ? seg.gid_pos[h] : 0u] = out;
+      return;
+    }
+    const uint32_t rec = head_of[h];
+    const uint32_t p = rec & kCountMask, oct = (rec >> 27) & 15u;
+    if (!(rec & 0x80000000u)) {  // a malformed tree
+      atomicOr(err, FL_ERR_TREE);
+      return;
+    }
+    const uint32_t pfs = first_slot(first, ctot, p, roots);
+    const uint32_t pc = count[p];
+    const uint32_t rank = (uint32_t)__popc(omask[p] & ((1u << oct) - 1u)), slot = pfs + rank;
+    if (rank >= pc || pfs + pc > nslots) {  // a malformed tree
+      atomicOr(err, FL_ERR_TREE);
+      return;
+    }
+    cdata[slot] = out;
+    if (exact) slot64[slot] = val;
+    const uint32_t need = cells_among(cmeta, pfs, pc);
+    // acquire-release: each arrival publishes its cell; the last sees all of them
+    if (cuda::atomic_ref<uint32_t, cuda::thread_scope_device>(arrive[p])
+            .fetch_add(1u, cuda::memory_order_acq_rel) + 1u != need)
+      return;
+    h = p, cnt = pc, fs = pfs, D = depth[p];
   }
 }
 
@@ -794,7 +832,7 @@ __global__ void __launch_bounds__(kThreads) k_slots(
     const uint32_t* __restrict__ count, const uint32_t* __restrict__ first,
     const uint32_t* __restrict__ ctot, const float4* __restrict__ cell,
     const float4* __restrict__ leaf, float4* __restrict__ cdata, uint2* __restrict__ cmeta,
-    uint32_t* err, FlSegs seg) {
+    uint32_t* err, FlSegs seg, bool cells_later) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= 2 * n - 1) return;
   const bool pt = t >= n - 1;
@@ -802,7 +840,7 @@ __global__ void __launch_bounds__(kThreads) k_slots(
   const uint32_t roots = seg.graphs ? (uint32_t)seg.graphs : 1u;
   if (!pt && depth[x] != kGapDepth && parent[x] == x) {  // a graph's root: its own slot
     const uint32_t rs = seg.graphs ? seg.gid_pos[x] : 0u;
-    cdata[rs] = cell[x];
+    if (!cells_later) cdata[rs] = cell[x];
     cmeta[rs] = make_uint2(first_slot(first, ctot, x, roots), count[x] | ((uint32_t)depth[x] << 26));
   }
   const uint32_t rec = head_of[t];
@@ -820,7 +858,7 @@ __global__ void __launch_bounds__(kThreads) k_slots(
     cdata[slot] = leaf[x];
     cmeta[slot] = make_uint2(x, kLeafMark);
   } else {
-    cdata[slot] = cell[x];
+    if (!cells_later) cdata[slot] = cell[x];
     cmeta[slot] = make_uint2(first_slot(first, ctot, x, roots), count[x] | ((uint32_t)depth[x] << 26));
   }
 }
@@ -1445,7 +1483,7 @@ size_t fl_tree_bytes(int64_t n) {
   const size_t blocks = (N + kThreads - 1) / kThreads;
   return align256(4 * m) * 3 + align256(4 * N) + align256(8 * m) + align256(m) +
          align256(4 * m) * 3 + align256(16 * m) + align256(16 * N) + align256(16 * (2 * N + 1)) +
-         align256(8 * (2 * N + 1)) + align256(4 * blocks) + align256(32 * N) +
+         align256(8 * (2 * N + 1)) * 2 + align256(4 * blocks) + align256(32 * N) +
          align256(32 * blocks) + align256(4 * m) + align256(4 * (2 * N)) +
          align256((size_t)fl_walk_slots(n) * kWalkSpillPerWarp * 16) + align256(4) + 256;
 }
@@ -1482,6 +1520,7 @@ void fl_tree_carve(FlTreeBufs* t, void* base, int64_t n, int ndim) {
   t->count = (uint32_t*)take(4 * m);
   t->first = (uint32_t*)take(4 * m);
   t->flag = (uint32_t*)take(4 * m);
+  t->slot64 = (double*)take(8 * (2 * N + 1));
   t->cell = (float4*)take(16 * m);
   t->leaf = (float4*)take(16 * N);
   t->child_data = (float4*)take(16 * (2 * N + 1));
@@ -1585,17 +1624,17 @@ void fl_launch_cells(const FlTreeBufs* t, bool closed, float sign, const float* 
                                            fx_exp, t->cell, segs);
   k_top_u32<<<1, kTopThreads, 0, st>>>(ctot, g);
   *launches += 2;
-  if (!closed) {
-    cudaMemsetAsync(t->flag, 0, 4 * (size_t)m, st);
-    k_cells_climb<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(
-        n, t->ndim, t->left, t->right, t->parent, t->leaf_parent, t->range, t->depth, t->count,
-        t->flag, t->cell, t->leaf, fp64_depth, err);
-    ++*launches;
-  }
   k_slots<<<g2, kThreads, 0, st>>>(n, t->ndim, t->head_of, t->omask, t->parent, t->range,
                                    t->depth, t->count, t->first, ctot, t->cell, t->leaf,
-                                   t->child_data, t->child_meta, err, segs);
+                                   t->child_data, t->child_meta, err, segs, !closed);
   ++*launches;
+  if (!closed) {
+    cudaMemsetAsync(t->flag, 0, 4 * (size_t)m, st);
+    k_cells_up<<<g, kThreads, 0, st>>>(n, t->ndim, t->parent, t->head_of, t->omask, t->depth,
+                                       t->count, t->first, ctot, t->flag, t->child_data,
+                                       t->child_meta, t->slot64, fp64_depth, err, segs);
+    ++*launches;
+  }
 }
 
 void fl_launch_aggregate(const FlTreeBufs* t, const uint64_t* skeys, bool closed, float sign,

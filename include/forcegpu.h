@@ -172,9 +172,9 @@ int32_t fl_buffers(fl_sim* sim, fl_buffer_info* out);
  * tree-walk traversal, 16 or 32, or 1 for one point per warp with the warp's lanes testing up to
  * 32 of its children at once (0, the default: 1 up to 32,768 nodes, else 32); FL_TUNE_CELL_SUMS, how the many-body cells' values
  * and centroids are summed: FL_CELLS_AUTO (default: exact fixed-point prefix sums when the
- * strengths share one sign, else the bottom-up recursion with FP64 sums near the root),
- * FL_CELLS_FP64_TOP (always that recursion) or FL_CELLS_FP32 (the recursion all in FP32, for
- * precision comparisons); FL_TUNE_GRAPHS, 1 (default) to run a block of ticks that fl_enqueue
+ * strengths share one sign, else the bottom-up recursion: d3's FP64 values bit for bit, FP64
+ * centroid sums near the root), FL_CELLS_FP64_TOP (always that recursion) or FL_CELLS_FP32 (the
+ * recursion all in FP32, for precision comparisons); FL_TUNE_GRAPHS, 1 (default) to run a block of ticks that fl_enqueue
  * has seen before (same length, same forces) as one CUDA graph, captured the second time it is
  * seen, or 0 to launch every kernel of every block directly; FL_TUNE_SORT_PASSES, the 8-bit digit
  * passes of the tree's radix sort, from the top of the Morton key (0 = 4, the default: the top
