@@ -179,7 +179,8 @@ struct FlTreeBufs {
   uint8_t* depth;        // [n-1] d3 depth of each internal node's cell
   uint32_t* count;       // [n-1] children of a head (0 for other nodes)
   uint32_t* first;       // [n-1] first child slot of a head
-  uint32_t* flag;        // [n-1] arrivals of each head's child cells (mixed-sign recursion)
+  uint32_t* flag;        // [n] mixed-sign recursion: arrivals of each head's child cells; [n-1] the start count
+  uint32_t* up_list;     // [n-1] mixed-sign recursion: the heads without child cells
   float4* cell;          // [n-1] head: centroid, value at its own depth
   float4* leaf;          // [n] sorted points: position, strength
   float4* child_data;    // [2n] slot: centroid or position, value at own depth / strength
@@ -188,7 +189,7 @@ struct FlTreeBufs {
   void* scan_scratch;
   double* wsum;          // [5n] per sorted point |a|, |a| x, |a| y, |a| z, a; then their prefix sums
   double* wtiles;        // [5 tiles] partial sums of the prefix scan
-  uint32_t* omask;       // [n-1] occupied octants of each head's cell
+  uint32_t* omask;       // [n-1] occupied octants of each head's cell; << 16, those of its child cells
   uint32_t* head_of;     // [2n-1] d3 child: its head | octant << 27 | 1 << 31 (internal, then points)
   uint4* spill;          // the walk stacks' overflow, one region per warp slot of its grid
   uint32_t* work;        // the walk's next group of 32 points to hand out

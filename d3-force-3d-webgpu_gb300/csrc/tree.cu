@@ -541,7 +541,7 @@ __global__ void __launch_bounds__(kThreads) k_frontier(
       if (Dp < levels_of(ndim)) {
         const uint64_t k = skeys[pt ? x : range[2 * x]];
         oct = (uint32_t)(k >> (64 - ndim * (Dp + 1))) & ((1u << ndim) - 1u);
-        atomicOr(omask + h, 1u << oct);
+        atomicOr(omask + h, (1u << oct) | (pt ? 0u : 1u << (16 + oct)));  // cells also above
       }
       rec = h | (oct << 27) | 0x80000000u;
     }
@@ -651,7 +651,8 @@ __device__ __forceinline__ float4 closed_cell(uint32_t i, int ndim, float sign,
 // Whether internal node i heads a d3 cell, and how many d3 children that cell has (its occupied
 // octants; at the deepest level, where the keys are equal, its points); the counts' exclusive
 // prefix within the block (first[]) and the block's total (ctot[]), for the slots. CLOSED (strengths
-// of one sign): a head's cell from the prefix sums too (closed_cell), into cell[].
+// of one sign): a head's cell from the prefix sums too (closed_cell), into cell[]. Otherwise the
+// heads without child cells (where the recursion starts) are listed in up_list[0, *up_count).
 template <bool CLOSED>
 __global__ void __launch_bounds__(kThreads) k_heads(int n, int ndim,
                                                     const uint32_t* __restrict__ parent,
@@ -665,22 +666,43 @@ __global__ void __launch_bounds__(kThreads) k_heads(int n, int ndim,
                                                     const D4* __restrict__ Ptot,
                                                     const float4* __restrict__ leaf,
                                                     const float* __restrict__ cube, int fx_exp,
-                                                    float4* __restrict__ cell, FlSegs seg) {
+                                                    float4* __restrict__ cell, FlSegs seg,
+                                                    uint32_t* __restrict__ up_list,
+                                                    uint32_t* __restrict__ up_count) {
   __shared__ uint32_t s_warp[kThreads / 32];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t c = 0;
+  bool start = false;
   if (i < n - 1) {
     const int D = depth[i];
     if (D != kGapDepth) {
       const uint32_t pa = parent[i];
       const bool head = pa == (uint32_t)i || depth[pa] < D;  // a graph's root, or a deeper cell
-      if (head) c = D >= levels_of(ndim) ? range[2 * i + 1] - range[2 * i] + 1 : __popc(omask[i]);
+      if (head) {
+        if (D >= levels_of(ndim)) {
+          c = range[2 * i + 1] - range[2 * i] + 1;
+          start = true;
+        } else {
+          const uint32_t om = omask[i];
+          c = __popc(om & 0xffffu);
+          start = !(om >> 16);
+        }
+      }
     }
     count[i] = c;
     if (CLOSED && c)
       cell[i] = closed_cell((uint32_t)i, ndim, sign, range, depth, P, Ptot, leaf, cube, fx_exp, seg);
   }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (!CLOSED) {  // one atomic per warp
+    const uint32_t bal = __ballot_sync(FL_FULL, start);
+    if (bal) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(up_count, (uint32_t)__popc(bal));
+      base = __shfl_sync(FL_FULL, base, 0);
+      if (start) up_list[base + __popc(bal & ((1u << lane) - 1u))] = (uint32_t)i;
+    }
+  }
   uint32_t x = c;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -695,77 +717,87 @@ __global__ void __launch_bounds__(kThreads) k_heads(int n, int ndim,
   if (threadIdx.x == kThreads - 1) ctot[blockIdx.x] = before + x;
 }
 
-// The cell children among a head's slots (the rest are points).
-__device__ __forceinline__ uint32_t cells_among(const uint2* __restrict__ cmeta, uint32_t fs,
-                                                uint32_t cnt) {
-  uint32_t k = 0;
-  for (uint32_t j = 0; j < cnt; ++j) k += cmeta[fs + j].y != kLeafMark;
-  return k;
-}
-
 // The recursion itself (strengths of both signs), over the d3 cells from the deepest up, reading
-// each head's children from its slots (k_slots has written the points and every slot's meta):
-// a head whose children are all points starts; a finished cell writes itself into its slot
-// among its parent's children and counts itself in at the parent, and the last of the parent's
-// cell children to arrive combines the parent. So the chain of dependent steps is the d3 depth.
+// each head's children from its slots (k_slots has written the points and every slot's meta).
+// The heads without child cells (k_heads listed them) start, one per thread. A finished cell
+// writes itself into its slot among its parent's children and counts itself in at the parent;
+// the last of the parent's child cells to arrive (their octants are the high half of the
+// parent's octant mask) puts the parent on its block's queue in shared memory, and the block
+// works through the queue a round at a time, one head per thread, until it is empty. So the
+// chain of dependent steps is the d3 depth, and a round's heads sit on consecutive lanes: FP64
+// runs at 2 lanes per clock per SM, and a warp instruction costs its 16 clocks however few of
+// its lanes are active, so heads climbing alone on scattered lanes made this pass FP64-bound.
 // A head combines its children as accumulate() does (src/manyBody.js:42-71). With
 // fp64_depth > 0 every value is d3's FP64 number bit for bit: the children's values summed in
 // slot order, which is d3's octant order (z << 2 | y << 1 | x), a chain of one-child cells
-// scaled by c once per level, the sum scaled by c; each cell's FP64 value rides in slot64 beside
-// its slot. So a cell whose children cancel is skipped (`!quad.value`, src/manyBody.js:74)
-// exactly when d3 skips it: a cancellation can leave d3 an FP64 residual, a value that d3
-// opens like any other. Centroids are weighted by the FP32 values, summed in FP64 above
-// fp64_depth and in FP32 below. fp64_depth 0 runs all of it in FP32 (values within 2^-20 of
-// their children's |values| count as 0), for precision comparisons.
-__global__ void __launch_bounds__(kThreads) k_cells_up(
-    int n, int ndim, const uint32_t* __restrict__ parent, const uint32_t* __restrict__ head_of,
+// scaled by c once per level, the sum scaled by c (c1, d3's Math.sqrt(4 / 2^dims), correctly
+// rounded); each cell's FP64 value rides in slot64 beside its slot. So a cell whose children
+// cancel is skipped (`!quad.value`, src/manyBody.js:74) exactly when d3 skips it: a
+// cancellation can leave d3 an FP64 residual, a value that d3 opens like any other. Centroids
+// are weighted by the FP32 values, summed in FP64 above fp64_depth and in FP32 below.
+// fp64_depth 0 runs all of it in FP32 (values within 2^-20 of their children's |values| count
+// as 0), for precision comparisons.
+constexpr int kUpBatch = 4;
+constexpr uint32_t kNoHead = 0xffffffffu;
+
+// One head of the recursion: combine its children into its cell, write the cell into its slot
+// and count it in at its parent. Returns the parent when this was its last child cell to
+// arrive, else kNoHead (also after a graph's root, and on a malformed tree).
+__device__ __forceinline__ uint32_t cells_up_one(
+    uint32_t h, int n, int ndim, const uint32_t* __restrict__ head_of,
     const uint32_t* __restrict__ omask, const uint8_t* __restrict__ depth,
     const uint32_t* __restrict__ count, const uint32_t* __restrict__ first,
     const uint32_t* __restrict__ ctot, uint32_t* __restrict__ arrive, float4* cdata,
-    const uint2* __restrict__ cmeta, double* slot64, int fp64_depth, uint32_t* err, FlSegs seg) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n - 1) return;
-  uint32_t h = (uint32_t)t;
-  int D = depth[h];
-  uint32_t cnt = D == kGapDepth ? 0u : count[h];
-  if (!cnt) return;  // not a head
-  const int L = levels_of(ndim);
+    const uint2* __restrict__ cmeta, double* slot64, int fp64_depth, double c1, uint32_t* err,
+    const FlSegs& seg) {
   const uint32_t roots = seg.graphs ? (uint32_t)seg.graphs : 1u;
   const uint32_t nslots = 2u * (uint32_t)n + 1u;
-  uint32_t fs = first_slot(first, ctot, h, roots);
+  const bool exact = fp64_depth > 0;
+  const int D = depth[h];
+  const uint32_t cnt = count[h], fs = first_slot(first, ctot, h, roots);
+  // the parent's record: its loads overlap the children's
+  const uint32_t rec = head_of[h];
+  const bool root = !(rec & 0x80000000u);
+  const uint32_t p = rec & kCountMask, oct = (rec >> 27) & 15u;
+  uint32_t pcnt = 0, pfirst = 0, ptot = 0, pmask = 0;
+  if (!root) pcnt = count[p], pfirst = first[p], ptot = ctot[p >> 8], pmask = omask[p];
   if (fs + cnt > nslots) {  // a malformed tree
     atomicOr(err, FL_ERR_TREE);
-    return;
+    return kNoHead;
   }
-  if (D < L && cells_among(cmeta, fs, cnt)) return;  // its last child cell combines it
-  const double c1 = sqrt(4.0 / (double)(1 << ndim));
-  const bool exact = fp64_depth > 0;
-  for (int guard = 0;; ++guard) {
-    if (guard > 64) {
-      atomicOr(err, FL_ERR_TREE);
-      return;
+  const bool wide = D < fp64_depth;
+  double sv = 0, sa = 0, sx = 0, sy = 0, sz = 0;
+  float fv = 0, fa = 0, fx = 0, fy = 0, fz = 0;
+  float4 firstpos = make_float4(0, 0, 0, 0);
+  for (uint32_t j0 = 0; j0 < cnt; j0 += kUpBatch) {
+    uint2 m[kUpBatch];
+    float4 q[kUpBatch];
+    double v64[kUpBatch];
+#pragma unroll
+    for (int k = 0; k < kUpBatch; ++k) {
+      if (j0 + k < cnt) {
+        m[k] = cmeta[fs + j0 + k];
+        q[k] = __ldcg(cdata + fs + j0 + k);
+        v64[k] = exact ? __ldcg(slot64 + fs + j0 + k) : 0.0;  // read for points too, unused
+      }
     }
-    const bool wide = D < fp64_depth;
-    double sv = 0, sa = 0, sx = 0, sy = 0, sz = 0;
-    float fv = 0, fa = 0, fx = 0, fy = 0, fz = 0;
-    float4 firstpos = make_float4(0, 0, 0, 0);
-    for (uint32_t j = 0; j < cnt; ++j) {
-      const uint2 m = cmeta[fs + j];
-      const float4 q = __ldcg(cdata + fs + j);
-      float v32 = q.w;  // the centroid weight's value
+#pragma unroll
+    for (int k = 0; k < kUpBatch; ++k) {
+      if (j0 + k >= cnt) break;
+      float v32 = q[k].w;  // the centroid weight's value
       double v = 0;
-      if (m.y == kLeafMark) {
-        if (exact) v = q.w;
+      if (m[k].y == kLeafMark) {
+        if (exact) v = q[k].w;
       } else {
         // the chain of one-child cells from D + 1 down to the child's depth scales by c
-        const int cd = (int)(m.y >> 26);
+        const int cd = (int)(m[k].y >> 26);
         v32 *= damp(ndim, cd - D - 1);
         if (exact) {
-          v = __ldcg(slot64 + fs + j);
-          for (int k = cd - D - 1; k > 0; --k) v *= c1;
+          v = v64[k];
+          for (int l = cd - D - 1; l > 0; --l) v *= c1;
         }
       }
-      if (j == 0) firstpos = q;
+      if (j0 + k == 0) firstpos = q[k];
       const float a = fabsf(v32);
       if (exact) {
         // d3 skips children whose value is 0 (or NaN): tested on the bits
@@ -777,48 +809,73 @@ __global__ void __launch_bounds__(kThreads) k_cells_up(
         fv += v32;
       }
       fa += a;
-      if (wide) sa += a, sx += (double)a * q.x, sy += (double)a * q.y, sz += (double)a * q.z;
-      else fx += a * q.x, fy += a * q.y, fz += a * q.z;
+      if (wide) sa += a, sx += (double)a * q[k].x, sy += (double)a * q[k].y, sz += (double)a * q[k].z;
+      else fx += a * q[k].x, fy += a * q[k].y, fz += a * q[k].z;
     }
-    float4 out;
-    if (wide)
-      out = sa > 0 ? make_float4((float)(sx / sa), (float)(sy / sa), (float)(sz / sa), 0.f) : firstpos;
-    else
-      out = fa > 0.f ? make_float4(fx / fa, fy / fa, fz / fa, 0.f) : firstpos;
-    double val = 0;
-    if (exact) {
-      val = sv * c1;
-      out.w = (float)val;
-      // a residual below FP32's range stays a value the walk does not skip
-      if (val != 0 && out.w == 0.f) out.w = copysignf(1.17549435e-38f, (float)val);
-    } else {
-      out.w = fabsf(fv) <= fa * 0x1p-20f ? 0.f : (float)((double)fv * c1);
+  }
+  float4 out;
+  if (wide)
+    out = sa > 0 ? make_float4((float)(sx / sa), (float)(sy / sa), (float)(sz / sa), 0.f) : firstpos;
+  else
+    out = fa > 0.f ? make_float4(fx / fa, fy / fa, fz / fa, 0.f) : firstpos;
+  double val = 0;
+  if (exact) {
+    val = sv * c1;
+    out.w = (float)val;
+    // a residual below FP32's range stays a value the walk does not skip
+    if (val != 0 && out.w == 0.f) out.w = copysignf(1.17549435e-38f, (float)val);
+  } else {
+    out.w = fabsf(fv) <= fa * 0x1p-20f ? 0.f : (float)((double)fv * c1);
+  }
+  if (root) {  // a graph's root: its own slot
+    cdata[seg.graphs ? seg.gid_pos[h] : 0u] = out;
+    return kNoHead;
+  }
+  const uint32_t pfs = roots + pfirst + ptot;
+  const uint32_t rank = (uint32_t)__popc(pmask & ((1u << oct) - 1u)), slot = pfs + rank;
+  if (rank >= pcnt || pfs + pcnt > nslots) {  // a malformed tree
+    atomicOr(err, FL_ERR_TREE);
+    return kNoHead;
+  }
+  cdata[slot] = out;
+  if (exact) slot64[slot] = val;
+  // acquire-release: each arrival publishes its cell; the last sees all of them
+  const uint32_t w = cuda::atomic_ref<uint32_t, cuda::thread_scope_device>(arrive[p])
+                         .fetch_add(1u, cuda::memory_order_acq_rel);
+  return w + 1u == (uint32_t)__popc(pmask >> 16) ? p : kNoHead;
+}
+
+__global__ void __launch_bounds__(kThreads) k_cells_up(
+    int n, int ndim, const uint32_t* __restrict__ head_of, const uint32_t* __restrict__ omask,
+    const uint8_t* __restrict__ depth, const uint32_t* __restrict__ count,
+    const uint32_t* __restrict__ first, const uint32_t* __restrict__ ctot,
+    uint32_t* __restrict__ arrive, float4* cdata, const uint2* __restrict__ cmeta,
+    double* slot64, int fp64_depth, double c1, uint32_t* err, FlSegs seg,
+    const uint32_t* __restrict__ up_list, const uint32_t* __restrict__ up_count) {
+  __shared__ uint32_t s_queue[kThreads];
+  __shared__ uint32_t s_len;
+  const uint32_t starts = min(*up_count, (uint32_t)(n - 1));
+  if (blockIdx.x * blockDim.x >= starts) return;  // the whole block
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t h = t < starts ? up_list[t] : kNoHead;
+  for (int round = 0;; ++round) {
+    if (threadIdx.x == 0) s_len = 0;
+    __syncthreads();
+    if (h != kNoHead) {
+      if (round > 64) {  // deeper than any d3 tree: a malformed tree
+        atomicOr(err, FL_ERR_TREE);
+      } else {
+        const uint32_t next = cells_up_one(h, n, ndim, head_of, omask, depth, count, first,
+                                           ctot, arrive, cdata, cmeta, slot64, fp64_depth, c1,
+                                           err, seg);
+        if (next != kNoHead) s_queue[atomicAdd(&s_len, 1u)] = next;
+      }
     }
-    if (parent[h] == h) {  // a graph's root: its own slot
-      cdata[seg.graphs ? seg.gid_pos[h] : 0u] = out;
-      return;
-    }
-    const uint32_t rec = head_of[h];
-    const uint32_t p = rec & kCountMask, oct = (rec >> 27) & 15u;
-    if (!(rec & 0x80000000u)) {  // a malformed tree
-      atomicOr(err, FL_ERR_TREE);
-      return;
-    }
-    const uint32_t pfs = first_slot(first, ctot, p, roots);
-    const uint32_t pc = count[p];
-    const uint32_t rank = (uint32_t)__popc(omask[p] & ((1u << oct) - 1u)), slot = pfs + rank;
-    if (rank >= pc || pfs + pc > nslots) {  // a malformed tree
-      atomicOr(err, FL_ERR_TREE);
-      return;
-    }
-    cdata[slot] = out;
-    if (exact) slot64[slot] = val;
-    const uint32_t need = cells_among(cmeta, pfs, pc);
-    // acquire-release: each arrival publishes its cell; the last sees all of them
-    if (cuda::atomic_ref<uint32_t, cuda::thread_scope_device>(arrive[p])
-            .fetch_add(1u, cuda::memory_order_acq_rel) + 1u != need)
-      return;
-    h = p, cnt = pc, fs = pfs, D = depth[p];
+    __syncthreads();
+    const uint32_t len = s_len;
+    h = threadIdx.x < len ? s_queue[threadIdx.x] : kNoHead;
+    if (len == 0) return;  // block-uniform
+    __syncthreads();  // everyone has its head before the queue is reset
   }
 }
 
@@ -1482,7 +1539,8 @@ size_t fl_tree_bytes(int64_t n) {
   const size_t m = (size_t)(n > 1 ? n - 1 : 1), N = (size_t)(n > 0 ? n : 1);
   const size_t blocks = (N + kThreads - 1) / kThreads;
   return align256(4 * m) * 3 + align256(4 * N) + align256(8 * m) + align256(m) +
-         align256(4 * m) * 3 + align256(16 * m) + align256(16 * N) + align256(16 * (2 * N + 1)) +
+         align256(4 * m) * 3 + align256(4 * (m + 1)) + align256(16 * m) + align256(16 * N) +
+         align256(16 * (2 * N + 1)) +
          align256(8 * (2 * N + 1)) * 2 + align256(4 * blocks) + align256(32 * N) +
          align256(32 * blocks) + align256(4 * m) + align256(4 * (2 * N)) +
          align256((size_t)fl_walk_slots(n) * kWalkSpillPerWarp * 16) + align256(4) + 256;
@@ -1519,7 +1577,8 @@ void fl_tree_carve(FlTreeBufs* t, void* base, int64_t n, int ndim) {
   t->depth = (uint8_t*)take(m);
   t->count = (uint32_t*)take(4 * m);
   t->first = (uint32_t*)take(4 * m);
-  t->flag = (uint32_t*)take(4 * m);
+  t->flag = (uint32_t*)take(4 * (m + 1));
+  t->up_list = (uint32_t*)take(4 * m);
   t->slot64 = (double*)take(8 * (2 * N + 1));
   t->cell = (float4*)take(16 * m);
   t->leaf = (float4*)take(16 * N);
@@ -1614,14 +1673,17 @@ void fl_launch_cells(const FlTreeBufs* t, bool closed, float sign, const float* 
   uint32_t* ctot = static_cast<uint32_t*>(t->scan_scratch);
   const D4* P = reinterpret_cast<const D4*>(t->wsum);
   const D4* Ptot = reinterpret_cast<const D4*>(t->wtiles);
+  // the recursion's start list and its count, and the arrival counts (zeroed)
+  uint32_t* up_count = t->flag + m;
+  if (!closed) cudaMemsetAsync(t->flag, 0, 4 * (size_t)(m + 1), st);
   if (closed)
     k_heads<true><<<g, kThreads, 0, st>>>(n, t->ndim, t->parent, t->range, t->depth, t->omask,
                                           t->count, t->first, ctot, sign, P, Ptot, t->leaf, cube,
-                                          fx_exp, t->cell, segs);
+                                          fx_exp, t->cell, segs, t->up_list, up_count);
   else
     k_heads<false><<<g, kThreads, 0, st>>>(n, t->ndim, t->parent, t->range, t->depth, t->omask,
                                            t->count, t->first, ctot, sign, P, Ptot, t->leaf, cube,
-                                           fx_exp, t->cell, segs);
+                                           fx_exp, t->cell, segs, t->up_list, up_count);
   k_top_u32<<<1, kTopThreads, 0, st>>>(ctot, g);
   *launches += 2;
   k_slots<<<g2, kThreads, 0, st>>>(n, t->ndim, t->head_of, t->omask, t->parent, t->range,
@@ -1629,10 +1691,11 @@ void fl_launch_cells(const FlTreeBufs* t, bool closed, float sign, const float* 
                                    t->child_data, t->child_meta, err, segs, !closed);
   ++*launches;
   if (!closed) {
-    cudaMemsetAsync(t->flag, 0, 4 * (size_t)m, st);
-    k_cells_up<<<g, kThreads, 0, st>>>(n, t->ndim, t->parent, t->head_of, t->omask, t->depth,
-                                       t->count, t->first, ctot, t->flag, t->child_data,
-                                       t->child_meta, t->slot64, fp64_depth, err, segs);
+    // d3's c = Math.sqrt(4 / 2^dims), correctly rounded as IEEE sqrt is on host and device
+    const double c1 = std::sqrt(4.0 / (double)(1 << t->ndim));
+    k_cells_up<<<g, kThreads, 0, st>>>(n, t->ndim, t->head_of, t->omask, t->depth, t->count,
+                                       t->first, ctot, t->flag, t->child_data, t->child_meta,
+                                       t->slot64, fp64_depth, c1, err, segs, t->up_list, up_count);
     ++*launches;
   }
 }
