@@ -87,6 +87,9 @@ def parse():
                    help="ticks queued per enqueue call (a block seen twice runs as a CUDA graph)")
     p.add_argument("--no-autotune", action="store_true",
                    help="keep the default tuning (else fl_autotune picks it before the warm-up)")
+    p.add_argument("--mixed-charges", action="store_true",
+                   help="many-body strengths +20 on every 4th node and -30 on the rest (the cell "
+                        "recursion for strengths of both signs) instead of -30 everywhere")
     p.add_argument("--walk-group", type=int, default=0, choices=[0, 1, 16, 32],
                    help="points per tree-walk traversal (FL_TUNE_WALK_GROUP; 0 = by size)")
     p.add_argument("--precision", action="store_true",
@@ -172,12 +175,12 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def cpu_baseline(xyz, src, dst, n, ticks=2):
+def cpu_baseline(xyz, src, dst, n, ticks=2, mixed=False):
     """The oracle (one core) on a bounded sample: 1 warm + `ticks` timed ticks at full size."""
     import oracle
     o = oracle.OracleSim(n, 3, xyz=xyz)
     o.link(src, dst, distance=30.0)
-    o.manybody(theta=0.9)
+    o.manybody(charges(n, mixed), theta=0.9)
     o.center()
     o.tick(1)
     t0 = time.perf_counter()
@@ -635,13 +638,18 @@ def run_config2(args):
     print(json.dumps(line), flush=True)
 
 
-def plain_forces(n, src, dst, bias, strength):
+def charges(n, mixed=False):
+    """The many-body strengths: -30 (d3's default), or with mixed, +20 on every 4th node."""
+    return np.where(np.arange(n) % 4 == 0, 20.0, -30.0) if mixed else np.full(n, -30.0)
+
+
+def plain_forces(n, src, dst, bias, strength, mixed=False):
     """The benchmark's force list: link (distance 30, d3's default strength and bias), many-body
-    (-30, theta 0.9), center."""
+    (-30, or charges(n, mixed), theta 0.9), center."""
     from forcegpu._lib import desc_from_gpu
     links = {"type": "link", "version": 1, "source": src, "target": dst, "iterations": 1,
              "strengths": strength, "distances": np.full(len(src), 30.0), "bias": bias}
-    charge = {"type": "manyBody", "version": 1, "strengths": np.full(n, -30.0), "distanceMin2": 1.0,
+    charge = {"type": "manyBody", "version": 1, "strengths": charges(n, mixed), "distanceMin2": 1.0,
               "distanceMax2": math.inf, "theta2": 0.81}
     center = {"type": "center", "x": 0, "y": 0, "z": 0, "strength": 1.0}
     return [desc_from_gpu(links, 1, n), desc_from_gpu(charge, 2, n), desc_from_gpu(center, 3, n)]
@@ -683,7 +691,7 @@ def main():
     pos4[:, :3] = xyz
     eng = Engine(local)
     eng.set_nodes(pos4, 3)
-    eng.set_forces(plain_forces(n, src, dst, bias, strength))
+    eng.set_forces(plain_forces(n, src, dst, bias, strength, args.mixed_charges))
     eng.set_seed(12345)
     eng.set_tuning(TUNE_WALK_GROUP, args.walk_group)
     decay = 0.6
@@ -829,7 +837,9 @@ def main():
     line = {"metric": METRIC, "value": ms_tick, "unit": UNIT, "n_gpus": world, "steps": K,
             "warmup": W, "ms_per_step": ms_tick, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": plain_config(n, len(src)),
+            "config": dict(plain_config(n, len(src)),
+                           **({"charges": "+20 on every 4th node, -30 elsewhere"}
+                              if args.mixed_charges else {})),
             "ticks_timed": [W + 1, W + K],
             "preroll": "the same %d ticks twice before the warm-up, from the start state "
                        "(fl_upload_all), so that every tick block runs as a CUDA graph" % (W + K),
@@ -848,7 +858,7 @@ def main():
         line["batched"] = batched_summary(args, local)
         line["served"] = served_summary(args, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        ms_cpu, t = cpu_baseline(xyz, src, dst, n)
+        ms_cpu, t = cpu_baseline(xyz, src, dst, n, mixed=args.mixed_charges)
         line["cpu_baseline"] = {"value": ms_cpu, "unit": UNIT, "cores": 1, "kind": "port",
                                 "sample": "ticks 2-%d of the same 1M-node layout (oracle, FP64, one core)" % (1 + t),
                                 "host_cores": os.cpu_count()}
