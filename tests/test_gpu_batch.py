@@ -33,7 +33,8 @@ def oracle_run(s, dims, ticks):
     o.set_params(alphaDecay=s.alpha_decay, velocityDecay=s.velocity_decay)
     if len(s.source):
         o.link(s.source, s.target, mode=oracle.MODE_JACOBI)
-    o.manybody(theta=s.theta, distanceMin=s.distance_min, distanceMax=s.distance_max)
+    o.manybody(None if s.charge is None else np.asarray(s.charge, float), theta=s.theta,
+               distanceMin=s.distance_min, distanceMax=s.distance_max)
     if s.radii is not None:
         o.collide(np.asarray(s.radii, float), s.collide_strength, s.collide_iterations,
                   oracle.MODE_JACOBI)
@@ -90,6 +91,49 @@ def test_graphs_with_collide_in_a_batch_match_the_oracle(dims):
     for s_, p in zip(specs, got):
         want = oracle_run(s_, dims, ticks)
         assert_close(p, want, 1e-3, tree_outliers(len(p)) + len(p) // 200)
+
+
+def mixed_charges(n):
+    return np.where(np.arange(n) % 4 == 0, 12.0, -20.0)
+
+
+@pytest.mark.parametrize("dims", [2, 3])
+def test_graphs_with_mixed_sign_charges_in_a_batch_match_the_oracle(dims):
+    """A graph whose charges have both signs puts the whole batch on d3's cell recursion (the
+    others' cells too): every graph against the oracle, the mixed ones with distanceMax, where
+    a cell whose children cancel decides whether a near node sees its children."""
+    sizes = [2, 600, 2000, 40, 1500]
+    specs = [spec(n, dims, 400 + i) for i, n in enumerate(sizes)]
+    for i in (1, 2, 4):
+        specs[i].charge = mixed_charges(sizes[i])
+    specs[2].theta, specs[2].distance_min, specs[2].distance_max = 0.7, 2.0, 80.0
+    b = Batch()
+    b.set_graphs(specs, ndim=dims, seed=7)
+    ticks = 2
+    b.run(ticks)
+    got = b.positions()
+    for s_, p in zip(specs, got):
+        want = oracle_run(s_, dims, ticks)
+        assert_close(p, want, 1e-3, tree_outliers(len(p)))
+
+
+def test_a_mixed_charge_graph_alone_and_in_a_mix_agree_bit_for_bit():
+    """The cell recursion keeps each graph's cells its own: a mixed-charge graph alone and among
+    other graphs, 100 ticks, the same bit for bit."""
+    me = spec(1500, 3, 9)
+    me.charge = mixed_charges(1500)
+    others = [spec(n, 3, 50 + i) for i, n in enumerate([700, 2, 2500, 31])]
+    others[0].charge = mixed_charges(700)
+    alone = Batch()
+    alone.set_graphs([me], ndim=3, seed=3)
+    alone.run(100)
+    a = alone.positions()[0]
+    mix = Batch()
+    mix.set_graphs(others[:2] + [me] + others[2:], ndim=3, seed=3)
+    mix.run(100)
+    m = mix.positions()[2]
+    assert np.isfinite(a).all()
+    assert np.array_equal(m, a)
 
 
 @pytest.mark.parametrize("dims", [2, 3])
