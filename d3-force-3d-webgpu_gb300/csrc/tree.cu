@@ -731,7 +731,8 @@ __global__ void __launch_bounds__(kThreads) k_heads(int n, int ndim,
 // fp64_depth > 0 every value is d3's FP64 number bit for bit: the children's values summed in
 // slot order, which is d3's octant order (z << 2 | y << 1 | x), a chain of one-child cells
 // scaled by c once per level, the sum scaled by c (c1, d3's Math.sqrt(4 / 2^dims), correctly
-// rounded); each cell's FP64 value rides in slot64 beside its slot. So a cell whose children
+// rounded); each cell's FP64 value rides in slot64 beside its slot (a point's strength too,
+// converted by k_slots on full warps). So a cell whose children
 // cancel is skipped (`!quad.value`, src/manyBody.js:74) exactly when d3 skips it: a
 // cancellation can leave d3 an FP64 residual, a value that d3 opens like any other. Centroids
 // are weighted by the FP32 values, summed in FP64 above fp64_depth and in FP32 below.
@@ -778,7 +779,7 @@ __device__ __forceinline__ uint32_t cells_up_one(
       if (j0 + k < cnt) {
         m[k] = cmeta[fs + j0 + k];
         q[k] = __ldcg(cdata + fs + j0 + k);
-        v64[k] = exact ? __ldcg(slot64 + fs + j0 + k) : 0.0;  // read for points too, unused
+        v64[k] = exact ? __ldcg(slot64 + fs + j0 + k) : 0.0;
       }
     }
 #pragma unroll
@@ -787,7 +788,7 @@ __device__ __forceinline__ uint32_t cells_up_one(
       float v32 = q[k].w;  // the centroid weight's value
       double v = 0;
       if (m[k].y == kLeafMark) {
-        if (exact) v = q[k].w;
+        v = v64[k];  // the point's strength, as k_slots wrote it
       } else {
         // the chain of one-child cells from D + 1 down to the child's depth scales by c
         const int cd = (int)(m[k].y >> 26);
@@ -889,7 +890,7 @@ __global__ void __launch_bounds__(kThreads) k_slots(
     const uint32_t* __restrict__ count, const uint32_t* __restrict__ first,
     const uint32_t* __restrict__ ctot, const float4* __restrict__ cell,
     const float4* __restrict__ leaf, float4* __restrict__ cdata, uint2* __restrict__ cmeta,
-    uint32_t* err, FlSegs seg, bool cells_later) {
+    uint32_t* err, FlSegs seg, bool cells_later, double* __restrict__ slot64) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= 2 * n - 1) return;
   const bool pt = t >= n - 1;
@@ -912,7 +913,10 @@ __global__ void __launch_bounds__(kThreads) k_slots(
     return;
   }
   if (pt) {
-    cdata[slot] = leaf[x];
+    const float4 l = leaf[x];
+    cdata[slot] = l;
+    // the recursion's FP64 value of the point, converted here on full warps
+    if (slot64) slot64[slot] = (double)l.w;
     cmeta[slot] = make_uint2(x, kLeafMark);
   } else {
     if (!cells_later) cdata[slot] = cell[x];
@@ -1688,7 +1692,8 @@ void fl_launch_cells(const FlTreeBufs* t, bool closed, float sign, const float* 
   *launches += 2;
   k_slots<<<g2, kThreads, 0, st>>>(n, t->ndim, t->head_of, t->omask, t->parent, t->range,
                                    t->depth, t->count, t->first, ctot, t->cell, t->leaf,
-                                   t->child_data, t->child_meta, err, segs, !closed);
+                                   t->child_data, t->child_meta, err, segs, !closed,
+                                   closed || fp64_depth == 0 ? nullptr : t->slot64);
   ++*launches;
   if (!closed) {
     // d3's c = Math.sqrt(4 / 2^dims), correctly rounded as IEEE sqrt is on host and device
