@@ -738,7 +738,9 @@ __global__ void __launch_bounds__(kThreads) k_heads(int n, int ndim,
 // are weighted by the FP32 values, summed in FP64 above fp64_depth and in FP32 below.
 // fp64_depth 0 runs all of it in FP32 (values within 2^-20 of their children's |values| count
 // as 0), for precision comparisons.
-constexpr int kUpBatch = 4;
+// Children whose slots are loaded together: 1 measured fastest at 1M nodes (48 registers, more
+// blocks resident; 2 and 4 children, 60 and 70 registers, were 6 and 20 us slower per tick).
+constexpr int kUpBatch = 1;
 constexpr uint32_t kNoHead = 0xffffffffu;
 
 // One head of the recursion: combine its children into its cell, write the cell into its slot
