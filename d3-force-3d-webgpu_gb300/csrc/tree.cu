@@ -732,12 +732,12 @@ __global__ void __launch_bounds__(kThreads) k_heads(int n, int ndim,
 // slot order, which is d3's octant order (z << 2 | y << 1 | x), a chain of one-child cells
 // scaled by c once per level, the sum scaled by c (c1, d3's Math.sqrt(4 / 2^dims), correctly
 // rounded); each cell's FP64 value rides in slot64 beside its slot (a point's strength too,
-// converted by k_slots on full warps). So a cell whose children
-// cancel is skipped (`!quad.value`, src/manyBody.js:74) exactly when d3 skips it: a
-// cancellation can leave d3 an FP64 residual, a value that d3 opens like any other. Centroids
-// are weighted by the FP32 values, summed in FP64 above fp64_depth and in FP32 below.
-// fp64_depth 0 runs all of it in FP32 (values within 2^-20 of their children's |values| count
-// as 0), for precision comparisons.
+// converted by k_slots on full warps). So a cell whose children cancel is skipped
+// (`!quad.value`, src/manyBody.js:74) exactly when d3 skips it: a cancellation can leave d3 an
+// FP64 residual, a value that d3 opens like any other. Centroids are weighted by the FP32
+// values, summed in FP64 above fp64_depth and in FP32 below. fp64_depth 0 runs all of it in
+// FP32 (values within 2^-20 of their children's |values| count as 0), for precision
+// comparisons.
 // Children whose slots are loaded together: 1 measured fastest at 1M nodes (48 registers, more
 // blocks resident; 2 and 4 children, 60 and 70 registers, were 6 and 20 us slower per tick).
 constexpr int kUpBatch = 1;
